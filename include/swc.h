@@ -1,0 +1,169 @@
+/*
+ * swc.h -- C ABI of the GB300 dual-particle ("virtual particle") SPH pressure
+ * projection.  Drop-in for DualParticleSphLiquid::advance of
+ * skytang0205/sand-water-coupling (Cores/Physics/DualParticleSphLiquid.cpp:112-126)
+ * and for the projection it performs, VirtualParticle::project
+ * (Cores/Structures/VirtualParticle.h:81-87, VirtualParticle.cpp:76-86).
+ *
+ * Conventions
+ *   - One context owns every device buffer of one simulation on one GPU and
+ *     one CUDA stream.  Calls on a context are not re-entrant.
+ *   - Host arrays are FP64, `dim` components per particle, particle-major: the
+ *     layout of the reference's .sav files (Cores/Utilities/IO.h:19-26).  They
+ *     are copied in or out and never retained.
+ *   - Device state is FP32; CG dot products and norms accumulate in FP64.
+ *   - Every call returns an swc_status code.  Nothing exits the process: the
+ *     reference's std::exit(-1) on solver failure (Cores/Solvers/IterativeSolver.h:28-31,35-38)
+ *     becomes SWC_CG_NOT_CONVERGED / SWC_NAN_DETECTED.
+ *   - There is no CPU fallback: without a usable GPU swc_create fails with
+ *     SWC_CUDA_ERROR.
+ */
+#ifndef SWC_H
+#define SWC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWC_API_VERSION 1
+
+typedef enum swc_status {
+    SWC_OK               = 0,
+    SWC_CG_NOT_CONVERGED = 1, /* iteration cap reached above tolerance */
+    SWC_NAN_DETECTED     = 2, /* NaN / breakdown in the solve */
+    SWC_BAD_ARG          = 3,
+    SWC_CUDA_ERROR       = 4,
+    SWC_NOT_INITIALIZED  = 5,
+    SWC_OUT_OF_MEMORY    = 6
+} swc_status;
+
+typedef enum swc_warm_start {
+    SWC_WARM_PREFIX  = 0, /* reference: previous pressure vector by position in the active list */
+    SWC_WARM_NODE    = 1, /* previous pressure of the same lattice node (0 for new nodes) */
+    SWC_WARM_ZERO    = 2,
+    SWC_WARM_LEARNED = 3  /* MLP prediction; falls back to NODE when its initial residual is larger */
+} swc_warm_start;
+
+typedef struct swc_ctx swc_ctx;
+
+/* Scene: replaces the reference constructor DualParticleSphLiquid(StaggeredGrid, radius)
+ * (Cores/Physics/DualParticleSphLiquid.h:27-29) and the members it fixes. */
+typedef struct swc_scene {
+    int32_t dim;             /* 2 or 3 */
+    int32_t enable_gravity;  /* SmthParticleHydrodLiquid::_enableGravity */
+    double  particle_radius; /* r; real and boundary kernel support h = 4 r */
+    double  mass;            /* real particle mass m */
+    double  boundary_mass;   /* reference sets it to m (DualParticleSphLiquid.cpp:86) */
+    double  grid_origin[3];  /* node-grid origin (StaggeredGrid::nodeGrid) */
+    double  grid_spacing;    /* node spacing; virtual kernel support H = 4 * spacing */
+    int32_t grid_size[3];    /* node counts per axis (z ignored in 2D) */
+    int32_t reserved0;
+    double  gravity[3];      /* reference: (0, -9.8, 0) */
+    double  viscosity;       /* div-free Laplacian coefficient (reference 0.01) */
+    double  target_density;  /* <= 0: max rho_i at initialize (reference) */
+    double  kappa;           /* < 0: 1 / packed kernel sum (reference) */
+} swc_scene;
+
+typedef struct swc_solver_opts {
+    double  tolerance;             /* relative residual (reference default 1e-6) */
+    int32_t max_iterations;        /* < 0: 2 * N_v (Eigen default) */
+    int32_t warm_start;            /* swc_warm_start */
+    int32_t check_interval;        /* CG iterations between host convergence checks (0: auto) */
+    int32_t keep_virtual_velocity; /* store vbar_I for swc_get_virtual */
+    int32_t compute_true_residual; /* evaluate |b - A x| / |b| after each solve */
+    int32_t keep_features;         /* keep per-node neighbour counts (learned warm start) */
+    int32_t reserved[2];
+} swc_solver_opts;
+
+typedef struct swc_stats {
+    int64_t n_particles;
+    int64_t n_boundary;
+    int64_t n_virtual;          /* active virtual particles N_v */
+    int32_t active_bricks;
+    int32_t cg_iterations;      /* SpMVs inside the CG loop (Eigen's count is one less on convergence) */
+    double  rel_residual;       /* recursive |r| / |b| at exit */
+    double  true_rel_residual;  /* |b - A x| / |b| (when requested, else -1) */
+    double  rhs_norm;           /* |b| = |D| */
+    double  initial_rel_residual;
+    int32_t warm_start_used;    /* swc_warm_start actually used */
+    int32_t status;
+    double  device_ms;          /* device time of the call (CUDA events) */
+} swc_stats;
+
+/* Defaults: tolerance 1e-6, max_iterations -1, warm start PREFIX. */
+void swc_default_solver_opts(swc_solver_opts * opts);
+const char * swc_status_str(int status);
+const char * swc_last_error(const swc_ctx * ctx);
+
+/* Create / destroy.  Allocates the node-lattice buffers for scene->grid_size. */
+int  swc_create(const swc_scene * scene, const swc_solver_opts * opts, swc_ctx ** out);
+void swc_destroy(swc_ctx * ctx);
+/* Use the caller's cudaStream_t (NULL: the context's own stream). */
+int  swc_set_stream(swc_ctx * ctx, void * cuda_stream);
+int  swc_set_solver_opts(swc_ctx * ctx, const swc_solver_opts * opts);
+
+/* Particle state (SmthParticleHydrodLiquid::_particles / _velocities; addShape and
+ * loadFrame, Cores/Physics/SmthParticleHydrodLiquid.cpp:34-55,124-131). */
+int swc_set_particles(swc_ctx * ctx, const double * pos, const double * vel, int64_t n);
+int swc_get_particles(swc_ctx * ctx, double * pos, double * vel, int64_t n);
+/* Boundary particles with inward normals and velocities
+ * (BoundaryParticles::addSurface, Cores/Structures/SmoothedParticles.cpp:111-155). */
+int swc_set_boundary(swc_ctx * ctx, const double * pos, const double * normals, const double * vel, int64_t nb);
+/* Rigidly rotating part of the boundary: flags[nb] (1 = moving), rotation about the
+ * y axis through `center` at angular velocity omega; applied at every advance. */
+int swc_set_boundary_motion(swc_ctx * ctx, const uint8_t * moving, const double center[3], double omega);
+
+/* DualParticleSphLiquid::initialize (Cores/Physics/DualParticleSphLiquid.cpp:78-110):
+ * rho_i, V_i = m / rho_i, rho0, boundary rho_b / V_b, alpha0 (FP64), kappa. */
+int swc_initialize(swc_ctx * ctx);
+/* DualParticleSphLiquid::advance(dt) (DualParticleSphLiquid.cpp:112-126):
+ * move, rho_i, gravity, viscosity, virtual generation, projection. */
+int swc_advance(swc_ctx * ctx, double dt, swc_stats * stats);
+/* Projection of the current state: rho_i, virtual generation, then
+ * VirtualParticle::project (VirtualParticle.cpp:76-86). */
+int swc_project(swc_ctx * ctx, swc_stats * stats);
+/* SmthParticleHydrodLiquid::getTimeStep (Cores/Physics/SmthParticleHydrodLiquid.h:39-41):
+ * step_rate * 2 r / max |v|. */
+int swc_get_time_step(swc_ctx * ctx, double step_rate, double * dt);
+
+/* Inspection and replay. */
+int swc_get_real_info(swc_ctx * ctx, double * rho, double * vol, int64_t n);
+int swc_set_volumes(swc_ctx * ctx, const double * vol, int64_t n);
+int swc_get_boundary_info(swc_ctx * ctx, double * rho, double * vol, int64_t nb);
+int swc_set_boundary_info(swc_ctx * ctx, const double * rho, const double * vol, int64_t nb);
+int swc_get_scalars(swc_ctx * ctx, double * rho0, double * alpha0, double * kappa);
+int swc_set_scalars(swc_ctx * ctx, double rho0, double alpha0, double kappa);
+int64_t swc_num_virtual(swc_ctx * ctx);
+/* Active virtual particles in reference order (x-fastest over the node grid):
+ * node ids, rho_I, V_I, vbar_I (n x dim; needs keep_virtual_velocity), D_I,
+ * alpha_hat_I, p_I.  Any pointer may be NULL.  capacity >= swc_num_virtual. */
+int swc_get_virtual(swc_ctx * ctx, int64_t * node_id, double * rho, double * vol, double * vbar, double * div,
+                    double * alpha_hat, double * pressure, int64_t capacity);
+/* Pressure vector (reference order) used as the next PREFIX warm start. */
+int swc_set_pressure(swc_ctx * ctx, const double * p, int64_t n);
+/* y = A x with the operator of the last projection (reference order, length N_v). */
+int swc_apply_operator(swc_ctx * ctx, const double * x, double * y, int64_t n);
+
+/* Device time of the kernels of the last advance/project by phase (ms):
+ * [0] binning, [1] densities, [2] forces, [3] virtual generation (gather +
+ * compaction + alpha_hat), [4] warm start, [5] CG, [6] pressure gradient,
+ * [7] export.  Requires swc_set_profiling(ctx, 1). */
+int swc_set_profiling(swc_ctx * ctx, int on);
+int swc_get_phase_times(swc_ctx * ctx, double * ms, int n);
+/* Times `reps` back-to-back launches of one kernel on the live state with CUDA
+ * events (0: CG SpMV, 1: CG update, 2: virtual gather, 3: pressure gradient,
+ * 4: density, 5: forces); writes the mean ms per launch. */
+int swc_time_kernel(swc_ctx * ctx, int which, int reps, double * mean_ms);
+
+/* Pinned host memory helpers for callers that stream state every step. */
+void * swc_host_alloc(size_t bytes);
+void   swc_host_free(void * p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SWC_H */

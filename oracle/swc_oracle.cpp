@@ -1,0 +1,717 @@
+// swc_oracle.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// CPU FP64 restatement of the dual-particle ("virtual particle") SPH pressure
+// projection of skytang0205/sand-water-coupling.  It exists to check the GPU
+// product: only the tests, the smoke check and the CPU-baseline leg of the
+// benchmark load it.  The product never links or calls it.
+//
+// Parity status: the reference cannot be compiled here (Eigen and yaml-cpp are
+// absent) and ships no tests, fixtures or golden vectors, so this oracle is
+// pinned only by analytic known answers (kernel normalisation, packed-lattice
+// kernel sums, lattice neighbour counts, operator identities) -- "parity
+// unpinned" against an executable of the reference.  CG iteration counts
+// depend on Eigen's reduction order (Eigen version unpinned by the reference).
+//
+// Every function cites the reference file:line it restates (paths relative to
+// the reference project root).  Reference quirks are kept on purpose:
+//   * V_i = m / rho_i is computed once in initialize and then travels with the
+//     particle id (Cores/Physics/DualParticleSphLiquid.cpp:88-89).
+//   * rho_I uses the virtual kernel W_H but the real searcher (radius h), so W_H
+//     is truncated at h (Cores/Structures/VirtualParticle.cpp:18-27).
+//   * gradientKernel(d) = -W'(|d|) d/|d|  (Cores/Structures/SmoothedParticles.h:96-98).
+//   * eta = 1e-6 absolute in alpha_IJ (VirtualParticle.cpp:157).
+//   * the CG warm start keeps the stale prefix of the previous pressure vector
+//     (Cores/Structures/ParticlesBasedData.h:25-29 via VirtualParticle.cpp:95).
+//   * virtual nodes are activated when the real-particle weight exceeds 1e-6
+//     (VirtualParticle.cpp:56).
+#include <algorithm>
+#include <array>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <numbers>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+using ullong = unsigned long long;
+
+// Cubic-spline kernel of SmoothedParticles (Cores/Structures/SmoothedParticles.h:60-72,
+// coefficients Cores/Structures/SmoothedParticles.cpp:17-22).
+struct Kernel {
+    double radius, h, h2, inv_h, inv_h2, c0, c1;
+    Kernel() = default;
+    Kernel(double r, int dim, double rate = 4) {
+        radius = r;
+        h      = r * rate;
+        h2     = h * h;
+        inv_h  = 1 / h;
+        inv_h2 = 1 / h2;
+        c0     = std::numbers::inv_pi * inv_h2 * (dim == 2 ? 40.0 / 7 : 8 * inv_h);
+        c1     = 6 * inv_h * c0;
+    }
+    double W(double dist) const {
+        const double x = dist * inv_h;
+        if (x < .5) return c0 * (6 * x * x * (x - 1) + 1);
+        if (x < 1) return c0 * 2 * (1 - x) * (1 - x) * (1 - x);
+        return 0;
+    }
+    double dW(double dist) const {
+        const double x = dist * inv_h;
+        if (x < .5) return c1 * x * (3 * x - 2);
+        if (x < 1) return c1 * (1 - x) * (x - 1);
+        return 0;
+    }
+    // SmoothedParticles::getPackedKernelSum (Cores/Structures/SmoothedParticles.cpp:74-80).
+    double packedSum(int dim) const {
+        if (dim == 2) return W(0) + W(radius * 2) * 6 + W(radius * 2 * std::numbers::sqrt3) * 6;
+        return W(0) + W(radius * 2) * 12 + W(radius * 2 * std::numbers::sqrt2) * 6
+            + W(radius * 2 * std::numbers::sqrt3) * 24;
+    }
+};
+
+template<int D> using Vec = std::array<double, D>;
+
+template<int D> inline double dot(const Vec<D> & a, const Vec<D> & b) {
+    double s = 0;
+    for (int k = 0; k < D; k++) s += a[k] * b[k];
+    return s;
+}
+template<int D> inline Vec<D> sub(const Vec<D> & a, const Vec<D> & b) {
+    Vec<D> c;
+    for (int k = 0; k < D; k++) c[k] = a[k] - b[k];
+    return c;
+}
+template<int D> inline double norm(const Vec<D> & a) { return std::sqrt(dot<D>(a, a)); }
+
+// -grad W as SmoothedParticles::gradientKernel (SmoothedParticles.h:96-98); a zero
+// offset normalises to zero (and W'(0) = 0 anyway).
+template<int D> inline Vec<D> gradKernel(const Kernel & k, const Vec<D> & d) {
+    const double r = norm<D>(d);
+    Vec<D> g{};
+    if (r > 0) {
+        const double s = -k.dW(r);
+        for (int a = 0; a < D; a++) g[a] = s * (d[a] / r);
+    }
+    return g;
+}
+
+// Spatial hash with 2N buckets and a 3^D cell query
+// (Cores/Structures/ParticlesNearbySearcher.h:37-74, ParticlesNearbySearcher.cpp:10-35,
+// Grid::getQuadraticLower Cores/Structures/Grid.h:70, quadraticNearbyDataPoints Grid.cpp:26-45).
+// The visited set is every j with |x_j - x|^2 < h^2 (strict).
+template<int D> struct HashGrid {
+    static constexpr ullong kP0 = 73856093, kP1 = 19349663, kP2 = 83492791;
+    double h = 1, inv_h = 1, h2 = 1;
+    std::vector<std::vector<int>> buckets;
+
+    void setRadius(double kr) { h = kr, inv_h = 1 / kr, h2 = kr * kr; }
+    std::array<int, D> lower(const Vec<D> & p) const {
+        std::array<int, D> c;
+        for (int a = 0; a < D; a++) c[a] = int(std::floor(p[a] * inv_h - 0.5));
+        return c;
+    }
+    int key(const std::array<int, D> & c) const {
+        ullong v = kP0 * ullong(c[0]) | kP1 * ullong(c[1]);
+        if constexpr (D == 3) v |= kP2 * ullong(c[2]);
+        return int(v % ullong(buckets.size()));
+    }
+    void reset(const std::vector<Vec<D>> & pos) {
+        buckets.assign(pos.size() * 2, {});
+        for (int i = 0; i < int(pos.size()); i++) {
+            auto c = lower(pos[i]);
+            for (int a = 0; a < D; a++) c[a] += 1;
+            buckets[key(c)].push_back(i);
+        }
+    }
+    template<class F> void forEach(const std::vector<Vec<D>> & pos, const Vec<D> & q, F && f) const {
+        if (buckets.empty()) return;
+        constexpr int K = D == 2 ? 9 : 27;
+        std::array<int, K> keys;
+        const auto lo = lower(q);
+        int n = 0;
+        if constexpr (D == 2) {
+            for (int j = 0; j < 3; j++)
+                for (int i = 0; i < 3; i++) keys[n++] = key({lo[0] + i, lo[1] + j});
+        } else {
+            for (int k = 0; k < 3; k++)
+                for (int j = 0; j < 3; j++)
+                    for (int i = 0; i < 3; i++) keys[n++] = key({lo[0] + i, lo[1] + j, lo[2] + k});
+        }
+        std::sort(keys.begin(), keys.end());
+        for (int t = 0; t < K; t++) {
+            if (t && keys[t] == keys[t - 1]) continue;
+            for (const int j : buckets[keys[t]]) {
+                const auto d = sub<D>(pos[j], q);
+                if (dot<D>(d, d) < h2) f(j, pos[j]);
+            }
+        }
+    }
+};
+
+struct Params {
+    int32_t dim;
+    int32_t enable_gravity;
+    double  particle_radius;
+    double  mass;
+    double  boundary_mass;
+    double  grid_origin[3];
+    double  grid_spacing;
+    int32_t grid_size[3];
+    int32_t max_iterations;
+    double  gravity[3];
+    double  viscosity;
+    double  target_density;  // <= 0: max rho_i at initialize (reference behaviour)
+    double  kappa;           // < 0: 1 / packed kernel sum (reference behaviour)
+    double  tolerance;
+};
+
+// Deterministic FP64 sum: fixed 4096-element blocks, independent of thread count.
+inline double blockedSum(const std::vector<double> & t) {
+    const size_t B = 4096, nb = (t.size() + B - 1) / B;
+    std::vector<double> part(nb, 0.0);
+#pragma omp parallel for schedule(static)
+    for (long long b = 0; b < (long long) nb; b++) {
+        double s = 0;
+        const size_t e = std::min(t.size(), size_t(b + 1) * B);
+        for (size_t i = size_t(b) * B; i < e; i++) s += t[i];
+        part[b] = s;
+    }
+    double s = 0;
+    for (double v : part) s += v;
+    return s;
+}
+
+template<int D> struct Oracle {
+    Params P{};
+    Kernel Kh, KH;  // real/boundary kernel (radius h) and virtual kernel (radius H)
+
+    std::vector<Vec<D>> x, v;  // real particles
+    std::vector<double> rho, vol;
+    std::vector<Vec<D>> xb, nb, vb;  // boundary particles
+    std::vector<double> rhob, volb;
+    std::vector<Vec<D>> xv;  // virtual particles (active nodes in x-fastest order)
+    std::vector<int64_t> node;
+    std::vector<double> rhov, volv, div, alphaHat, pres;
+    std::vector<Vec<D>> vbar;
+    std::vector<int64_t> rowStart;
+    std::vector<int32_t> col;
+    std::vector<double>  val;
+
+    HashGrid<D> sReal, sBnd, sVirt;
+    double rho0 = 0, alpha0 = -1e6, kappa = 0;
+    int cgIters = 0, cgEigenIters = 0, status = 0;
+    double cgRelRes = 0, rhsNorm = 0;
+
+    void setup(const Params & p) {
+        P = p;
+        Kh = Kernel(P.particle_radius, D);
+        KH = Kernel(P.grid_spacing, D);
+        sReal.setRadius(Kh.h);
+        sBnd.setRadius(Kh.h);
+        sVirt.setRadius(KH.h);
+    }
+
+    Vec<D> nodePos(const std::array<int64_t, D> & k) const {
+        Vec<D> p;
+        for (int a = 0; a < D; a++) p[a] = P.grid_origin[a] + double(k[a]) * P.grid_spacing;
+        return p;
+    }
+
+    // SmoothedParticles::computeDensities (SmoothedParticles.cpp:25-31, getNeighborWeight :48-54).
+    void computeRealDensities() {
+        rho.assign(x.size(), 0);
+#pragma omp parallel for schedule(dynamic, 256)
+        for (long long i = 0; i < (long long) x.size(); i++) {
+            double s = 0;
+            sReal.forEach(x, x[i], [&](int, const Vec<D> & pj) { s += Kh.W(norm<D>(sub<D>(x[i], pj))); });
+            rho[i] = P.mass * s;
+        }
+    }
+
+    // SmthParticleHydrodLiquid::moveParticles (Cores/Physics/SmthParticleHydrodLiquid.cpp:72-82),
+    // no colliders are registered for the dual-particle liquid.
+    void moveParticles(double dt) {
+#pragma omp parallel for
+        for (long long i = 0; i < (long long) x.size(); i++)
+            for (int a = 0; a < D; a++) x[i][a] += v[i][a] * dt;
+        sReal.reset(x);
+        computeRealDensities();
+    }
+
+    // applyExternalForces (SmthParticleHydrodLiquid.cpp:84-88); gravity vector is a
+    // parameter (the reference subtracts 9.8 dt from component 1).
+    void applyExternalForces(double dt) {
+        if (!P.enable_gravity) return;
+#pragma omp parallel for
+        for (long long i = 0; i < (long long) x.size(); i++)
+            for (int a = 0; a < D; a++) v[i][a] += P.gravity[a] * dt;
+    }
+
+    // applyViscosityForce (SmthParticleHydrodLiquid.cpp:90-98) with
+    // ParticlesBasedVectorField::divFreeLaplacianAtDataPoint (ParticlesBasedVectorField.cpp:56-69).
+    void applyViscosityForce(double dt) {
+        if (P.viscosity == 0) return;
+        std::vector<Vec<D>> nv = v;
+#pragma omp parallel for schedule(dynamic, 256)
+        for (long long i = 0; i < (long long) x.size(); i++) {
+            Vec<D> lapl{};
+            sReal.forEach(x, x[i], [&](int j, const Vec<D> & pj) {
+                const auto dp = sub<D>(pj, x[i]);
+                bool any      = false;
+                for (int a = 0; a < D; a++) any |= dp[a] != 0;
+                if (!any) return;
+                const double s = dot<D>(sub<D>(v[j], v[i]), dp) / dot<D>(dp, dp);
+                const auto   g = gradKernel<D>(Kh, dp);
+                for (int a = 0; a < D; a++) lapl[a] += s * g[a] / rho[j];
+            });
+            for (int a = 0; a < D; a++) nv[i][a] += P.viscosity * (lapl[a] * 2 * (D + 2.0) * P.mass) * dt;
+        }
+        v.swap(nv);
+    }
+
+    // VirtualParticle::generateParticles (Cores/Structures/VirtualParticle.cpp:45-62):
+    // weight over every node of the node grid, x-fastest compaction (Grid.cpp:231-244),
+    // then computeInfo (:18-38).
+    void generateParticles() {
+        const int64_t nx = P.grid_size[0], ny = P.grid_size[1], nz = D == 3 ? P.grid_size[2] : 1;
+        const int64_t total = nx * ny * nz;
+        std::vector<double> w(total, 0);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long long id = 0; id < (long long) total; id++) {
+            std::array<int64_t, D> k;
+            k[0] = id % nx;
+            k[1] = (id / nx) % ny;
+            if constexpr (D == 3) k[2] = id / (nx * ny);
+            const auto pI = nodePos(k);
+            double s = 0;
+            sReal.forEach(x, pI, [&](int, const Vec<D> & pj) { s += Kh.W(norm<D>(sub<D>(pI, pj))); });
+            w[id] = s;
+        }
+        xv.clear();
+        node.clear();
+        for (int64_t id = 0; id < total; id++)
+            if (w[id] > 1e-6) {
+                std::array<int64_t, D> k;
+                k[0] = id % nx;
+                k[1] = (id / nx) % ny;
+                if constexpr (D == 3) k[2] = id / (nx * ny);
+                xv.push_back(nodePos(k));
+                node.push_back(id);
+            }
+        sVirt.reset(xv);
+        const size_t n = xv.size();
+        rhov.assign(n, 0);
+        volv.assign(n, 0);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long long I = 0; I < (long long) n; I++) {
+            double r = 0, V = 0;
+            sReal.forEach(x, xv[I], [&](int j, const Vec<D> & pj) {
+                const double d = norm<D>(sub<D>(xv[I], pj));
+                r += KH.W(d);  // virtual kernel over the real searcher (truncated at h)
+                V += vol[j] * vol[j] * Kh.W(d);
+            });
+            rhov[I] = r * P.mass;
+            volv[I] = V;
+        }
+    }
+
+    // VirtualParticle::calculateCoef (VirtualParticle.cpp:149-169), stored row-wise with
+    // duplicates merged and columns ascending (the column order Eigen's setFromTriplets gives).
+    void calculateCoef(double a0) {
+        const size_t n = xv.size();
+        std::vector<std::vector<std::pair<int, double>>> rows(n);
+        alphaHat.assign(n, 0);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long long I = 0; I < (long long) n; I++) {
+            double sum = 0;
+            auto & row = rows[I];
+            sVirt.forEach(xv, xv[I], [&](int J, const Vec<D> & pJ) {
+                const double r = norm<D>(sub<D>(xv[I], pJ));
+                const double a = 2. * volv[J] * KH.dW(r) / (r + 1e-6);
+                sum -= a;
+                row.push_back({J, a});
+            });
+            const double dg = std::max(sum, a0);
+            row.push_back({int(I), dg});
+            std::sort(row.begin(), row.end(), [](auto & l, auto & r) { return l.first < r.first; });
+            size_t o = 0;
+            for (size_t t = 0; t < row.size(); t++) {
+                if (o && row[o - 1].first == row[t].first) row[o - 1].second += row[t].second;
+                else row[o++] = row[t];
+            }
+            row.resize(o);
+            alphaHat[I] = dg;
+        }
+        rowStart.assign(n + 1, 0);
+        for (size_t I = 0; I < n; I++) rowStart[I + 1] = rowStart[I] + int64_t(rows[I].size());
+        col.resize(rowStart[n]);
+        val.resize(rowStart[n]);
+#pragma omp parallel for
+        for (long long I = 0; I < (long long) n; I++) {
+            int64_t o = rowStart[I];
+            for (auto & e : rows[I]) col[o] = e.first, val[o] = e.second, o++;
+        }
+    }
+
+    void spmv(const std::vector<double> & in, std::vector<double> & out) const {
+        const size_t n = xv.size();
+        out.resize(n);
+#pragma omp parallel for schedule(static)
+        for (long long I = 0; I < (long long) n; I++) {
+            double s = 0;
+            for (int64_t e = rowStart[I]; e < rowStart[I + 1]; e++) s += val[e] * in[col[e]];
+            out[I] = s;
+        }
+    }
+
+    double vdot(const std::vector<double> & a, const std::vector<double> & b) const {
+        std::vector<double> t(a.size());
+#pragma omp parallel for schedule(static)
+        for (long long i = 0; i < (long long) a.size(); i++) t[i] = a[i] * b[i];
+        return blockedSum(t);
+    }
+
+    // IterativeSolver::solve (Cores/Solvers/IterativeSolver.h:21-40): textbook
+    // Hestenes-Stiefel CG, identity preconditioner, warm start from `pres`,
+    // tolerance max(tol, eps/|b|), relative test |r|^2 < tol^2 |b|^2, at most
+    // 2n iterations by default.  Failure returns status 1 instead of exit(-1).
+    void solve() {
+        const size_t n = xv.size();
+        auto & xx = pres;
+        const auto & b = div;
+        const double bb = vdot(b, b);
+        rhsNorm = std::sqrt(bb);
+        cgIters = cgEigenIters = 0;
+        status = 0;
+        if (n == 0) { cgRelRes = 0; return; }
+        if (bb == 0) {
+            std::fill(xx.begin(), xx.end(), 0.0);
+            cgRelRes = 0;
+            return;
+        }
+        const double tol = std::max(P.tolerance, std::numeric_limits<double>::epsilon() / rhsNorm);
+        const int64_t maxIt = P.max_iterations >= 0 ? P.max_iterations : 2 * int64_t(n);
+        const double threshold = std::max(tol * tol * bb, std::numeric_limits<double>::min());
+        std::vector<double> r(n), q(n), p(n);
+        spmv(xx, q);
+        for (size_t i = 0; i < n; i++) r[i] = b[i] - q[i];
+        double rr = vdot(r, r);
+        if (rr < threshold) { cgRelRes = std::sqrt(rr / bb); return; }
+        p = r;
+        double absNew = rr;
+        int64_t it = 0;
+        int spmvs = 0;
+        while (it < maxIt) {
+            spmv(p, q);
+            spmvs++;
+            const double alpha = absNew / vdot(p, q);
+#pragma omp parallel for schedule(static)
+            for (long long i = 0; i < (long long) n; i++) {
+                xx[i] += alpha * p[i];
+                r[i] -= alpha * q[i];
+            }
+            rr = vdot(r, r);
+            if (rr < threshold) break;
+            const double absOld = absNew;
+            absNew = rr;
+            const double beta = absNew / absOld;
+#pragma omp parallel for schedule(static)
+            for (long long i = 0; i < (long long) n; i++) p[i] = r[i] + beta * p[i];
+            it++;
+        }
+        cgEigenIters = int(it);
+        cgIters = spmvs;
+        cgRelRes = std::sqrt(rr / bb);
+        status = cgRelRes <= tol ? 0 : 1;
+    }
+
+    // VirtualParticle::calculateVelocity (VirtualParticle.cpp:137-147) and calculateDiv
+    // (:172-201) with ParticlesBasedVectorField::operator()/divergence
+    // (ParticlesBasedVectorField.cpp:5-21) and getBiasWeight/getBiasGradient
+    // (SmoothedParticles.cpp:56-72).
+    void buildRhs() {
+        const size_t n = xv.size();
+        vbar.assign(n, Vec<D>{});
+        div.assign(n, 0);
+        const double mb = P.boundary_mass;
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long long I = 0; I < (long long) n; I++) {
+            const auto & pI = xv[I];
+            Vec<D> velR{}, velB{}, gR{}, gB{};
+            double bwR = 0, bwB = 0, divR = 0, divB = 0;
+            sReal.forEach(x, pI, [&](int j, const Vec<D> & pj) {
+                const auto d = sub<D>(pI, pj);
+                const double w = Kh.W(norm<D>(d));
+                for (int a = 0; a < D; a++) velR[a] += v[j][a] * w / rho[j];
+                bwR += vol[j] * w;
+                const auto g = gradKernel<D>(Kh, d);
+                divR += dot<D>(v[j], g) * vol[j];
+                for (int a = 0; a < D; a++) gR[a] += vol[j] * g[a];
+            });
+            sBnd.forEach(xb, pI, [&](int j, const Vec<D> & pj) {
+                const auto d = sub<D>(pI, pj);
+                const double w = Kh.W(norm<D>(d));
+                for (int a = 0; a < D; a++) velB[a] += vb[j][a] * w / rhob[j];
+                bwB += volb[j] * w;
+                const auto g = gradKernel<D>(Kh, d);
+                divB += dot<D>(vb[j], g) * volb[j];
+                for (int a = 0; a < D; a++) gB[a] += volb[j] * g[a];
+            });
+            const double den = bwR + bwB + 1e-6;
+            Vec<D> vb_;
+            for (int a = 0; a < D; a++) vb_[a] = (velR[a] * P.mass + velB[a] * mb) / den;
+            vbar[I] = vb_;
+            div[I] = divR - dot<D>(vb_, gR) + divB - dot<D>(vb_, gB)
+                - kappa * std::max(rhov[I] - rho0, 0.) / rho0;
+        }
+    }
+
+    // VirtualParticle::applyPressureGradient (VirtualParticle.cpp:111-134).
+    void applyPressureGradient() {
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long long i = 0; i < (long long) x.size(); i++) {
+            const auto & pi = x[i];
+            Vec<D> f{};
+            sVirt.forEach(xv, pi, [&](int J, const Vec<D> & pJ) {
+                const auto g = gradKernel<D>(KH, sub<D>(pi, pJ));
+                for (int a = 0; a < D; a++) f[a] += volv[J] * pres[J] * g[a];
+            });
+            sBnd.forEach(xb, pi, [&](int j, const Vec<D> & pj) {
+                const double vn = std::min(dot<D>(nb[j], sub<D>(v[i], vb[j])), 0.);
+                const double w  = Kh.W(norm<D>(sub<D>(pi, pj)));
+                for (int a = 0; a < D; a++) f[a] -= volb[j] * vn * nb[j][a] * w;
+            });
+            for (int a = 0; a < D; a++) v[i][a] += f[a];
+        }
+    }
+
+    // VirtualParticle::project / buildLinearSystem (VirtualParticle.cpp:76-103).
+    void project() {
+        pres.resize(xv.size(), 0.0);  // stale-prefix warm start
+        buildRhs();
+        calculateCoef(alpha0);
+        solve();
+        applyPressureGradient();
+    }
+
+    // DualParticleSphLiquid::initialize (Cores/Physics/DualParticleSphLiquid.cpp:78-110);
+    // the boundary set is supplied by the scene instead of the hard-coded box shell.
+    void initialize() {
+        sReal.reset(x);
+        computeRealDensities();
+        vol.resize(x.size());
+        for (size_t i = 0; i < x.size(); i++) vol[i] = P.mass / rho[i];
+        rho0 = 0;
+        for (double r : rho) rho0 = std::max(rho0, r);
+        if (P.target_density > 0) rho0 = P.target_density;
+        sBnd.reset(xb);
+        rhob.assign(xb.size(), 0);
+        volb.assign(xb.size(), 0);
+#pragma omp parallel for schedule(dynamic, 256)
+        for (long long j = 0; j < (long long) xb.size(); j++) {
+            double s = 0;
+            sBnd.forEach(xb, xb[j], [&](int, const Vec<D> & pk) { s += Kh.W(norm<D>(sub<D>(xb[j], pk))); });
+            rhob[j] = P.boundary_mass * s;
+            volb[j] = P.boundary_mass / rhob[j];
+        }
+        // VirtualParticle::setAlpha (VirtualParticle.cpp:64-73): clamp off, alpha0 = max diagonal.
+        generateParticles();
+        calculateCoef(-1e6);
+        alpha0 = -1e6;
+        for (double a : alphaHat) alpha0 = std::max(alpha0, a);
+        kappa = P.kappa >= 0 ? P.kappa : 1. / Kh.packedSum(D);
+        pres.clear();
+    }
+
+    // DualParticleSphLiquid::advance (DualParticleSphLiquid.cpp:112-126).
+    void advance(double dt) {
+        moveParticles(dt);
+        applyExternalForces(dt);
+        applyViscosityForce(dt);
+        generateParticles();
+        project();
+    }
+};
+
+struct Handle {
+    int dim;
+    Oracle<2> o2;
+    Oracle<3> o3;
+};
+
+template<int D> void loadVecs(std::vector<Vec<D>> & dst, const double * src, int64_t n) {
+    dst.resize(n);
+    for (int64_t i = 0; i < n; i++)
+        for (int a = 0; a < D; a++) dst[i][a] = src ? src[i * D + a] : 0.0;
+}
+template<int D> void storeVecs(const std::vector<Vec<D>> & src, double * dst) {
+    for (size_t i = 0; i < src.size(); i++)
+        for (int a = 0; a < D; a++) dst[i * D + a] = src[i][a];
+}
+
+}  // namespace orc
+
+using orc::Handle;
+
+#define DISPATCH(h, ...)                                                                                              \
+    do {                                                                                                               \
+        if ((h)->dim == 2) {                                                                                           \
+            auto & O = (h)->o2;                                                                                        \
+            constexpr int D = 2;                                                                                       \
+            (void) D;                                                                                                  \
+            __VA_ARGS__;                                                                                               \
+        } else {                                                                                                       \
+            auto & O = (h)->o3;                                                                                        \
+            constexpr int D = 3;                                                                                       \
+            (void) D;                                                                                                  \
+            __VA_ARGS__;                                                                                               \
+        }                                                                                                              \
+    } while (0)
+
+extern "C" {
+
+Handle * orc_create(const orc::Params * p) {
+    if (!p || (p->dim != 2 && p->dim != 3)) return nullptr;
+    auto h = new Handle();
+    h->dim = p->dim;
+    DISPATCH(h, O.setup(*p));
+    return h;
+}
+void orc_destroy(Handle * h) { delete h; }
+int orc_num_threads() {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void) n;
+#endif
+}
+
+void orc_set_particles(Handle * h, int64_t n, const double * x, const double * v) {
+    DISPATCH(h, { orc::loadVecs<D>(O.x, x, n); orc::loadVecs<D>(O.v, v, n); });
+}
+void orc_get_particles(Handle * h, double * x, double * v) {
+    DISPATCH(h, { if (x) orc::storeVecs<D>(O.x, x); if (v) orc::storeVecs<D>(O.v, v); });
+}
+void orc_set_boundary(Handle * h, int64_t n, const double * x, const double * nrm, const double * v) {
+    DISPATCH(h, {
+        orc::loadVecs<D>(O.xb, x, n);
+        orc::loadVecs<D>(O.nb, nrm, n);
+        orc::loadVecs<D>(O.vb, v, n);
+    });
+}
+void orc_initialize(Handle * h) { DISPATCH(h, O.initialize()); }
+void orc_advance(Handle * h, double dt) { DISPATCH(h, O.advance(dt)); }
+void orc_move_and_forces(Handle * h, double dt) {
+    DISPATCH(h, { O.moveParticles(dt); O.applyExternalForces(dt); O.applyViscosityForce(dt); });
+}
+// Projection of the current state: rho_i from current positions, virtual generation,
+// then project (the second half of advance).
+void orc_project(Handle * h) {
+    DISPATCH(h, {
+        O.sReal.reset(O.x);
+        O.computeRealDensities();
+        O.generateParticles();
+        O.project();
+    });
+}
+void orc_compute_densities(Handle * h) { DISPATCH(h, { O.sReal.reset(O.x); O.computeRealDensities(); }); }
+
+// Scalars: rho0, alpha0, kappa.
+void orc_get_scalars(Handle * h, double * out3) { DISPATCH(h, { out3[0] = O.rho0; out3[1] = O.alpha0; out3[2] = O.kappa; }); }
+void orc_set_scalars(Handle * h, const double * in3) { DISPATCH(h, { O.rho0 = in3[0]; O.alpha0 = in3[1]; O.kappa = in3[2]; }); }
+void orc_get_real_info(Handle * h, double * rho, double * vol) {
+    DISPATCH(h, {
+        if (rho) std::copy(O.rho.begin(), O.rho.end(), rho);
+        if (vol) std::copy(O.vol.begin(), O.vol.end(), vol);
+    });
+}
+void orc_set_volumes(Handle * h, const double * vol) { DISPATCH(h, O.vol.assign(vol, vol + O.x.size())); }
+void orc_get_boundary_info(Handle * h, double * rho, double * vol) {
+    DISPATCH(h, {
+        if (rho) std::copy(O.rhob.begin(), O.rhob.end(), rho);
+        if (vol) std::copy(O.volb.begin(), O.volb.end(), vol);
+    });
+}
+void orc_set_boundary_info(Handle * h, const double * rho, const double * vol) {
+    DISPATCH(h, { O.rhob.assign(rho, rho + O.xb.size()); O.volb.assign(vol, vol + O.xb.size()); });
+}
+int64_t orc_num_virtual(Handle * h) {
+    int64_t n = 0;
+    DISPATCH(h, n = int64_t(O.xv.size()));
+    return n;
+}
+// Per active node (x-fastest order): node id, rho_I, V_I, vbar (n*dim), D_I, alpha_hat, p.
+void orc_get_virtual(Handle * h, int64_t * node, double * rho, double * vol, double * vbar, double * dv,
+                     double * ahat, double * p) {
+    DISPATCH(h, {
+        const size_t n = O.xv.size();
+        if (node) std::copy(O.node.begin(), O.node.end(), node);
+        if (rho) std::copy(O.rhov.begin(), O.rhov.end(), rho);
+        if (vol) std::copy(O.volv.begin(), O.volv.end(), vol);
+        if (vbar && O.vbar.size() == n) orc::storeVecs<D>(O.vbar, vbar);
+        if (dv && O.div.size() == n) std::copy(O.div.begin(), O.div.end(), dv);
+        if (ahat && O.alphaHat.size() == n) std::copy(O.alphaHat.begin(), O.alphaHat.end(), ahat);
+        if (p && O.pres.size() == n) std::copy(O.pres.begin(), O.pres.end(), p);
+    });
+}
+// Pressure vector used as the next warm start (reference: the stale prefix survives resize).
+void orc_set_pressure(Handle * h, int64_t n, const double * p) { DISPATCH(h, O.pres.assign(p, p + n)); }
+// y = A x with the operator assembled by the last project / initialize.
+void orc_apply_operator(Handle * h, const double * in, double * out) {
+    DISPATCH(h, {
+        std::vector<double> a(in, in + O.xv.size()), b;
+        O.spmv(a, b);
+        std::copy(b.begin(), b.end(), out);
+    });
+}
+// Solver statistics: iterations (SpMV count), iterations as Eigen reports them,
+// relative residual, |b|, status.
+void orc_get_stats(Handle * h, int32_t * iters, int32_t * eigenIters, double * relres, double * bnorm, int32_t * status) {
+    DISPATCH(h, {
+        *iters = O.cgIters;
+        *eigenIters = O.cgEigenIters;
+        *relres = O.cgRelRes;
+        *bnorm = O.rhsNorm;
+        *status = O.status;
+    });
+}
+// Neighbour query with the reference searcher semantics: for each query point, the
+// sorted ids of real particles (which=0), boundary particles (1) or virtual
+// particles (2) with |x_j - q|^2 < radius^2.  Returns counts; fills `ids` (CSR by
+// query) when non-null.
+void orc_neighbors(Handle * h, int which, int64_t nq, const double * q, int64_t * counts, int64_t * offsets, int64_t * ids) {
+    DISPATCH(h, {
+        const auto & S = which == 0 ? O.sReal : which == 1 ? O.sBnd : O.sVirt;
+        const auto & X = which == 0 ? O.x : which == 1 ? O.xb : O.xv;
+        for (int64_t t = 0; t < nq; t++) {
+            orc::Vec<D> p;
+            for (int a = 0; a < D; a++) p[a] = q[t * D + a];
+            std::vector<int64_t> got;
+            S.forEach(X, p, [&](int j, const orc::Vec<D> &) { got.push_back(j); });
+            std::sort(got.begin(), got.end());
+            counts[t] = int64_t(got.size());
+            if (ids) std::copy(got.begin(), got.end(), ids + offsets[t]);
+        }
+    });
+}
+// Kernel evaluations for known-answer tests: which 0 = W, 1 = W'; radius = particle radius.
+double orc_kernel(int dim, double radius, int which, double dist) {
+    orc::Kernel k(radius, dim);
+    return which == 0 ? k.W(dist) : k.dW(dist);
+}
+double orc_packed_kernel_sum(int dim, double radius) { return orc::Kernel(radius, dim).packedSum(dim); }
+
+}  // extern "C"

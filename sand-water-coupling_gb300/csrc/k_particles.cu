@@ -1,0 +1,642 @@
+// k_particles.cu -- particle-side kernels of the dual-particle SPH projection:
+// host-format conversion, advection, counting-sort binning into node cells,
+// real and boundary densities, gravity + div-free viscosity, brick activation,
+// the pressure-gradient update G_i and the export back to host order.
+#include "swc_kernels.h"
+
+namespace swc {
+
+// ---------------------------------------------------------------------------
+// Host FP64 AoS (dim components per particle, the .sav layout of
+// Cores/Utilities/IO.h:19-26) <-> device float4.
+// ---------------------------------------------------------------------------
+__global__ void k_import(const double * __restrict__ x, const double * __restrict__ v, int dim, long long n,
+                         float4 * __restrict__ pos, float4 * __restrict__ vel, int * __restrict__ id) {
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f), u = make_float4(0.f, 0.f, 0.f, 0.f);
+        p.x = float(x[i * dim]);
+        p.y = float(x[i * dim + 1]);
+        if (dim == 3) p.z = float(x[i * dim + 2]);
+        if (v) {
+            u.x = float(v[i * dim]);
+            u.y = float(v[i * dim + 1]);
+            if (dim == 3) u.z = float(v[i * dim + 2]);
+        }
+        pos[i] = p;
+        vel[i] = u;
+        if (id) id[i] = int(i);
+    }
+}
+
+__global__ void k_export(const float4 * __restrict__ pos, const float4 * __restrict__ vel, const int * __restrict__ id,
+                         int dim, long long n, double * __restrict__ x, double * __restrict__ v) {
+    for (long long s = blockIdx.x * (long long) blockDim.x + threadIdx.x; s < n; s += (long long) gridDim.x * blockDim.x) {
+        const long long i = id[s];
+        const float4 p = pos[s], u = vel[s];
+        if (x) {
+            x[i * dim]     = p.x;
+            x[i * dim + 1] = p.y;
+            if (dim == 3) x[i * dim + 2] = p.z;
+        }
+        if (v) {
+            v[i * dim]     = u.x;
+            v[i * dim + 1] = u.y;
+            if (dim == 3) v[i * dim + 2] = u.z;
+        }
+    }
+}
+
+// Scatter a per-slot float attribute to original-id order (FP64 out).
+__global__ void k_export_scalar(const float * __restrict__ a, int stride, int comp, const int * __restrict__ id,
+                                long long n, double * __restrict__ out) {
+    for (long long s = blockIdx.x * (long long) blockDim.x + threadIdx.x; s < n; s += (long long) gridDim.x * blockDim.x)
+        out[id[s]] = a[s * stride + comp];
+}
+
+// x += v dt  (SmthParticleHydrodLiquid::moveParticles, Cores/Physics/SmthParticleHydrodLiquid.cpp:72-76).
+__global__ void k_advect(float4 * __restrict__ pos, const float4 * __restrict__ vel, long long n, float dt) {
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        float4 p = pos[i];
+        const float4 u = vel[i];
+        p.x = fmaf(u.x, dt, p.x);
+        p.y = fmaf(u.y, dt, p.y);
+        p.z = fmaf(u.z, dt, p.z);
+        pos[i] = p;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Counting sort into cells.  Order within a cell is made deterministic by an
+// insertion sort on the original id, so the final order is (cell, id).
+// ---------------------------------------------------------------------------
+template<int DIM>
+__global__ void k_cell_count(const float4 * __restrict__ pos, long long n, Lattice L, int * __restrict__ key,
+                             int * __restrict__ rank, int * __restrict__ count) {
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        const float4 p = pos[i];
+        const int3 c   = cell_of<DIM>(L, p.x, p.y, p.z);
+        const int k    = int(cell_linear(L, c));
+        key[i]         = k;
+        rank[i]        = atomicAdd(count + k, 1);
+    }
+}
+
+__global__ void k_cell_scatter(const int * __restrict__ key, const int * __restrict__ rank,
+                               const int * __restrict__ start, long long n, int * __restrict__ perm) {
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+        perm[start[key[i]] + rank[i]] = int(i);
+}
+
+__global__ void k_cell_sort_segments(const int * __restrict__ start, long long ncells, const int * __restrict__ id,
+                                     int * __restrict__ perm) {
+    for (long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x; c < ncells; c += (long long) gridDim.x * blockDim.x) {
+        const int b = start[c], e = start[c + 1];
+        if (e - b < 2) continue;
+        for (int i = b + 1; i < e; i++) {
+            const int pi = perm[i];
+            const int ki = id[pi];
+            int j        = i - 1;
+            while (j >= b && id[perm[j]] > ki) {
+                perm[j + 1] = perm[j];
+                j--;
+            }
+            perm[j + 1] = pi;
+        }
+    }
+}
+
+__global__ void k_permute(const int * __restrict__ perm, long long n, const float4 * __restrict__ a0,
+                          const float4 * __restrict__ a1, const float4 * __restrict__ a2, const int * __restrict__ i0,
+                          float4 * __restrict__ b0, float4 * __restrict__ b1, float4 * __restrict__ b2,
+                          int * __restrict__ j0) {
+    for (long long s = blockIdx.x * (long long) blockDim.x + threadIdx.x; s < n; s += (long long) gridDim.x * blockDim.x) {
+        const int src = perm[s];
+        b0[s]         = a0[src];
+        b1[s]         = a1[src];
+        if (a2) b2[s] = a2[src];
+        j0[s] = i0[src];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour iteration over cells for a query point and radius R (particle
+// queries): rows pruned by their slab distance, x-range per row from the
+// remaining radius.
+// ---------------------------------------------------------------------------
+template<int DIM, class F>
+__device__ __forceinline__ void for_each_in_radius(const Lattice & L, const int * __restrict__ cellStart,
+                                                   float qx, float qy, float qz, float R, float R2, F && f) {
+    const int cy0 = clampi(__float2int_rd((qy - R - L.oy) * L.inv_dx), 0, L.ny - 1);
+    const int cy1 = clampi(__float2int_rd((qy + R - L.oy) * L.inv_dx), 0, L.ny - 1);
+    int cz0 = 0, cz1 = 0;
+    if (DIM == 3) {
+        cz0 = clampi(__float2int_rd((qz - R - L.oz) * L.inv_dx), 0, L.nz - 1);
+        cz1 = clampi(__float2int_rd((qz + R - L.oz) * L.inv_dx), 0, L.nz - 1);
+    }
+    for (int cz = cz0; cz <= cz1; cz++) {
+        const float dz  = DIM == 3 ? slab_dist(qz, cz, L.nz, L.oz, L.dx) : 0.f;
+        const float rz2 = R2 - dz * dz;
+        if (rz2 <= 0.f) continue;
+        for (int cy = cy0; cy <= cy1; cy++) {
+            const float dy  = slab_dist(qy, cy, L.ny, L.oy, L.dx);
+            const float rem = rz2 - dy * dy;
+            if (rem <= 0.f) continue;
+            const float rx = sqrtf(rem) * 1.000001f + 1e-7f * L.dx;
+            const int cx0  = clampi(__float2int_rd((qx - rx - L.ox) * L.inv_dx), 0, L.nx - 1);
+            const int cx1  = clampi(__float2int_rd((qx + rx - L.ox) * L.inv_dx), 0, L.nx - 1);
+            const long long row = (long long) L.nx * (cy + (long long) L.ny * cz);
+            const int b = cellStart[row + cx0], e = cellStart[row + cx1 + 1];
+            for (int j = b; j < e; j++) f(j);
+        }
+    }
+}
+
+// rho_i = m sum_j W_h(x_i - x_j)  (SmoothedParticles::computeDensities,
+// Cores/Structures/SmoothedParticles.cpp:25-31).  Writes vel.w = m / rho_i and rho_i.
+template<int DIM>
+__global__ void __launch_bounds__(256) k_density(const float4 * __restrict__ pos, float4 * __restrict__ vel,
+                                                 float * __restrict__ rho_out, long long n, Lattice L, Phys P,
+                                                 const int * __restrict__ cellStart, float mass) {
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        const float4 q = pos[i];
+        float s        = 0.f;
+        for_each_in_radius<DIM>(L, cellStart, q.x, q.y, q.z, P.h, P.h2, [&](int j) {
+            const float4 p = pos[j];
+            const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 < P.h2) s += kW(sqrtf(r2), P.inv_h, P.c0h);
+        });
+        const float rho = mass * s;
+        if (rho_out) rho_out[i] = rho;
+        vel[i].w = mass / rho;
+    }
+}
+
+// V_i = m / rho_i, stored in pos.w (initialize only; DualParticleSphLiquid.cpp:88-89).
+__global__ void k_set_volume(float4 * __restrict__ pos, const float * __restrict__ rho, long long n, float mass) {
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+        pos[i].w = mass / rho[i];
+}
+
+// Gravity (applyExternalForces, SmthParticleHydrodLiquid.cpp:84-88) followed by
+// the div-free Laplacian viscosity (applyViscosityForce :90-98 with
+// ParticlesBasedVectorField::divFreeLaplacianAtDataPoint,
+// Cores/Structures/ParticlesBasedVectorField.cpp:56-69).  Velocity differences
+// are invariant under the uniform gravity increment, so both run in one pass.
+template<int DIM>
+__global__ void __launch_bounds__(256) k_forces(const float4 * __restrict__ pos, const float4 * __restrict__ vel,
+                                                float4 * __restrict__ vel_out, long long n, Lattice L, Phys P,
+                                                const int * __restrict__ cellStart, float dt) {
+    const float visc = P.viscosity * 2.f * (DIM + 2.f) * P.mass * dt;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        const float4 q = pos[i];
+        const float4 vi = vel[i];
+        float lx = 0.f, ly = 0.f, lz = 0.f;
+        if (P.viscosity != 0.f) {
+            for_each_in_radius<DIM>(L, cellStart, q.x, q.y, q.z, P.h, P.h2, [&](int j) {
+                const float4 p = pos[j];
+                const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;  // x_j - x_i
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 < P.h2 && r2 > 0.f) {
+                    const float4 vj = vel[j];
+                    const float r   = sqrtf(r2);
+                    const float s   = ((vj.x - vi.x) * dx + (vj.y - vi.y) * dy + (vj.z - vi.z) * dz) / r2;
+                    // gradientKernel(x_j - x_i) = -W'(r) (x_j - x_i)/r, divided by rho_j = m / vel.w
+                    const float g = -kdW(r, P.inv_h, P.c1h) / r * s * (vj.w / P.mass);
+                    lx += g * dx;
+                    ly += g * dy;
+                    lz += g * dz;
+                }
+            });
+        }
+        float4 o = vi;
+        if (P.gravity_on) {
+            o.x += P.gx * dt;
+            o.y += P.gy * dt;
+            if (DIM == 3) o.z += P.gz * dt;
+        }
+        o.x += visc * lx;
+        o.y += visc * ly;
+        if (DIM == 3) o.z += visc * lz;
+        vel_out[i] = o;
+    }
+}
+
+// Boundary densities from boundary-boundary neighbours (initialize,
+// DualParticleSphLiquid.cpp:93-94): rho_b = m_b sum W_h, V_b = m_b / rho_b.
+template<int DIM>
+__global__ void __launch_bounds__(256) k_boundary_density(float4 * __restrict__ bpos, float4 * __restrict__ bvel,
+                                                          float * __restrict__ rho_out, long long nb, Lattice L,
+                                                          Phys P, const int * __restrict__ bcellStart) {
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < nb; i += (long long) gridDim.x * blockDim.x) {
+        const float4 q = bpos[i];
+        float s        = 0.f;
+        for_each_in_radius<DIM>(L, bcellStart, q.x, q.y, q.z, P.h, P.h2, [&](int j) {
+            const float4 p = bpos[j];
+            const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 < P.h2) s += kW(sqrtf(r2), P.inv_h, P.c0h);
+        });
+        const float rho = P.bmass * s;
+        if (rho_out) rho_out[i] = rho;
+        bpos[i].w = P.bmass / rho;
+        bvel[i].w = P.bmass / rho;
+    }
+}
+
+// Mark every brick that holds a node within h of a real particle (only those
+// nodes can have a positive weight, VirtualParticle.cpp:50-56).
+template<int DIM>
+__global__ void k_mark_bricks(const float4 * __restrict__ pos, long long n, Lattice L, Phys P,
+                              unsigned char * __restrict__ bflag) {
+    using G = BrickGeom<DIM>;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        const float4 p = pos[i];
+        const int x0 = clampi(__float2int_ru((p.x - P.h - L.ox) * L.inv_dx), 0, L.nx - 1);
+        const int x1 = clampi(__float2int_rd((p.x + P.h - L.ox) * L.inv_dx), 0, L.nx - 1);
+        const int y0 = clampi(__float2int_ru((p.y - P.h - L.oy) * L.inv_dx), 0, L.ny - 1);
+        const int y1 = clampi(__float2int_rd((p.y + P.h - L.oy) * L.inv_dx), 0, L.ny - 1);
+        int z0 = 0, z1 = 0;
+        if (DIM == 3) {
+            z0 = clampi(__float2int_ru((p.z - P.h - L.oz) * L.inv_dx), 0, L.nz - 1);
+            z1 = clampi(__float2int_rd((p.z + P.h - L.oz) * L.inv_dx), 0, L.nz - 1);
+        }
+        // widen by one node to stay safe against FP32 rounding at the support edge
+        const int bx0 = max(x0 - 1, 0) / G::BX, bx1 = min(x1 + 1, L.nx - 1) / G::BX;
+        const int by0 = max(y0 - 1, 0) / G::BY, by1 = min(y1 + 1, L.ny - 1) / G::BY;
+        const int bz0 = DIM == 3 ? max(z0 - 1, 0) / G::BZ : 0, bz1 = DIM == 3 ? min(z1 + 1, L.nz - 1) / G::BZ : 0;
+        for (int bz = bz0; bz <= bz1; bz++)
+            for (int by = by0; by <= by1; by++)
+                for (int bx = bx0; bx <= bx1; bx++) bflag[bx + L.bnx * (by + L.bny * bz)] = 1;
+    }
+}
+
+// Pressure-gradient update (VirtualParticle::applyPressureGradient,
+// Cores/Structures/VirtualParticle.cpp:111-134):
+//   v_i += sum_{J in N_H(i)} V_J p_J gradW_H(x_i - x_J)
+//          - sum_{b in N_h(i)} V_b min(n_b.(v_i - v_b), 0) n_b W_h(x_i - x_b)
+template<int DIM>
+__global__ void __launch_bounds__(256) k_pressure_gradient(
+    const float4 * __restrict__ pos, float4 * __restrict__ vel, long long n, Lattice L, Phys P,
+    const unsigned char * __restrict__ bflag, const float * __restrict__ nodeV, const float * __restrict__ nodeP,
+    const float4 * __restrict__ bpos, const float4 * __restrict__ bvel, const float4 * __restrict__ bnrm,
+    const int * __restrict__ bcellStart) {
+    using G = BrickGeom<DIM>;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        const float4 q  = pos[i];
+        const float4 vi = vel[i];
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        // virtual nodes within H: node coordinates k with |x_i - x_k| < H
+        const float ux = (q.x - L.ox) * L.inv_dx, uy = (q.y - L.oy) * L.inv_dx, uz = (q.z - L.oz) * L.inv_dx;
+        const float Hn = P.H * L.inv_dx;  // support in node units
+        const int y0 = max(__float2int_ru(uy - Hn), 0), y1 = min(__float2int_rd(uy + Hn), L.ny - 1);
+        int z0 = 0, z1 = 0;
+        if (DIM == 3) z0 = max(__float2int_ru(uz - Hn), 0), z1 = min(__float2int_rd(uz + Hn), L.nz - 1);
+        for (int kz = z0; kz <= z1; kz++) {
+            const float zn = L.oz + kz * L.dx;
+            const float dz = DIM == 3 ? q.z - zn : 0.f;
+            for (int ky = y0; ky <= y1; ky++) {
+                const float yn  = L.oy + ky * L.dx;
+                const float dy  = q.y - yn;
+                const float rem = P.H2 - dy * dy - dz * dz;
+                if (rem <= 0.f) continue;
+                const float rn = sqrtf(rem) * L.inv_dx;
+                const int x0 = max(__float2int_ru(ux - rn), 0), x1 = min(__float2int_rd(ux + rn), L.nx - 1);
+                for (int kx = x0; kx <= x1; kx++) {
+                    const int brick = kx / G::BX + L.bnx * (ky / G::BY + L.bny * (DIM == 3 ? kz / G::BZ : 0));
+                    if (!bflag[brick]) continue;
+                    const long long s = node_slot<DIM>(L, kx, ky, kz);
+                    const float u     = nodeV[s] * nodeP[s];
+                    if (u == 0.f) continue;
+                    const float dx = q.x - (L.ox + kx * L.dx);
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    if (r2 >= P.H2 || r2 <= 0.f) continue;
+                    const float r = sqrtf(r2);
+                    const float g = -kdW(r, P.inv_H, P.c1H) / r * u;
+                    fx += g * dx;
+                    fy += g * dy;
+                    fz += g * dz;
+                }
+            }
+        }
+        // boundary friction-free wall term
+        for_each_in_radius<DIM>(L, bcellStart, q.x, q.y, q.z, P.h, P.h2, [&](int j) {
+            const float4 p = bpos[j];
+            const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 < P.h2) {
+                const float4 nb = bnrm[j];
+                const float4 vb = bvel[j];
+                const float vn  = fminf(nb.x * (vi.x - vb.x) + nb.y * (vi.y - vb.y) + nb.z * (vi.z - vb.z), 0.f);
+                const float w   = kW(sqrtf(r2), P.inv_h, P.c0h);
+                const float c   = p.w * vn * w;
+                fx -= c * nb.x;
+                fy -= c * nb.y;
+                fz -= c * nb.z;
+            }
+        });
+        float4 o = vi;
+        o.x += fx;
+        o.y += fy;
+        if (DIM == 3) o.z += fz;
+        vel[i] = o;
+    }
+}
+
+// Rigid motion of boundary particles flagged as moving (paddle): rotation about
+// the y axis through c with angular velocity omega; v_b = omega x (x - c).
+// The moving flag travels with the particle in bnrm.w (1 = moving).
+__global__ void k_rotate_boundary(float4 * __restrict__ bpos, float4 * __restrict__ bvel, float4 * __restrict__ bnrm,
+                                  long long nb, float cx, float cz, float omega, float dt) {
+    const float ca = cosf(omega * dt), sa = sinf(omega * dt);
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < nb; i += (long long) gridDim.x * blockDim.x) {
+        float4 p = bpos[i], v = bvel[i], nn = bnrm[i];
+        if (nn.w == 0.f) continue;
+        // rotation by -omega dt about +y (x' = x cos + z sin, z' = -x sin + z cos)
+        const float rx = p.x - cx, rz = p.z - cz;
+        const float nx = rx * ca + rz * sa, nz = -rx * sa + rz * ca;
+        p.x = cx + nx;
+        p.z = cz + nz;
+        const float mx = nn.x * ca + nn.z * sa, mz = -nn.x * sa + nn.z * ca;
+        nn.x = mx;
+        nn.z = mz;
+        v.x = omega * nz;
+        v.z = -omega * nx;
+        bpos[i] = p;
+        bvel[i] = v;
+        bnrm[i] = nn;
+    }
+}
+
+// pos.w = vol_by_id[id[s]] (V_i travels with the particle id).
+__global__ void k_fill_w_by_id(float4 * __restrict__ pos, const float * __restrict__ vol, const int * __restrict__ id,
+                               long long n) {
+    for (long long s = blockIdx.x * (long long) blockDim.x + threadIdx.x; s < n; s += (long long) gridDim.x * blockDim.x)
+        pos[s].w = vol[id ? id[s] : s];
+}
+// vol_by_id[id[s]] = pos[s].w
+__global__ void k_scatter_w_to_id(const float4 * __restrict__ pos, const int * __restrict__ id, long long n,
+                                  float * __restrict__ vol) {
+    for (long long s = blockIdx.x * (long long) blockDim.x + threadIdx.x; s < n; s += (long long) gridDim.x * blockDim.x)
+        vol[id[s]] = pos[s].w;
+}
+// Boundary rho_b / V_b given by original id (replay of another run's initialize).
+__global__ void k_set_boundary_info(float4 * __restrict__ bpos, float4 * __restrict__ bvel, float * __restrict__ brho,
+                                    const float * __restrict__ rho, const float * __restrict__ vol,
+                                    const int * __restrict__ bid, long long nb, float bmass) {
+    for (long long s = blockIdx.x * (long long) blockDim.x + threadIdx.x; s < nb; s += (long long) gridDim.x * blockDim.x) {
+        const int i = bid[s];
+        brho[s]     = rho[i];
+        bpos[s].w   = vol[i];
+        bvel[s].w   = bmass / rho[i];
+    }
+}
+// bnrm.w = moving[bid[s]]
+__global__ void k_set_moving(float4 * __restrict__ bnrm, const unsigned char * __restrict__ moving,
+                             const int * __restrict__ bid, long long nb) {
+    for (long long s = blockIdx.x * (long long) blockDim.x + threadIdx.x; s < nb; s += (long long) gridDim.x * blockDim.x)
+        bnrm[s].w = moving[bid[s]] ? 1.f : 0.f;
+}
+
+// Max over a positive float array (ordered as int bits).
+__global__ void k_max_positive(const float * __restrict__ a, long long n, int * __restrict__ out_bits) {
+    int m = 0;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+        m = max(m, __float_as_int(a[i]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out_bits, m);
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan of int32 counts (three phases: tile sums, scan of tile sums,
+// tile scan + offset).  out has n + 1 entries; out[n] = total.
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 256, kScanItems = 8, kScanTile = kScanThreads * kScanItems;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int * __restrict__ in, long long n,
+                                                              int * __restrict__ tile_sum) {
+    __shared__ int sm[kScanThreads / 32];
+    const long long base = (long long) blockIdx.x * kScanTile;
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        const long long i = base + threadIdx.x + (long long) k * kScanThreads;
+        if (i < n) s += in[i];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < kScanThreads / 32; w++) t += sm[w];
+        tile_sum[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(int * __restrict__ tile_sum, int ntiles) {
+    __shared__ int sm[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < ntiles; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int v = i < ntiles ? tile_sum[i] : 0;
+        int x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) >= o) x += y;
+        }
+        if ((threadIdx.x & 31) == 31) sm[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            int w = sm[threadIdx.x];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, w, o);
+                if (threadIdx.x >= o) w += y;
+            }
+            sm[threadIdx.x] = w;
+        }
+        __syncthreads();
+        const int warp_off = (threadIdx.x >> 5) ? sm[(threadIdx.x >> 5) - 1] : 0;
+        const int incl     = x + warp_off + carry;
+        if (i < ntiles) tile_sum[i] = incl - v;  // exclusive
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = incl;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int * __restrict__ in, long long n,
+                                                              const int * __restrict__ tile_off, int * __restrict__ out) {
+    __shared__ int sm[kScanThreads / 32];
+    const long long base = (long long) blockIdx.x * kScanTile + (long long) threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        const long long i = base + k;
+        v[k]              = i < n ? in[i] : 0;
+        s += v[k];
+    }
+    int x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) >= o) x += y;
+    }
+    if ((threadIdx.x & 31) == 31) sm[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int w = threadIdx.x < kScanThreads / 32 ? sm[threadIdx.x] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (threadIdx.x >= o) w += y;
+        }
+        if (threadIdx.x < kScanThreads / 32) sm[threadIdx.x] = w;
+    }
+    __syncthreads();
+    int run = tile_off[blockIdx.x] + x - s + ((threadIdx.x >> 5) ? sm[(threadIdx.x >> 5) - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        const long long i = base + k;
+        if (i < n) out[i] = run;
+        run += v[k];
+        if (i == n - 1) out[n] = run;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+static inline int grid_for(long long n, int threads, int cap = 152 * 16) {
+    long long g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return int(g);
+}
+
+void launch_import(const double * x, const double * v, int dim, long long n, float4 * pos, float4 * vel, int * id,
+                   cudaStream_t st) {
+    if (n > 0) k_import<<<grid_for(n, 256), 256, 0, st>>>(x, v, dim, n, pos, vel, id);
+}
+void launch_export(const float4 * pos, const float4 * vel, const int * id, int dim, long long n, double * x,
+                   double * v, cudaStream_t st) {
+    if (n > 0) k_export<<<grid_for(n, 256), 256, 0, st>>>(pos, vel, id, dim, n, x, v);
+}
+void launch_export_scalar(const float * a, int stride, int comp, const int * id, long long n, double * out,
+                          cudaStream_t st) {
+    if (n > 0) k_export_scalar<<<grid_for(n, 256), 256, 0, st>>>(a, stride, comp, id, n, out);
+}
+void launch_advect(float4 * pos, const float4 * vel, long long n, float dt, cudaStream_t st) {
+    if (n > 0) k_advect<<<grid_for(n, 256), 256, 0, st>>>(pos, vel, n, dt);
+}
+
+void launch_scan(const int * in, long long n, int * out, int * tile_buf, cudaStream_t st) {
+    const long long ntiles = (n + kScanTile - 1) / kScanTile;
+    if (n <= 0) {
+        cudaMemsetAsync(out, 0, sizeof(int), st);
+        return;
+    }
+    k_scan_tiles<<<int(ntiles), kScanThreads, 0, st>>>(in, n, tile_buf);
+    k_scan_top<<<1, 1024, 0, st>>>(tile_buf, int(ntiles));
+    k_scan_apply<<<int(ntiles), kScanThreads, 0, st>>>(in, n, tile_buf, out);
+}
+long long scan_tile_count(long long n) { return (n + kScanTile - 1) / kScanTile + 1; }
+
+template<int DIM>
+void launch_bin(const Lattice & L, long long n, float4 * pos, float4 * vel, float4 * aux, int * id, SortScratch & S,
+                int * cellStart, cudaStream_t st) {
+    cudaMemsetAsync(S.count, 0, sizeof(int) * L.ncells, st);
+    if (n > 0) k_cell_count<DIM><<<grid_for(n, 256), 256, 0, st>>>(pos, n, L, S.key, S.rank, S.count);
+    launch_scan(S.count, L.ncells, cellStart, S.tiles, st);
+    if (n == 0) return;
+    k_cell_scatter<<<grid_for(n, 256), 256, 0, st>>>(S.key, S.rank, cellStart, n, S.perm);
+    k_cell_sort_segments<<<grid_for(L.ncells, 256), 256, 0, st>>>(cellStart, L.ncells, id, S.perm);
+    k_permute<<<grid_for(n, 256), 256, 0, st>>>(S.perm, n, pos, vel, aux, id, S.pos2, S.vel2, S.aux2, S.id2);
+    cudaMemcpyAsync(pos, S.pos2, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(vel, S.vel2, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
+    if (aux) cudaMemcpyAsync(aux, S.aux2, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(id, S.id2, sizeof(int) * n, cudaMemcpyDeviceToDevice, st);
+}
+
+template<int DIM>
+void launch_density(const float4 * pos, float4 * vel, float * rho, long long n, const Lattice & L, const Phys & P,
+                    const int * cellStart, cudaStream_t st) {
+    if (n > 0) k_density<DIM><<<grid_for(n, 256, 1 << 20), 256, 0, st>>>(pos, vel, rho, n, L, P, cellStart, P.mass);
+}
+void launch_set_volume(float4 * pos, const float * rho, long long n, float mass, cudaStream_t st) {
+    if (n > 0) k_set_volume<<<grid_for(n, 256), 256, 0, st>>>(pos, rho, n, mass);
+}
+template<int DIM>
+void launch_forces(const float4 * pos, const float4 * vel, float4 * vel_out, long long n, const Lattice & L,
+                   const Phys & P, const int * cellStart, float dt, cudaStream_t st) {
+    if (n > 0)
+        k_forces<DIM><<<grid_for(n, 256, 1 << 20), 256, 0, st>>>(pos, vel, vel_out, n, L, P, cellStart, dt);
+}
+template<int DIM>
+void launch_boundary_density(float4 * bpos, float4 * bvel, float * rho, long long nb, const Lattice & L,
+                             const Phys & P, const int * bcellStart, cudaStream_t st) {
+    if (nb > 0)
+        k_boundary_density<DIM><<<grid_for(nb, 256, 1 << 20), 256, 0, st>>>(bpos, bvel, rho, nb, L, P, bcellStart);
+}
+template<int DIM>
+void launch_mark_bricks(const float4 * pos, long long n, const Lattice & L, const Phys & P, unsigned char * bflag,
+                        cudaStream_t st) {
+    cudaMemsetAsync(bflag, 0, L.nbricks, st);
+    if (n > 0) k_mark_bricks<DIM><<<grid_for(n, 256), 256, 0, st>>>(pos, n, L, P, bflag);
+}
+template<int DIM>
+void launch_pressure_gradient(const float4 * pos, float4 * vel, long long n, const Lattice & L, const Phys & P,
+                              const unsigned char * bflag, const float * nodeV, const float * nodeP,
+                              const float4 * bpos, const float4 * bvel, const float4 * bnrm, const int * bcellStart,
+                              cudaStream_t st) {
+    if (n > 0)
+        k_pressure_gradient<DIM><<<grid_for(n, 256, 1 << 20), 256, 0, st>>>(pos, vel, n, L, P, bflag, nodeV, nodeP,
+                                                                              bpos, bvel, bnrm, bcellStart);
+}
+void launch_rotate_boundary(float4 * bpos, float4 * bvel, float4 * bnrm, long long nb, float cx, float cz,
+                            float omega, float dt, cudaStream_t st) {
+    if (nb > 0) k_rotate_boundary<<<grid_for(nb, 256), 256, 0, st>>>(bpos, bvel, bnrm, nb, cx, cz, omega, dt);
+}
+void launch_fill_w_by_id(float4 * pos, const float * vol, const int * id, long long n, cudaStream_t st) {
+    if (n > 0) k_fill_w_by_id<<<grid_for(n, 256), 256, 0, st>>>(pos, vol, id, n);
+}
+void launch_scatter_w_to_id(const float4 * pos, const int * id, long long n, float * vol, cudaStream_t st) {
+    if (n > 0) k_scatter_w_to_id<<<grid_for(n, 256), 256, 0, st>>>(pos, id, n, vol);
+}
+void launch_set_boundary_info(float4 * bpos, float4 * bvel, float * brho, const float * rho, const float * vol,
+                              const int * bid, long long nb, float bmass, cudaStream_t st) {
+    if (nb > 0) k_set_boundary_info<<<grid_for(nb, 256), 256, 0, st>>>(bpos, bvel, brho, rho, vol, bid, nb, bmass);
+}
+void launch_set_moving(float4 * bnrm, const unsigned char * moving, const int * bid, long long nb, cudaStream_t st) {
+    if (nb > 0) k_set_moving<<<grid_for(nb, 256), 256, 0, st>>>(bnrm, moving, bid, nb);
+}
+void launch_max_positive(const float * a, long long n, int * out_bits, cudaStream_t st) {
+    cudaMemsetAsync(out_bits, 0, sizeof(int), st);
+    if (n > 0) k_max_positive<<<grid_for(n, 256), 256, 0, st>>>(a, n, out_bits);
+}
+
+#define SWC_INST(D)                                                                                                    \
+    template void launch_bin<D>(const Lattice &, long long, float4 *, float4 *, float4 *, int *, SortScratch &, int *, \
+                                cudaStream_t);                                                                         \
+    template void launch_density<D>(const float4 *, float4 *, float *, long long, const Lattice &, const Phys &,       \
+                                    const int *, cudaStream_t);                                                        \
+    template void launch_forces<D>(const float4 *, const float4 *, float4 *, long long, const Lattice &, const Phys &,  \
+                                   const int *, float, cudaStream_t);                                                  \
+    template void launch_boundary_density<D>(float4 *, float4 *, float *, long long, const Lattice &, const Phys &,    \
+                                             const int *, cudaStream_t);                                               \
+    template void launch_mark_bricks<D>(const float4 *, long long, const Lattice &, const Phys &, unsigned char *,     \
+                                        cudaStream_t);                                                                 \
+    template void launch_pressure_gradient<D>(const float4 *, float4 *, long long, const Lattice &, const Phys &,      \
+                                              const unsigned char *, const float *, const float *, const float4 *,     \
+                                              const float4 *, const float4 *, const int *, cudaStream_t);
+SWC_INST(2)
+SWC_INST(3)
+#undef SWC_INST
+
+}  // namespace swc

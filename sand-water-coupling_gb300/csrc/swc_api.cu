@@ -1,0 +1,1013 @@
+// swc_api.cu -- host orchestration and C ABI of the GB300 dual-particle SPH
+// projection (see include/swc.h).  One context = one simulation on one GPU and
+// one CUDA stream.  The CG loop runs from device-resident scalars; batches of
+// iterations are replayed from captured CUDA graphs between host convergence
+// checks.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numbers>
+#include <string>
+#include <vector>
+
+#include "../../include/swc.h"
+#include "swc_kernels.h"
+
+using namespace swc;
+
+namespace {
+
+constexpr int kPhases = 8;
+
+struct HostCg {
+    CgState st;
+    int     nv;
+    int     nbricks;
+};
+
+}  // namespace
+
+struct swc_ctx {
+    int             dim = 3;
+    swc_scene       scene{};
+    swc_solver_opts opts{};
+    cudaStream_t    stream     = nullptr;
+    bool            own_stream = false;
+    int             device = 0, num_sms = 152;
+    Lattice         L{};
+    Phys            P{};
+    Stencil         S{};
+    StencilD        SD{};
+    int             grid = 1;  // persistent grid of the brick kernels
+    std::string     err;
+
+    // real particles (sorted by cell)
+    long long  n = 0;
+    float4 *   pos = nullptr, *vel = nullptr, *vel2 = nullptr;
+    int *      id = nullptr;
+    float *    rho = nullptr;
+    float *    vol_by_id = nullptr;
+    double *   stage = nullptr;  // FP64 host-format staging (2 * n * dim)
+    int *      cellStart = nullptr;
+    SortScratch sortR{};
+
+    // boundary particles
+    long long  nb = 0;
+    float4 *   bpos = nullptr, *bvel = nullptr, *bnrm = nullptr;
+    int *      bid = nullptr;
+    float *    brho = nullptr;
+    int *      bcellStart = nullptr;
+    SortScratch sortB{};
+    bool       has_motion = false;
+    double     motion_c[3] = {0, 0, 0};
+    double     motion_omega = 0;
+    double *   bstage = nullptr;
+
+    // lattice
+    NodeArrays  N{};
+    BrickArrays B{};
+    float *     pcomp = nullptr;
+    int *       nv_prev = nullptr;
+    int *       scan_tiles = nullptr;
+    CgState *   cg = nullptr;
+    double *    partials = nullptr;
+    HostCg *    hcg = nullptr;  // pinned
+    unsigned long long * diag_bits = nullptr;
+    int *       max_bits = nullptr;
+    double *    res2 = nullptr;
+    cudaGraphExec_t g1 = nullptr, g8 = nullptr;
+
+    bool   initialized = false;
+    double rho0 = 0, alpha0 = -1e6, kappa = 0;
+    int    last_iters = 16;
+    bool   profiling = false;
+    cudaEvent_t ev[kPhases + 2] = {};
+    cudaEvent_t evA = nullptr, evB = nullptr;
+    double phase_ms[kPhases] = {};
+};
+
+namespace {
+
+#define CK(call)                                                                                                       \
+    do {                                                                                                               \
+        cudaError_t e_ = (call);                                                                                       \
+        if (e_ != cudaSuccess) {                                                                                       \
+            if (c) c->err = std::string(#call) + ": " + cudaGetErrorString(e_);                                        \
+            return e_ == cudaErrorMemoryAllocation ? SWC_OUT_OF_MEMORY : SWC_CUDA_ERROR;                               \
+        }                                                                                                              \
+    } while (0)
+
+template<class T> int dalloc(swc_ctx * c, T ** p, size_t count) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    if (count == 0) count = 1;
+    CK(cudaMalloc(reinterpret_cast<void **>(p), sizeof(T) * count));
+    return SWC_OK;
+}
+template<class T> void dfree(T *& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+double kernelW(double dist, double h, int dim) {
+    const double inv_h = 1 / h, inv_h2 = 1 / (h * h);
+    const double c0 = std::numbers::inv_pi * inv_h2 * (dim == 2 ? 40.0 / 7 : 8 * inv_h);
+    const double x  = dist * inv_h;
+    if (x < .5) return c0 * (6 * x * x * (x - 1) + 1);
+    if (x < 1) return c0 * 2 * (1 - x) * (1 - x) * (1 - x);
+    return 0;
+}
+double kernelDW(double dist, double h, int dim) {
+    const double inv_h = 1 / h, inv_h2 = 1 / (h * h);
+    const double c0 = std::numbers::inv_pi * inv_h2 * (dim == 2 ? 40.0 / 7 : 8 * inv_h);
+    const double c1 = 6 * inv_h * c0;
+    const double x  = dist * inv_h;
+    if (x < .5) return c1 * x * (3 * x - 2);
+    if (x < 1) return c1 * (1 - x) * (x - 1);
+    return 0;
+}
+
+int alloc_sort(swc_ctx * c, SortScratch & S, long long n, bool aux) {
+    int rc;
+    if ((rc = dalloc(c, &S.key, n))) return rc;
+    if ((rc = dalloc(c, &S.rank, n))) return rc;
+    if ((rc = dalloc(c, &S.perm, n))) return rc;
+    if ((rc = dalloc(c, &S.count, c->L.ncells))) return rc;
+    if ((rc = dalloc(c, &S.tiles, scan_tile_count(c->L.ncells + 1) + 2))) return rc;
+    if ((rc = dalloc(c, &S.pos2, n))) return rc;
+    if ((rc = dalloc(c, &S.vel2, n))) return rc;
+    if (aux && (rc = dalloc(c, &S.aux2, n))) return rc;
+    if ((rc = dalloc(c, &S.id2, n))) return rc;
+    return SWC_OK;
+}
+void free_sort(SortScratch & S) {
+    dfree(S.key);
+    dfree(S.rank);
+    dfree(S.perm);
+    dfree(S.count);
+    dfree(S.tiles);
+    dfree(S.pos2);
+    dfree(S.vel2);
+    dfree(S.aux2);
+    dfree(S.id2);
+}
+
+void setup_phys(swc_ctx * c) {
+    const swc_scene & s = c->scene;
+    const int dim       = s.dim;
+    Phys & P            = c->P;
+    const double h = s.particle_radius * 4, H = s.grid_spacing * 4;
+    auto coeffs = [&](double kr, float & inv, float & c0, float & c1) {
+        const double ih = 1 / kr, ih2 = 1 / (kr * kr);
+        const double k0 = std::numbers::inv_pi * ih2 * (dim == 2 ? 40.0 / 7 : 8 * ih);
+        inv = float(ih);
+        c0  = float(k0);
+        c1  = float(6 * ih * k0);
+    };
+    P.h  = float(h);
+    P.h2 = float(h * h);
+    coeffs(h, P.inv_h, P.c0h, P.c1h);
+    P.H  = float(H);
+    P.H2 = float(H * H);
+    coeffs(H, P.inv_H, P.c0H, P.c1H);
+    P.h_d     = h;
+    P.inv_h_d = 1 / h;
+    P.c0h_d   = std::numbers::inv_pi * (1 / (h * h)) * (dim == 2 ? 40.0 / 7 : 8 * (1 / h));
+    P.mass    = float(s.mass);
+    P.bmass   = float(s.boundary_mass);
+    P.rho0    = float(c->rho0 > 0 ? c->rho0 : 1.0);
+    P.kappa   = float(c->kappa);
+    P.alpha0  = float(c->alpha0);
+    double ratio = h / s.grid_spacing;
+    if (std::fabs(ratio - std::round(ratio)) < 1e-9) ratio = std::round(ratio);
+    P.cell_lo    = int(std::floor(-ratio));
+    P.cell_hi    = int(std::ceil(ratio)) - 1;
+    P.gx         = float(s.gravity[0]);
+    P.gy         = float(s.gravity[1]);
+    P.gz         = float(s.gravity[2]);
+    P.viscosity  = float(s.viscosity);
+    P.gravity_on = s.enable_gravity ? 1 : 0;
+    // virtual stencil: c(|k|^2) = 2 W'_H(r) / (r + 1e-6), r = |k| * spacing
+    // (alpha_IJ / V_J of VirtualParticle::calculateCoef, VirtualParticle.cpp:157)
+    for (int r2 = 0; r2 < 16; r2++) {
+        const double r = std::sqrt(double(r2)) * s.grid_spacing;
+        const double v = r2 == 0 ? 0.0 : 2.0 * kernelDW(r, H, dim) / (r + 1e-6);
+        c->SD.c[r2]    = v;
+        c->S.c[r2]     = float(v);
+    }
+}
+
+template<int DIM> int run_bin_real(swc_ctx * c) {
+    launch_bin<DIM>(c->L, c->n, c->pos, c->vel, nullptr, c->id, c->sortR, c->cellStart, c->stream);
+    return SWC_OK;
+}
+template<int DIM> int run_bin_boundary(swc_ctx * c) {
+    launch_bin<DIM>(c->L, c->nb, c->bpos, c->bvel, c->bnrm, c->bid, c->sortB, c->bcellStart, c->stream);
+    return SWC_OK;
+}
+
+inline void mark(swc_ctx * c, int k) {
+    if (c->profiling) cudaEventRecord(c->ev[k], c->stream);
+}
+
+// Virtual generation: active bricks, fused gather, reference-order compaction,
+// alpha_hat (VirtualParticle::generateParticles + calculateCoef diagonal).
+template<int DIM> void run_generate(swc_ctx * c, bool with_ahat) {
+    launch_mark_bricks<DIM>(c->pos, c->n, c->L, c->P, c->B.flag, c->stream);
+    launch_brick_list(c->B.flag, c->L.nbricks, c->B.list, c->B.count, c->stream);
+    launch_node_gather<DIM>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel, c->bcellStart,
+                            c->grid, c->stream);
+    launch_segments<DIM>(c->L, c->B, c->N, c->scan_tiles, c->grid, c->stream);
+    if (with_ahat) launch_ahat<DIM>(c->L, c->P, c->B, c->N, c->S, c->grid, c->stream);
+}
+
+int capture_graphs(swc_ctx * c) {
+    for (int k = 0; k < 2; k++) {
+        const int reps = k == 0 ? 1 : 8;
+        cudaGraph_t g  = nullptr;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        for (int i = 0; i < reps; i++) {
+            if (c->dim == 2) launch_cg_iteration<2>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->grid, c->stream);
+            else launch_cg_iteration<3>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->grid, c->stream);
+        }
+        CK(cudaStreamEndCapture(c->stream, &g));
+        cudaGraphExec_t ge = nullptr;
+        CK(cudaGraphInstantiate(&ge, g, 0));
+        cudaGraphDestroy(g);
+        if (k == 0) c->g1 = ge;
+        else c->g8 = ge;
+    }
+    return SWC_OK;
+}
+
+// CG solve from the warm start in N.x; fills stats.
+template<int DIM> int run_cg(swc_ctx * c, swc_stats * st) {
+    const int * nv = c->B.seg_off + c->B.nseg;
+    if (!c->g1) {
+        CK(cudaStreamSynchronize(c->stream));
+        int rc = capture_graphs(c);
+        if (rc) return rc;
+    }
+    launch_cg_init<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->opts.tolerance, c->opts.max_iterations, nv,
+                        c->grid, c->stream);
+    CK(cudaMemcpyAsync(&c->hcg->st, c->cg, sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&c->hcg->nv, nv, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&c->hcg->nbricks, c->B.count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    const double rr0 = c->hcg->st.rr0, bb = c->hcg->st.bb;
+    int first        = c->opts.check_interval > 0 ? c->opts.check_interval : std::max(4, c->last_iters);
+    while (!c->hcg->st.done) {
+        const int room = c->hcg->st.max_iter - c->hcg->st.iter;
+        int m          = std::min(first, std::max(room, 1));
+        for (; m >= 8; m -= 8) CK(cudaGraphLaunch(c->g8, c->stream));
+        for (; m > 0; m--) CK(cudaGraphLaunch(c->g1, c->stream));
+        CK(cudaMemcpyAsync(&c->hcg->st, c->cg, sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        first = c->opts.check_interval > 0 ? c->opts.check_interval : 8;
+    }
+    const CgState & h = c->hcg->st;
+    int status        = SWC_OK;
+    if (h.done == 4) launch_zero_active<DIM>(c->L, c->B, c->N.x, c->grid, c->stream);  // b = 0 -> x = 0
+    if (h.done == 2) status = SWC_CG_NOT_CONVERGED;
+    if (h.done == 3) status = SWC_NAN_DETECTED;
+    c->last_iters = std::max(1, h.iter);
+    if (st) {
+        st->n_virtual            = c->hcg->nv;
+        st->active_bricks        = c->hcg->nbricks;
+        st->cg_iterations        = h.iter;
+        st->rhs_norm             = std::sqrt(bb);
+        st->rel_residual         = bb > 0 ? std::sqrt(h.rr / bb) : 0.0;
+        st->initial_rel_residual = bb > 0 ? std::sqrt(rr0 / bb) : 0.0;
+        st->true_rel_residual    = -1;
+        st->status               = status;
+    }
+    if (c->opts.compute_true_residual && st) {
+        launch_true_residual<DIM>(c->L, c->B, c->N, c->S, c->partials, c->res2, c->grid, c->stream);
+        double r2[2];
+        CK(cudaMemcpyAsync(r2, c->res2, sizeof(r2), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        st->true_rel_residual = r2[1] > 0 ? std::sqrt(r2[0] / r2[1]) : 0.0;
+    }
+    return status;
+}
+
+// The shared tail of advance / project: virtual generation, projection, G_i.
+template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
+    mark(c, 3);
+    run_generate<DIM>(c, true);
+    mark(c, 4);
+    launch_warm_start<DIM>(c->L, c->B, c->N, c->opts.warm_start == SWC_WARM_LEARNED ? kWarmNode : c->opts.warm_start,
+                           c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
+    mark(c, 5);
+    int rc = run_cg<DIM>(c, st);
+    if (rc != SWC_OK && rc != SWC_CG_NOT_CONVERGED && rc != SWC_NAN_DETECTED) return rc;
+    const int cg_status = rc;
+    mark(c, 6);
+    launch_pressure_gradient<DIM>(c->pos, c->vel, c->n, c->L, c->P, c->B.flag, c->N.V, c->N.x, c->bpos, c->bvel,
+                                  c->bnrm, c->bcellStart, c->stream);
+    mark(c, 7);
+    // p in reference order (next step's prefix warm start) and N_v for it
+    launch_compact_export<DIM>(c->L, c->B, c->N, c->pcomp, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                               nullptr, nullptr, c->grid, c->stream);
+    CK(cudaMemcpyAsync(c->nv_prev, c->B.seg_off + c->B.nseg, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+    mark(c, 8);
+    if (st) {
+        st->warm_start_used = c->opts.warm_start == SWC_WARM_LEARNED ? SWC_WARM_NODE : c->opts.warm_start;
+        st->n_particles     = c->n;
+        st->n_boundary      = c->nb;
+    }
+    return cg_status;
+}
+
+void save_prev_flags(swc_ctx * c) {
+    using namespace swc;
+    const size_t bn = c->dim == 3 ? BrickGeom<3>::BN : BrickGeom<2>::BN;
+    cudaMemcpyAsync(c->N.flag_prev, c->N.flag, size_t(c->L.nbricks) * bn, cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(c->B.flag_prev, c->B.flag, size_t(c->L.nbricks), cudaMemcpyDeviceToDevice, c->stream);
+}
+
+template<int DIM> int do_advance(swc_ctx * c, double dt, swc_stats * st, bool move) {
+    CK(cudaEventRecord(c->evA, c->stream));
+    mark(c, 0);
+    save_prev_flags(c);
+    if (move) {
+        launch_advect(c->pos, c->vel, c->n, float(dt), c->stream);
+        if (c->has_motion && c->nb > 0) {
+            launch_rotate_boundary(c->bpos, c->bvel, c->bnrm, c->nb, float(c->motion_c[0]), float(c->motion_c[2]),
+                                   float(c->motion_omega), float(dt), c->stream);
+        }
+    }
+    if (move && c->has_motion && c->nb > 0) {
+        // moving solids: rebin the boundary (the motion flag travels in bnrm.w)
+        run_bin_boundary<DIM>(c);
+    }
+    run_bin_real<DIM>(c);
+    mark(c, 1);
+    launch_density<DIM>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->stream);
+    mark(c, 2);
+    if (move) {
+        launch_forces<DIM>(c->pos, c->vel, c->vel2, c->n, c->L, c->P, c->cellStart, float(dt), c->stream);
+        std::swap(c->vel, c->vel2);
+    }
+    int rc = run_projection<DIM>(c, st);
+    if (rc != SWC_OK && rc != SWC_CG_NOT_CONVERGED && rc != SWC_NAN_DETECTED) return rc;
+    const int status = rc;
+    CK(cudaEventRecord(c->evB, c->stream));
+    CK(cudaEventSynchronize(c->evB));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->evA, c->evB);
+    if (st) st->device_ms = ms;
+    if (c->profiling) {
+        for (int k = 0; k < kPhases; k++) {
+            float t = 0;
+            cudaEventElapsedTime(&t, c->ev[k], c->ev[k + 1]);
+            c->phase_ms[k] = t;
+        }
+    }
+    CK(cudaGetLastError());
+    return status;
+}
+
+template<int DIM> int do_initialize(swc_ctx * c) {
+    if (c->n <= 0) {
+        c->err = "no particles";
+        return SWC_BAD_ARG;
+    }
+    run_bin_real<DIM>(c);
+    launch_density<DIM>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->stream);
+    launch_set_volume(c->pos, c->rho, c->n, float(c->scene.mass), c->stream);
+    // V_i per particle id (travels with the particle)
+    launch_scatter_w_to_id(c->pos, c->id, c->n, c->vol_by_id, c->stream);
+    // rho0 = max rho_i (DualParticleSphLiquid.cpp:91)
+    launch_max_positive(c->rho, c->n, c->max_bits, c->stream);
+    int bits = 0;
+    CK(cudaMemcpyAsync(&bits, c->max_bits, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    // boundary
+    if (c->nb > 0) {
+        run_bin_boundary<DIM>(c);
+        launch_boundary_density<DIM>(c->bpos, c->bvel, c->brho, c->nb, c->L, c->P, c->bcellStart, c->stream);
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    float rmax = 0;
+    std::memcpy(&rmax, &bits, sizeof(float));
+    c->rho0   = c->scene.target_density > 0 ? c->scene.target_density : double(rmax);
+    c->kappa  = c->scene.kappa >= 0 ? c->scene.kappa : 0.0;
+    if (c->scene.kappa < 0) {
+        const double r = c->scene.particle_radius, h = 4 * r;
+        const int d    = c->dim;
+        const double packed = d == 2 ? kernelW(0, h, d) + kernelW(r * 2, h, d) * 6 +
+                                           kernelW(r * 2 * std::numbers::sqrt3, h, d) * 6
+                                     : kernelW(0, h, d) + kernelW(r * 2, h, d) * 12 +
+                                           kernelW(r * 2 * std::numbers::sqrt2, h, d) * 6 +
+                                           kernelW(r * 2 * std::numbers::sqrt3, h, d) * 24;
+        c->kappa = 1.0 / packed;
+    }
+    setup_phys(c);
+    // alpha0 = max diagonal with the clamp off, in FP64 (VirtualParticle::setAlpha)
+    run_generate<DIM>(c, false);
+    launch_diag_max_f64<DIM>(c->L, c->B, c->N, c->SD, c->diag_bits, c->grid, c->stream);
+    unsigned long long dbits = 0;
+    CK(cudaMemcpyAsync(&dbits, c->diag_bits, sizeof(dbits), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    double a0 = 0;
+    std::memcpy(&a0, &dbits, sizeof(double));
+    c->alpha0 = dbits ? a0 : -1e6;
+    setup_phys(c);
+    // no previous pressure: empty prefix
+    CK(cudaMemsetAsync(c->nv_prev, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(c->N.x, 0, sizeof(float) * size_t(c->L.nbricks) * (DIM == 3 ? 512 : 256), c->stream));
+    CK(cudaMemsetAsync(c->N.flag, 0, size_t(c->L.nbricks) * (DIM == 3 ? 512 : 256), c->stream));
+    CK(cudaMemsetAsync(c->B.flag, 0, size_t(c->L.nbricks), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+    c->initialized = true;
+    return SWC_OK;
+}
+
+bool valid_ctx(const swc_ctx * c) { return c != nullptr; }
+
+}  // namespace
+
+extern "C" {
+
+void swc_default_solver_opts(swc_solver_opts * o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->tolerance      = 1e-6;
+    o->max_iterations = -1;
+    o->warm_start     = SWC_WARM_PREFIX;
+}
+
+const char * swc_status_str(int s) {
+    switch (s) {
+    case SWC_OK: return "ok";
+    case SWC_CG_NOT_CONVERGED: return "CG did not converge";
+    case SWC_NAN_DETECTED: return "NaN or breakdown detected";
+    case SWC_BAD_ARG: return "bad argument";
+    case SWC_CUDA_ERROR: return "CUDA error";
+    case SWC_NOT_INITIALIZED: return "not initialized";
+    case SWC_OUT_OF_MEMORY: return "out of device memory";
+    default: return "unknown status";
+    }
+}
+
+const char * swc_last_error(const swc_ctx * c) { return c ? c->err.c_str() : "null context"; }
+
+int swc_create(const swc_scene * s, const swc_solver_opts * o, swc_ctx ** out) {
+    if (!s || !out) return SWC_BAD_ARG;
+    *out = nullptr;
+    if ((s->dim != 2 && s->dim != 3) || !(s->particle_radius > 0) || !(s->grid_spacing > 0) || !(s->mass > 0) ||
+        s->grid_size[0] < 1 || s->grid_size[1] < 1 || (s->dim == 3 && s->grid_size[2] < 1))
+        return SWC_BAD_ARG;
+    auto * c  = new swc_ctx();
+    c->dim    = s->dim;
+    c->scene  = *s;
+    if (s->boundary_mass <= 0) c->scene.boundary_mass = s->mass;
+    if (o) c->opts = *o;
+    else swc_default_solver_opts(&c->opts);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        c->err = "no CUDA device";
+        delete c;
+        return SWC_CUDA_ERROR;
+    }
+    cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    Lattice & L = c->L;
+    L.ox = float(s->grid_origin[0]);
+    L.oy = float(s->grid_origin[1]);
+    L.oz = float(s->dim == 3 ? s->grid_origin[2] : 0.0);
+    L.ox_d = s->grid_origin[0];
+    L.oy_d = s->grid_origin[1];
+    L.oz_d = s->dim == 3 ? s->grid_origin[2] : 0.0;
+    L.dx   = float(s->grid_spacing);
+    L.dx_d = s->grid_spacing;
+    L.inv_dx = float(1.0 / s->grid_spacing);
+    L.nx = s->grid_size[0];
+    L.ny = s->grid_size[1];
+    L.nz = s->dim == 3 ? s->grid_size[2] : 1;
+    const int bx = s->dim == 3 ? 8 : 16, by = s->dim == 3 ? 8 : 16, bz = s->dim == 3 ? 8 : 1;
+    L.bnx = (L.nx + bx - 1) / bx;
+    L.bny = (L.ny + by - 1) / by;
+    L.bnz = (L.nz + bz - 1) / bz;
+    L.nbricks = L.bnx * L.bny * L.bnz;
+    L.ncells  = (long long) L.nx * L.ny * L.nz;
+    if ((long long) L.nbricks * bx * by * bz > (1LL << 31) - 1 || L.ncells > (1LL << 31) - 2) {
+        c->err = "node grid too large";
+        delete c;
+        return SWC_BAD_ARG;
+    }
+    c->grid = std::max(1, std::min(L.nbricks, c->num_sms * 8));
+    setup_phys(c);
+    int rc = SWC_OK;
+    const size_t slots = size_t(L.nbricks) * bx * by * bz;
+    auto fail = [&](int r) {
+        swc_destroy(c);
+        return r;
+    };
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(SWC_CUDA_ERROR);
+    c->own_stream = true;
+    if ((rc = dalloc(c, &c->N.flag, slots)) || (rc = dalloc(c, &c->N.flag_prev, slots)) ||
+        (rc = dalloc(c, &c->N.V, slots)) || (rc = dalloc(c, &c->N.D, slots)) || (rc = dalloc(c, &c->N.rho, slots)) ||
+        (rc = dalloc(c, &c->N.ahat, slots)) || (rc = dalloc(c, &c->N.x, slots)) || (rc = dalloc(c, &c->N.r, slots)) ||
+        (rc = dalloc(c, &c->N.q, slots)) || (rc = dalloc(c, &c->N.d0, slots)) || (rc = dalloc(c, &c->N.d1, slots)))
+        return fail(rc);
+    if (c->opts.keep_virtual_velocity && (rc = dalloc(c, &c->N.vbar, slots))) return fail(rc);
+    if (c->opts.keep_features && (rc = dalloc(c, &c->N.nreal, slots))) return fail(rc);
+    c->B.nseg = (long long) L.ny * L.nz * L.bnx;
+    if ((rc = dalloc(c, &c->B.flag, L.nbricks)) || (rc = dalloc(c, &c->B.flag_prev, L.nbricks)) ||
+        (rc = dalloc(c, &c->B.list, L.nbricks)) || (rc = dalloc(c, &c->B.count, 1)) ||
+        (rc = dalloc(c, &c->B.seg, c->B.nseg)) || (rc = dalloc(c, &c->B.seg_off, c->B.nseg + 1)))
+        return fail(rc);
+    if ((rc = dalloc(c, &c->pcomp, size_t(L.ncells))) || (rc = dalloc(c, &c->nv_prev, 1)) ||
+        (rc = dalloc(c, &c->scan_tiles, scan_tile_count(std::max<long long>(c->B.nseg, L.ncells) + 1) + 2)) ||
+        (rc = dalloc(c, &c->cg, 1)) || (rc = dalloc(c, &c->partials, 2 * size_t(c->grid) + 8)) ||
+        (rc = dalloc(c, &c->diag_bits, 1)) || (rc = dalloc(c, &c->max_bits, 1)) || (rc = dalloc(c, &c->res2, 2)) ||
+        (rc = dalloc(c, &c->cellStart, L.ncells + 1)) || (rc = dalloc(c, &c->bcellStart, L.ncells + 1)))
+        return fail(rc);
+    if (cudaMallocHost(reinterpret_cast<void **>(&c->hcg), sizeof(HostCg)) != cudaSuccess) return fail(SWC_OUT_OF_MEMORY);
+    cudaMemsetAsync(c->cg, 0, sizeof(CgState), c->stream);
+    cudaMemsetAsync(c->partials, 0, sizeof(double) * (2 * size_t(c->grid) + 8), c->stream);
+    cudaMemsetAsync(c->B.flag, 0, L.nbricks, c->stream);
+    cudaMemsetAsync(c->B.flag_prev, 0, L.nbricks, c->stream);
+    cudaMemsetAsync(c->N.flag, 0, slots, c->stream);
+    cudaMemsetAsync(c->N.x, 0, slots * sizeof(float), c->stream);
+    cudaMemsetAsync(c->nv_prev, 0, sizeof(int), c->stream);
+    cudaMemsetAsync(c->bcellStart, 0, sizeof(int) * (L.ncells + 1), c->stream);
+    for (auto & e : c->ev) cudaEventCreate(&e);
+    cudaEventCreate(&c->evA);
+    cudaEventCreate(&c->evB);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(SWC_CUDA_ERROR);
+    *out = c;
+    return SWC_OK;
+}
+
+void swc_destroy(swc_ctx * c) {
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->g1) cudaGraphExecDestroy(c->g1);
+    if (c->g8) cudaGraphExecDestroy(c->g8);
+    dfree(c->pos);
+    dfree(c->vel);
+    dfree(c->vel2);
+    dfree(c->id);
+    dfree(c->rho);
+    dfree(c->vol_by_id);
+    dfree(c->stage);
+    dfree(c->cellStart);
+    free_sort(c->sortR);
+    dfree(c->bpos);
+    dfree(c->bvel);
+    dfree(c->bnrm);
+    dfree(c->bid);
+    dfree(c->brho);
+    dfree(c->bcellStart);
+    dfree(c->bstage);
+    free_sort(c->sortB);
+    dfree(c->N.flag);
+    dfree(c->N.flag_prev);
+    dfree(c->N.V);
+    dfree(c->N.D);
+    dfree(c->N.rho);
+    dfree(c->N.ahat);
+    dfree(c->N.x);
+    dfree(c->N.r);
+    dfree(c->N.q);
+    dfree(c->N.d0);
+    dfree(c->N.d1);
+    dfree(c->N.vbar);
+    dfree(c->N.nreal);
+    dfree(c->B.flag);
+    dfree(c->B.flag_prev);
+    dfree(c->B.list);
+    dfree(c->B.count);
+    dfree(c->B.seg);
+    dfree(c->B.seg_off);
+    dfree(c->pcomp);
+    dfree(c->nv_prev);
+    dfree(c->scan_tiles);
+    dfree(c->cg);
+    dfree(c->partials);
+    dfree(c->diag_bits);
+    dfree(c->max_bits);
+    dfree(c->res2);
+    if (c->hcg) cudaFreeHost(c->hcg);
+    for (auto & e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->evA) cudaEventDestroy(c->evA);
+    if (c->evB) cudaEventDestroy(c->evB);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int swc_set_stream(swc_ctx * c, void * stream) {
+    if (!valid_ctx(c)) return SWC_BAD_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->g1) cudaGraphExecDestroy(c->g1);
+    if (c->g8) cudaGraphExecDestroy(c->g8);
+    c->g1 = c->g8 = nullptr;
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    if (stream) {
+        c->stream     = static_cast<cudaStream_t>(stream);
+        c->own_stream = false;
+    } else {
+        CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+    }
+    return SWC_OK;
+}
+
+int swc_set_solver_opts(swc_ctx * c, const swc_solver_opts * o) {
+    if (!valid_ctx(c) || !o) return SWC_BAD_ARG;
+    const bool need_vbar = o->keep_virtual_velocity && !c->N.vbar;
+    const bool need_feat = o->keep_features && !c->N.nreal;
+    c->opts = *o;
+    const size_t slots = size_t(c->L.nbricks) * (c->dim == 3 ? 512 : 256);
+    int rc;
+    if (need_vbar || need_feat) {
+        CK(cudaStreamSynchronize(c->stream));
+        if (c->g1) cudaGraphExecDestroy(c->g1);
+        if (c->g8) cudaGraphExecDestroy(c->g8);
+        c->g1 = c->g8 = nullptr;
+    }
+    if (need_vbar && (rc = dalloc(c, &c->N.vbar, slots))) return rc;
+    if (need_feat && (rc = dalloc(c, &c->N.nreal, slots))) return rc;
+    return SWC_OK;
+}
+
+int swc_set_particles(swc_ctx * c, const double * x, const double * v, int64_t n) {
+    if (!valid_ctx(c) || n < 0 || (n > 0 && !x)) return SWC_BAD_ARG;
+    if (n > (1LL << 30)) return SWC_BAD_ARG;
+    int rc;
+    if (n != c->n || !c->pos) {
+        if (c->initialized && n != c->n) {
+            c->err = "particle count changed after initialize";
+            return SWC_BAD_ARG;
+        }
+        CK(cudaStreamSynchronize(c->stream));
+        if ((rc = dalloc(c, &c->pos, n)) || (rc = dalloc(c, &c->vel, n)) || (rc = dalloc(c, &c->vel2, n)) ||
+            (rc = dalloc(c, &c->id, n)) || (rc = dalloc(c, &c->rho, n)) || (rc = dalloc(c, &c->vol_by_id, n)) ||
+            (rc = dalloc(c, &c->stage, size_t(2) * std::max<int64_t>(n, 1) * c->dim)))
+            return rc;
+        if ((rc = alloc_sort(c, c->sortR, n, false))) return rc;
+        c->n = n;
+    }
+    const size_t bytes = sizeof(double) * size_t(n) * c->dim;
+    CK(cudaMemcpyAsync(c->stage, x, bytes, cudaMemcpyHostToDevice, c->stream));
+    if (v) CK(cudaMemcpyAsync(c->stage + size_t(n) * c->dim, v, bytes, cudaMemcpyHostToDevice, c->stream));
+    launch_import(c->stage, v ? c->stage + size_t(n) * c->dim : nullptr, c->dim, n, c->pos, c->vel, c->id, c->stream);
+    if (c->initialized) launch_fill_w_by_id(c->pos, c->vol_by_id, nullptr, n, c->stream);  // ids are 0..n-1 here
+    CK(cudaGetLastError());
+    return SWC_OK;
+}
+
+int swc_get_particles(swc_ctx * c, double * x, double * v, int64_t n) {
+    if (!valid_ctx(c) || n != c->n) return SWC_BAD_ARG;
+    double * sx = c->stage;
+    double * sv = c->stage + size_t(n) * c->dim;
+    launch_export(c->pos, c->vel, c->id, c->dim, n, x ? sx : nullptr, v ? sv : nullptr, c->stream);
+    const size_t bytes = sizeof(double) * size_t(n) * c->dim;
+    if (x) CK(cudaMemcpyAsync(x, sx, bytes, cudaMemcpyDeviceToHost, c->stream));
+    if (v) CK(cudaMemcpyAsync(v, sv, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SWC_OK;
+}
+
+int swc_set_boundary(swc_ctx * c, const double * x, const double * nrm, const double * v, int64_t nb) {
+    if (!valid_ctx(c) || nb < 0 || (nb > 0 && (!x || !nrm))) return SWC_BAD_ARG;
+    int rc;
+    CK(cudaStreamSynchronize(c->stream));
+    if ((rc = dalloc(c, &c->bpos, nb)) || (rc = dalloc(c, &c->bvel, nb)) || (rc = dalloc(c, &c->bnrm, nb)) ||
+        (rc = dalloc(c, &c->bid, nb)) || (rc = dalloc(c, &c->brho, nb)) ||
+        (rc = dalloc(c, &c->bstage, size_t(3) * std::max<int64_t>(nb, 1) * c->dim)))
+        return rc;
+    if ((rc = alloc_sort(c, c->sortB, nb, true))) return rc;
+    c->nb = nb;
+    const size_t bytes = sizeof(double) * size_t(nb) * c->dim;
+    double * sx = c->bstage;
+    double * sn = c->bstage + size_t(nb) * c->dim;
+    double * sv = c->bstage + 2 * size_t(nb) * c->dim;
+    if (nb > 0) {
+        CK(cudaMemcpyAsync(sx, x, bytes, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(sn, nrm, bytes, cudaMemcpyHostToDevice, c->stream));
+        if (v) CK(cudaMemcpyAsync(sv, v, bytes, cudaMemcpyHostToDevice, c->stream));
+    }
+    launch_import(sx, v ? sv : nullptr, c->dim, nb, c->bpos, c->bvel, c->bid, c->stream);
+    launch_import(sn, nullptr, c->dim, nb, c->bnrm, c->sortB.vel2, nullptr, c->stream);
+    if (c->dim == 2) run_bin_boundary<2>(c);
+    else run_bin_boundary<3>(c);
+    c->has_motion = false;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+    return SWC_OK;
+}
+
+int swc_set_boundary_motion(swc_ctx * c, const uint8_t * moving, const double center[3], double omega) {
+    if (!valid_ctx(c) || !moving || !center || c->nb <= 0) return SWC_BAD_ARG;
+    unsigned char * d = nullptr;
+    CK(cudaMalloc(&d, c->nb));
+    CK(cudaMemcpy(d, moving, c->nb, cudaMemcpyHostToDevice));
+    launch_set_moving(c->bnrm, d, c->bid, c->nb, c->stream);
+    CK(cudaStreamSynchronize(c->stream));
+    cudaFree(d);
+    c->has_motion   = true;
+    c->motion_omega = omega;
+    for (int a = 0; a < 3; a++) c->motion_c[a] = center[a];
+    return SWC_OK;
+}
+
+int swc_initialize(swc_ctx * c) {
+    if (!valid_ctx(c)) return SWC_BAD_ARG;
+    int rc = c->dim == 2 ? do_initialize<2>(c) : do_initialize<3>(c);
+    return rc;
+}
+
+int swc_advance(swc_ctx * c, double dt, swc_stats * st) {
+    if (!valid_ctx(c)) return SWC_BAD_ARG;
+    if (!c->initialized) return SWC_NOT_INITIALIZED;
+    if (!(dt >= 0) || !std::isfinite(dt)) return SWC_BAD_ARG;
+    if (st) std::memset(st, 0, sizeof(*st));
+    return c->dim == 2 ? do_advance<2>(c, dt, st, true) : do_advance<3>(c, dt, st, true);
+}
+
+int swc_project(swc_ctx * c, swc_stats * st) {
+    if (!valid_ctx(c)) return SWC_BAD_ARG;
+    if (!c->initialized) return SWC_NOT_INITIALIZED;
+    if (st) std::memset(st, 0, sizeof(*st));
+    return c->dim == 2 ? do_advance<2>(c, 0.0, st, false) : do_advance<3>(c, 0.0, st, false);
+}
+
+int swc_get_time_step(swc_ctx * c, double step_rate, double * dt) {
+    if (!valid_ctx(c) || !dt) return SWC_BAD_ARG;
+    std::vector<double> v(size_t(c->n) * c->dim);
+    int rc = swc_get_particles(c, nullptr, v.data(), c->n);
+    if (rc) return rc;
+    double m2 = 0;
+    for (long long i = 0; i < c->n; i++) {
+        double s = 0;
+        for (int a = 0; a < c->dim; a++) s += v[i * c->dim + a] * v[i * c->dim + a];
+        m2 = std::max(m2, s);
+    }
+    *dt = step_rate * c->scene.particle_radius * 2 / std::sqrt(m2);
+    return SWC_OK;
+}
+
+int swc_get_real_info(swc_ctx * c, double * rho, double * vol, int64_t n) {
+    if (!valid_ctx(c) || n != c->n) return SWC_BAD_ARG;
+    double * s0 = c->stage;
+    double * s1 = c->stage + size_t(n) * c->dim;
+    if (rho) launch_export_scalar(c->rho, 1, 0, c->id, n, s0, c->stream);
+    if (vol) launch_export_scalar(reinterpret_cast<const float *>(c->pos), 4, 3, c->id, n, s1, c->stream);
+    if (rho) CK(cudaMemcpyAsync(rho, s0, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (vol) CK(cudaMemcpyAsync(vol, s1, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SWC_OK;
+}
+
+int swc_set_volumes(swc_ctx * c, const double * vol, int64_t n) {
+    if (!valid_ctx(c) || n != c->n || !vol) return SWC_BAD_ARG;
+    std::vector<float> vf(vol, vol + n);
+    CK(cudaMemcpy(c->vol_by_id, vf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    launch_fill_w_by_id(c->pos, c->vol_by_id, c->id, n, c->stream);
+    CK(cudaStreamSynchronize(c->stream));
+    return SWC_OK;
+}
+
+int swc_get_boundary_info(swc_ctx * c, double * rho, double * vol, int64_t nb) {
+    if (!valid_ctx(c) || nb != c->nb) return SWC_BAD_ARG;
+    if (nb == 0) return SWC_OK;
+    double * s0 = c->bstage;
+    double * s1 = c->bstage + size_t(nb) * c->dim;
+    if (rho) launch_export_scalar(c->brho, 1, 0, c->bid, nb, s0, c->stream);
+    if (vol) launch_export_scalar(reinterpret_cast<const float *>(c->bpos), 4, 3, c->bid, nb, s1, c->stream);
+    if (rho) CK(cudaMemcpyAsync(rho, s0, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
+    if (vol) CK(cudaMemcpyAsync(vol, s1, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SWC_OK;
+}
+
+int swc_set_boundary_info(swc_ctx * c, const double * rho, const double * vol, int64_t nb) {
+    if (!valid_ctx(c) || nb != c->nb || !rho || !vol) return SWC_BAD_ARG;
+    if (nb == 0) return SWC_OK;
+    std::vector<float> r(rho, rho + nb), v(vol, vol + nb);
+    float * tmp = nullptr;
+    CK(cudaMalloc(&tmp, sizeof(float) * 2 * nb));
+    cudaMemcpy(tmp, r.data(), sizeof(float) * nb, cudaMemcpyHostToDevice);
+    cudaMemcpy(tmp + nb, v.data(), sizeof(float) * nb, cudaMemcpyHostToDevice);
+    launch_set_boundary_info(c->bpos, c->bvel, c->brho, tmp, tmp + nb, c->bid, nb, float(c->scene.boundary_mass),
+                             c->stream);
+    cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    CK(cudaGetLastError());
+    return SWC_OK;
+}
+
+int swc_get_scalars(swc_ctx * c, double * rho0, double * alpha0, double * kappa) {
+    if (!valid_ctx(c)) return SWC_BAD_ARG;
+    if (rho0) *rho0 = c->rho0;
+    if (alpha0) *alpha0 = c->alpha0;
+    if (kappa) *kappa = c->kappa;
+    return SWC_OK;
+}
+
+int swc_set_scalars(swc_ctx * c, double rho0, double alpha0, double kappa) {
+    if (!valid_ctx(c) || !(rho0 > 0)) return SWC_BAD_ARG;
+    c->rho0   = rho0;
+    c->alpha0 = alpha0;
+    c->kappa  = kappa;
+    setup_phys(c);
+    return SWC_OK;
+}
+
+int64_t swc_num_virtual(swc_ctx * c) {
+    if (!valid_ctx(c)) return -1;
+    int nv = 0;
+    if (cudaMemcpy(&nv, c->B.seg_off + c->B.nseg, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    return nv;
+}
+
+int swc_get_virtual(swc_ctx * c, int64_t * node_id, double * rho, double * vol, double * vbar, double * div,
+                    double * ahat, double * p, int64_t capacity) {
+    if (!valid_ctx(c)) return SWC_BAD_ARG;
+    const int64_t nv = swc_num_virtual(c);
+    if (nv < 0) return SWC_CUDA_ERROR;
+    if (capacity < nv) return SWC_BAD_ARG;
+    if (vbar && !c->N.vbar) {
+        c->err = "vbar not kept (keep_virtual_velocity = 0)";
+        return SWC_BAD_ARG;
+    }
+    const size_t n1 = std::max<int64_t>(nv, 1);
+    long long * d_id = nullptr;
+    double * d_buf   = nullptr;
+    CK(cudaMalloc(&d_id, sizeof(long long) * n1));
+    CK(cudaMalloc(&d_buf, sizeof(double) * n1 * (5 + c->dim)));
+    double *dr = d_buf, *dv = d_buf + n1, *dd = d_buf + 2 * n1, *da = d_buf + 3 * n1, *dp = d_buf + 4 * n1,
+           *dvb = d_buf + 5 * n1;
+    if (c->dim == 2)
+        launch_compact_export<2>(c->L, c->B, c->N, nullptr, d_id, dr, dv, vbar ? dvb : nullptr, dd, da, dp, nullptr,
+                                 c->grid, c->stream);
+    else
+        launch_compact_export<3>(c->L, c->B, c->N, nullptr, d_id, dr, dv, vbar ? dvb : nullptr, dd, da, dp, nullptr,
+                                 c->grid, c->stream);
+    cudaStreamSynchronize(c->stream);
+    if (nv > 0) {
+        if (node_id) cudaMemcpy(node_id, d_id, sizeof(long long) * nv, cudaMemcpyDeviceToHost);
+        if (rho) cudaMemcpy(rho, dr, sizeof(double) * nv, cudaMemcpyDeviceToHost);
+        if (vol) cudaMemcpy(vol, dv, sizeof(double) * nv, cudaMemcpyDeviceToHost);
+        if (div) cudaMemcpy(div, dd, sizeof(double) * nv, cudaMemcpyDeviceToHost);
+        if (ahat) cudaMemcpy(ahat, da, sizeof(double) * nv, cudaMemcpyDeviceToHost);
+        if (p) cudaMemcpy(p, dp, sizeof(double) * nv, cudaMemcpyDeviceToHost);
+        if (vbar) cudaMemcpy(vbar, dvb, sizeof(double) * nv * c->dim, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(d_id);
+    cudaFree(d_buf);
+    CK(cudaGetLastError());
+    return SWC_OK;
+}
+
+int swc_set_pressure(swc_ctx * c, const double * p, int64_t n) {
+    if (!valid_ctx(c) || n < 0 || (n > 0 && !p) || n > c->L.ncells) return SWC_BAD_ARG;
+    std::vector<float> f(p, p + n);
+    if (n > 0) CK(cudaMemcpy(c->pcomp, f.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    int ni = int(n);
+    CK(cudaMemcpy(c->nv_prev, &ni, sizeof(int), cudaMemcpyHostToDevice));
+    return SWC_OK;
+}
+
+int swc_apply_operator(swc_ctx * c, const double * x, double * y, int64_t n) {
+    if (!valid_ctx(c) || !x || !y) return SWC_BAD_ARG;
+    const int64_t nv = swc_num_virtual(c);
+    if (n != nv) return SWC_BAD_ARG;
+    const size_t slots = size_t(c->L.nbricks) * (c->dim == 3 ? 512 : 256);
+    double * d_in = nullptr;
+    double * d_out = nullptr;
+    float * t_in = nullptr;
+    float * t_out = nullptr;
+    CK(cudaMalloc(&d_in, sizeof(double) * std::max<int64_t>(n, 1)));
+    CK(cudaMalloc(&d_out, sizeof(double) * std::max<int64_t>(n, 1)));
+    CK(cudaMalloc(&t_in, sizeof(float) * slots));
+    CK(cudaMalloc(&t_out, sizeof(float) * slots));
+    cudaMemcpy(d_in, x, sizeof(double) * n, cudaMemcpyHostToDevice);
+    // brick-layout vector: reuse compact export machinery through a temporary NodeArrays view
+    if (c->dim == 2) {
+        launch_compact_import<2>(c->L, c->B, c->N, d_in, t_in, c->grid, c->stream);
+        launch_apply_operator<2>(c->L, c->B, c->N, c->S, t_in, t_out, c->grid, c->stream);
+        NodeArrays T = c->N;
+        T.x          = t_out;
+        launch_compact_export<2>(c->L, c->B, T, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, d_out,
+                                 nullptr, c->grid, c->stream);
+    } else {
+        launch_compact_import<3>(c->L, c->B, c->N, d_in, t_in, c->grid, c->stream);
+        launch_apply_operator<3>(c->L, c->B, c->N, c->S, t_in, t_out, c->grid, c->stream);
+        NodeArrays T = c->N;
+        T.x          = t_out;
+        launch_compact_export<3>(c->L, c->B, T, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, d_out,
+                                 nullptr, c->grid, c->stream);
+    }
+    cudaStreamSynchronize(c->stream);
+    cudaMemcpy(y, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    cudaFree(d_in);
+    cudaFree(d_out);
+    cudaFree(t_in);
+    cudaFree(t_out);
+    CK(cudaGetLastError());
+    return SWC_OK;
+}
+
+int swc_set_profiling(swc_ctx * c, int on) {
+    if (!valid_ctx(c)) return SWC_BAD_ARG;
+    c->profiling = on != 0;
+    return SWC_OK;
+}
+
+int swc_get_phase_times(swc_ctx * c, double * ms, int n) {
+    if (!valid_ctx(c) || !ms) return SWC_BAD_ARG;
+    for (int k = 0; k < n && k < kPhases; k++) ms[k] = c->phase_ms[k];
+    return SWC_OK;
+}
+
+int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
+    if (!valid_ctx(c) || !mean_ms || reps <= 0 || !c->initialized) return SWC_BAD_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    // keep the solver state: run the CG kernels against a scratch copy of the scalars
+    CgState saved{};
+    CK(cudaMemcpy(&saved, c->cg, sizeof(CgState), cudaMemcpyDeviceToHost));
+    CgState run = saved;
+    run.done      = 0;
+    run.iter      = 2;  // beta path of the SpMV
+    run.threshold = 0;  // never converge while timing
+    run.max_iter  = 0x7fffffff;
+    if (!(run.rr_prev > 0)) run.rr_prev = 1, run.rr = 1;
+    if (!(run.pq != 0)) run.pq = 1;
+    CK(cudaMemcpy(c->cg, &run, sizeof(CgState), cudaMemcpyHostToDevice));
+    float * x_save = nullptr;
+    const size_t slots = size_t(c->L.nbricks) * (c->dim == 3 ? 512 : 256);
+    if (which == 1) {
+        CK(cudaMalloc(&x_save, sizeof(float) * slots * 2));
+        cudaMemcpy(x_save, c->N.x, sizeof(float) * slots, cudaMemcpyDeviceToDevice);
+        cudaMemcpy(x_save + slots, c->N.r, sizeof(float) * slots, cudaMemcpyDeviceToDevice);
+    }
+    float4 * vel_save = nullptr;
+    if (which == 3) {
+        CK(cudaMalloc(&vel_save, sizeof(float4) * std::max<long long>(c->n, 1)));
+        cudaMemcpy(vel_save, c->vel, sizeof(float4) * c->n, cudaMemcpyDeviceToDevice);
+    }
+    auto launch = [&]() {
+        if (c->dim == 3) {
+            switch (which) {
+            case 0: launch_cg_spmv<3>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->grid, c->stream); break;
+            case 1: launch_cg_update<3>(c->B, c->N, c->cg, c->partials, c->grid, c->stream); break;
+            case 2:
+                launch_node_gather<3>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel,
+                                      c->bcellStart, c->grid, c->stream);
+                break;
+            case 3:
+                launch_pressure_gradient<3>(c->pos, c->vel, c->n, c->L, c->P, c->B.flag, c->N.V, c->N.x, c->bpos,
+                                            c->bvel, c->bnrm, c->bcellStart, c->stream);
+                break;
+            case 4: launch_density<3>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->stream); break;
+            case 5: launch_forces<3>(c->pos, c->vel, c->vel2, c->n, c->L, c->P, c->cellStart, 0.f, c->stream); break;
+            }
+        } else {
+            switch (which) {
+            case 2:
+                launch_node_gather<2>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel,
+                                      c->bcellStart, c->grid, c->stream);
+                break;
+            case 4: launch_density<2>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->stream); break;
+            default: break;
+            }
+        }
+    };
+    launch();  // warm
+    CK(cudaEventRecord(c->evA, c->stream));
+    for (int k = 0; k < reps; k++) launch();
+    CK(cudaEventRecord(c->evB, c->stream));
+    CK(cudaEventSynchronize(c->evB));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->evA, c->evB);
+    *mean_ms = ms / reps;
+    CK(cudaMemcpy(c->cg, &saved, sizeof(CgState), cudaMemcpyHostToDevice));
+    if (x_save) {
+        cudaMemcpy(c->N.x, x_save, sizeof(float) * slots, cudaMemcpyDeviceToDevice);
+        cudaMemcpy(c->N.r, x_save + slots, sizeof(float) * slots, cudaMemcpyDeviceToDevice);
+        cudaFree(x_save);
+    }
+    if (vel_save) {
+        cudaMemcpy(c->vel, vel_save, sizeof(float4) * c->n, cudaMemcpyDeviceToDevice);
+        cudaFree(vel_save);
+    }
+    CK(cudaGetLastError());
+    return SWC_OK;
+}
+
+void * swc_host_alloc(size_t bytes) {
+    void * p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+    return p;
+}
+void swc_host_free(void * p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

@@ -1,0 +1,213 @@
+// swc_common.cuh -- shared device-side definitions of the GB300 dual-particle
+// SPH projection: lattice and brick addressing, the cubic-spline kernel, the
+// float-float (double-float) accumulator used by the CG reductions, and the
+// launcher declarations shared between translation units.
+//
+// Layout in HBM
+//   * Real and boundary particles are kept sorted by cell (cells are the node
+//     cells of the virtual-node lattice, x fastest), as SoA float4 arrays:
+//       pos = (x, y, z, V_i)    vel = (vx, vy, vz, m / rho_i)
+//     plus an int32 id (original index).  cellStart[ncells + 1] indexes them.
+//   * Node-lattice data (virtual particles) lives in 8x8x8 bricks (16x16 in 2D),
+//     addressed directly by brick id: value(node) = a[brick * BN + local].  Only
+//     bricks flagged active are touched; inactive bricks read as zero.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace swc {
+
+// --------------------------------------------------------------------------
+// Brick geometry
+// --------------------------------------------------------------------------
+template<int DIM> struct BrickGeom;
+template<> struct BrickGeom<3> {
+    static constexpr int BX = 8, BY = 8, BZ = 8, BN = 512;
+    static constexpr int HALO = 4;                                    // virtual stencil reach (|k|^2 < 16)
+    static constexpr int TX = BX + 2 * HALO, TY = BY + 2 * HALO, TZ = BZ + 2 * HALO;
+    static constexpr int PX = 24;                                     // padded row pitch (conflict-free)
+    static constexpr int PXY = PX * TY;
+    static constexpr int TILE = PXY * TZ;
+};
+template<> struct BrickGeom<2> {
+    static constexpr int BX = 16, BY = 16, BZ = 1, BN = 256;
+    static constexpr int HALO = 4;
+    static constexpr int TX = BX + 2 * HALO, TY = BY + 2 * HALO, TZ = 1;
+    static constexpr int PX = 24;
+    static constexpr int PXY = PX * TY;
+    static constexpr int TILE = PXY;
+};
+
+// Lattice of nodes (= cells) of the virtual-particle grid.
+struct Lattice {
+    float  ox, oy, oz;      // node-grid origin (FP32)
+    float  dx, inv_dx;      // node spacing
+    double ox_d, oy_d, oz_d, dx_d;  // FP64 copies for exact re-tests
+    int    nx, ny, nz;      // node counts (nz = 1 in 2D)
+    int    bnx, bny, bnz;   // brick counts
+    int    nbricks;
+    long long ncells;
+};
+
+// Kernel / physical constants.
+struct Phys {
+    float h, h2, inv_h, c0h, c1h;   // real / boundary kernel, support h = 4 r
+    float H, H2, inv_H, c0H, c1H;   // virtual kernel, support H = 4 * grid spacing
+    double h_d, inv_h_d, c0h_d;     // FP64 copies for the activation re-test
+    float mass, bmass;
+    float rho0, kappa, alpha0;
+    int   cell_lo, cell_hi;         // node-centred cell window for a radius-h query
+    float gx, gy, gz;               // gravity
+    float viscosity;
+    int   gravity_on;
+};
+
+// --------------------------------------------------------------------------
+// Cubic spline (reference: Cores/Structures/SmoothedParticles.h:60-72).
+// --------------------------------------------------------------------------
+__device__ __forceinline__ float kW(float r, float inv_h, float c0) {
+    const float x = r * inv_h;
+    if (x < 0.5f) return c0 * (6.f * x * x * (x - 1.f) + 1.f);
+    if (x < 1.f) {
+        const float t = 1.f - x;
+        return c0 * 2.f * t * t * t;
+    }
+    return 0.f;
+}
+__device__ __forceinline__ float kdW(float r, float inv_h, float c1) {
+    const float x = r * inv_h;
+    if (x < 0.5f) return c1 * x * (3.f * x - 2.f);
+    if (x < 1.f) return -c1 * (1.f - x) * (1.f - x);
+    return 0.f;
+}
+__device__ __forceinline__ double kW_d(double r, double inv_h, double c0) {
+    const double x = r * inv_h;
+    if (x < .5) return c0 * (6 * x * x * (x - 1) + 1);
+    if (x < 1) return c0 * 2 * (1 - x) * (1 - x) * (1 - x);
+    return 0;
+}
+
+// --------------------------------------------------------------------------
+// Float-float accumulation (error-free transforms, Knuth TwoSum / FMA TwoProd).
+// Products are exact; sums keep ~44 significant bits.  Used below the warp
+// level; warp partials are converted to FP64 and summed in FP64.
+// --------------------------------------------------------------------------
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ void ff_add(FF & a, float b) {
+    const float s  = __fadd_rn(a.hi, b);
+    const float bb = __fsub_rn(s, a.hi);
+    const float e  = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    a.hi = s;
+    a.lo = __fadd_rn(a.lo, e);
+}
+__device__ __forceinline__ void ff_add_prod(FF & a, float x, float y) {
+    const float p  = __fmul_rn(x, y);
+    const float pe = __fmaf_rn(x, y, -p);
+    ff_add(a, p);
+    a.lo = __fadd_rn(a.lo, pe);
+}
+__device__ __forceinline__ double ff_to_double(const FF & a) { return double(a.hi) + double(a.lo); }
+
+// Block-wide FP64 sum of one double per thread; result valid in thread 0.
+template<int NT> __device__ __forceinline__ double block_sum_double(double v, double * sm) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sm[w] = v;
+    __syncthreads();
+    double s = 0;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NT / 32; i++) s += sm[i];
+    }
+    __syncthreads();
+    return s;
+}
+
+// Warp-level reduction of a float-float value to FP64 (lane 0), then block FP64 sum.
+template<int NT> __device__ __forceinline__ double block_sum_ff(FF a, double * sm) {
+    double v = ff_to_double(a);
+    return block_sum_double<NT>(v, sm);
+}
+
+// Last-block-done reduction: every block writes `part` to partials[blockIdx.x];
+// the block that finishes last sums all partials in fixed order (deterministic)
+// and returns true with the total in *out (thread 0 only).
+__device__ __forceinline__ bool last_block_reduce(double part, double * partials, unsigned int * ticket,
+                                                  double * out, int * is_last_sm) {
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = part;
+        __threadfence();
+        const unsigned int t = atomicAdd(ticket, 1u);
+        *is_last_sm = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!*is_last_sm) return false;
+    __threadfence();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        volatile double * vp = partials;
+        for (unsigned int b = 0; b < gridDim.x; b++) s += vp[b];
+        *out    = s;
+        *ticket = 0u;
+    }
+    return true;
+}
+
+// --------------------------------------------------------------------------
+// Node / brick addressing.
+// --------------------------------------------------------------------------
+template<int DIM> __device__ __forceinline__ long long node_slot(const Lattice & L, int x, int y, int z) {
+    using G = BrickGeom<DIM>;
+    const int bx = x / G::BX, by = y / G::BY, bz = DIM == 3 ? z / G::BZ : 0;
+    const int lx = x - bx * G::BX, ly = y - by * G::BY, lz = DIM == 3 ? z - bz * G::BZ : 0;
+    const long long b = (long long) bx + (long long) L.bnx * (by + (long long) L.bny * bz);
+    return b * G::BN + lx + G::BX * (ly + G::BY * lz);
+}
+__device__ __forceinline__ int brick_of(const Lattice & L, int x, int y, int z, int bxs, int bys, int bzs) {
+    return x / bxs + L.bnx * (y / bys + L.bny * (z / bzs));
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Cell index of a position (cells = node cells, clamped to the lattice).
+template<int DIM> __device__ __forceinline__ int3 cell_of(const Lattice & L, float x, float y, float z) {
+    int3 c;
+    c.x = clampi(__float2int_rd((x - L.ox) * L.inv_dx), 0, L.nx - 1);
+    c.y = clampi(__float2int_rd((y - L.oy) * L.inv_dx), 0, L.ny - 1);
+    c.z = DIM == 3 ? clampi(__float2int_rd((z - L.oz) * L.inv_dx), 0, L.nz - 1) : 0;
+    return c;
+}
+__device__ __forceinline__ long long cell_linear(const Lattice & L, int3 c) {
+    return (long long) c.x + (long long) L.nx * (c.y + (long long) L.ny * c.z);
+}
+
+// Lower / upper edge of cell row `c` along an axis: border cells extend to infinity
+// (they also hold particles clamped in from outside the lattice).
+__device__ __forceinline__ float slab_dist(float q, int c, int n, float o, float dx) {
+    const float lo = (c == 0) ? -3.0e38f : o + c * dx;
+    const float hi = (c == n - 1) ? 3.0e38f : o + (c + 1) * dx;
+    return q < lo ? lo - q : (q > hi ? q - hi : 0.f);
+}
+
+// --------------------------------------------------------------------------
+// CG device state (one per context).
+// --------------------------------------------------------------------------
+struct CgState {
+    double bb;         // |b|^2
+    double rr;         // |r_i|^2
+    double rr_prev;    // |r_{i-1}|^2
+    double pq;         // d_i . A d_i
+    double threshold;  // max(tol^2 |b|^2, DBL_MIN)
+    double rr0;        // initial |r_0|^2
+    int    iter;       // completed iterations (SpMV count in the loop)
+    int    done;       // 0 running, 1 converged, 2 max iterations, 3 breakdown / NaN
+    int    max_iter;
+    int    pad;
+    unsigned int ticket[4];
+    int    is_last[4];
+};
+
+}  // namespace swc

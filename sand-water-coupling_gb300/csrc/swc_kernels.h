@@ -1,0 +1,141 @@
+// swc_kernels.h -- launcher declarations shared by the translation units of
+// the GB300 dual-particle SPH projection (internal; not part of the C ABI).
+#pragma once
+
+#include "swc_common.cuh"
+
+namespace swc {
+
+// Scratch for the counting sort of one particle set.
+struct SortScratch {
+    int *    key = nullptr, *rank = nullptr, *perm = nullptr, *count = nullptr, *tiles = nullptr;
+    float4 * pos2 = nullptr, *vel2 = nullptr, *aux2 = nullptr;
+    int *    id2 = nullptr;
+};
+
+// Radial stencil coefficients of the virtual Laplacian, indexed by |offset|^2
+// (0..15): c = 2 W'_H(r) / (r + 1e-6) with r = |offset| * grid spacing.
+struct Stencil {
+    float c[16];
+};
+struct StencilD {
+    double c[16];
+};
+
+// Node-lattice arrays (brick layout, indexed by brick * BN + local).
+struct NodeArrays {
+    unsigned char * flag      = nullptr;  // active this step
+    unsigned char * flag_prev = nullptr;  // active in the previous step
+    float *         V         = nullptr;  // virtual volume V_I (0 when inactive)
+    float *         D         = nullptr;  // divergence D_I (CG right-hand side)
+    float *         rho       = nullptr;  // virtual density rho_I
+    float *         ahat      = nullptr;  // clamped diagonal alpha_hat_I (1 when inactive)
+    float *         x         = nullptr;  // pressure (CG solution), kept across steps
+    float *         r         = nullptr;
+    float *         q         = nullptr;
+    float *         d0        = nullptr;
+    float *         d1        = nullptr;
+    float4 *        vbar      = nullptr;  // optional: virtual velocity (debug / export)
+    unsigned short * nreal    = nullptr;  // optional: real neighbours within h
+};
+
+struct BrickArrays {
+    unsigned char * flag      = nullptr;  // active this step
+    unsigned char * flag_prev = nullptr;
+    int *           list      = nullptr;  // active brick ids, ascending
+    int *           count     = nullptr;  // device: number of active bricks
+    int *           seg       = nullptr;  // per (row, brick column) active-node counts
+    int *           seg_off   = nullptr;  // exclusive scan of seg (+ total at the end)
+    long long       nseg      = 0;
+};
+
+// ---- k_particles.cu ----
+void launch_import(const double * x, const double * v, int dim, long long n, float4 * pos, float4 * vel, int * id,
+                   cudaStream_t st);
+void launch_export(const float4 * pos, const float4 * vel, const int * id, int dim, long long n, double * x,
+                   double * v, cudaStream_t st);
+void launch_export_scalar(const float * a, int stride, int comp, const int * id, long long n, double * out,
+                          cudaStream_t st);
+void launch_advect(float4 * pos, const float4 * vel, long long n, float dt, cudaStream_t st);
+void launch_scan(const int * in, long long n, int * out, int * tile_buf, cudaStream_t st);
+long long scan_tile_count(long long n);
+void launch_set_volume(float4 * pos, const float * rho, long long n, float mass, cudaStream_t st);
+void launch_rotate_boundary(float4 * bpos, float4 * bvel, float4 * bnrm, long long nb, float cx, float cz,
+                            float omega, float dt, cudaStream_t st);
+void launch_fill_w_by_id(float4 * pos, const float * vol, const int * id, long long n, cudaStream_t st);
+void launch_scatter_w_to_id(const float4 * pos, const int * id, long long n, float * vol, cudaStream_t st);
+void launch_set_boundary_info(float4 * bpos, float4 * bvel, float * brho, const float * rho, const float * vol,
+                              const int * bid, long long nb, float bmass, cudaStream_t st);
+void launch_set_moving(float4 * bnrm, const unsigned char * moving, const int * bid, long long nb, cudaStream_t st);
+void launch_max_positive(const float * a, long long n, int * out_bits, cudaStream_t st);
+template<int DIM>
+void launch_bin(const Lattice & L, long long n, float4 * pos, float4 * vel, float4 * aux, int * id, SortScratch & S,
+                int * cellStart, cudaStream_t st);
+template<int DIM>
+void launch_density(const float4 * pos, float4 * vel, float * rho, long long n, const Lattice & L, const Phys & P,
+                    const int * cellStart, cudaStream_t st);
+template<int DIM>
+void launch_forces(const float4 * pos, const float4 * vel, float4 * vel_out, long long n, const Lattice & L,
+                   const Phys & P, const int * cellStart, float dt, cudaStream_t st);
+template<int DIM>
+void launch_boundary_density(float4 * bpos, float4 * bvel, float * rho, long long nb, const Lattice & L,
+                             const Phys & P, const int * bcellStart, cudaStream_t st);
+template<int DIM>
+void launch_mark_bricks(const float4 * pos, long long n, const Lattice & L, const Phys & P, unsigned char * bflag,
+                        cudaStream_t st);
+template<int DIM>
+void launch_pressure_gradient(const float4 * pos, float4 * vel, long long n, const Lattice & L, const Phys & P,
+                              const unsigned char * bflag, const float * nodeV, const float * nodeP,
+                              const float4 * bpos, const float4 * bvel, const float4 * bnrm, const int * bcellStart,
+                              cudaStream_t st);
+
+// ---- k_nodes.cu ----
+void launch_brick_list(const unsigned char * bflag, int nbricks, int * list, int * count, cudaStream_t st);
+template<int DIM>
+void launch_node_gather(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
+                        const float4 * pos, const float4 * vel, const int * cellStart, const float4 * bpos,
+                        const float4 * bvel, const int * bcellStart, int grid, cudaStream_t st);
+template<int DIM>
+void launch_segments(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int * tiles, int grid,
+                     cudaStream_t st);
+template<int DIM>
+void launch_ahat(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
+                 int grid, cudaStream_t st);
+template<int DIM>
+void launch_diag_max_f64(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const StencilD & S,
+                         unsigned long long * out_bits, int grid, cudaStream_t st);
+// warm-start modes
+enum { kWarmPrefix = 0, kWarmNode = 1, kWarmZero = 2, kWarmGiven = 3 };
+template<int DIM>
+void launch_warm_start(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int mode, const float * pcomp,
+                       const int * nv_prev, const float * given, int grid, cudaStream_t st);
+template<int DIM>
+void launch_compact_export(const Lattice & L, const BrickArrays & B, const NodeArrays & N, float * pcomp,
+                           long long * node_id, double * rho, double * vol, double * vbar, double * div,
+                           double * ahat, double * p, unsigned short * nreal_out, int grid, cudaStream_t st);
+// CG
+template<int DIM>
+void launch_cg_init(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
+                    double * partials, double tol, int max_iterations, const int * nv, int grid, cudaStream_t st);
+template<int DIM>
+void launch_cg_iteration(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
+                         CgState * cg, double * partials, int grid, cudaStream_t st);
+template<int DIM>
+void launch_cg_spmv(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
+                    double * partials, int grid, cudaStream_t st);
+template<int DIM>
+void launch_cg_update(const BrickArrays & B, const NodeArrays & N, CgState * cg, double * partials, int grid,
+                      cudaStream_t st);
+template<int DIM>
+void launch_apply_operator(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
+                           const float * in, float * out, int grid, cudaStream_t st);
+template<int DIM>
+void launch_zero_active(const Lattice & L, const BrickArrays & B, float * a, int grid, cudaStream_t st);
+template<int DIM>
+void launch_compact_import(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const double * in,
+                           float * out, int grid, cudaStream_t st);
+template<int DIM>
+void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
+                          double * partials, double * out2, int grid, cudaStream_t st);
+
+}  // namespace swc

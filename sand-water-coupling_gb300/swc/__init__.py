@@ -1,0 +1,10 @@
+"""GB300-native dual-particle SPH pressure projection (skytang0205/sand-water-coupling).
+
+``DualParticleSphLiquid`` mirrors the reference's Simulation API over the C ABI
+in include/swc.h; ``scenes`` builds the seeded synthetic workloads.
+"""
+from . import scenes  # noqa: F401
+from ._lib import SwcError, load  # noqa: F401
+from .liquid import DualParticleSphLiquid  # noqa: F401
+
+__all__ = ["DualParticleSphLiquid", "SwcError", "load", "scenes"]

@@ -1,0 +1,59 @@
+"""Generates the golden fixtures in this folder from the CPU FP64 oracle.
+
+The reference publishes no golden vectors and cannot be built here, so these
+fixtures pin the oracle (itself cross-checked against an independent
+brute-force restatement in tests/bruteforce.py) on small seeded scenes:
+initialize + a few advance steps, every intermediate of the projection.
+Inputs are rounded through float32 so the GPU path sees identical values.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "sand-water-coupling_gb300"))
+
+from oracle import oracle as orc  # noqa: E402
+from swc import scenes  # noqa: E402
+
+CASES = {
+    "dam_break_2d_small": (lambda: scenes.dam_break_2d(seed=11, height_cells=16, width_cells=12), 3),
+    "projection_block_3d_n8": (lambda: scenes.projection_block_3d(n=8, seed=12), 2),
+}
+
+
+def make(name):
+    build, steps = CASES[name]
+    s = build().rounded_to_float32()
+    o = orc.Oracle(s)
+    o.initialize()
+    out = {"positions": s.positions, "velocities": s.velocities, "steps": steps, "dt": s.dt}
+    rho, vol = o.real_info()
+    rb, vb = o.boundary_info()
+    sc = o.scalars()
+    out.update(init_rho=rho, init_vol=vol, init_brho=rb, init_bvol=vb, rho0=sc["rho0"], alpha0=sc["alpha0"],
+               kappa=sc["kappa"])
+    for k in range(steps):
+        o.advance(s.dt)
+        v = o.virtual()
+        x, vel = o.particles()
+        st = o.stats()
+        for f in ("node", "rho", "vol", "div", "alpha_hat", "p"):
+            out[f"s{k}_{f}"] = v[f]
+        out[f"s{k}_x"] = x
+        out[f"s{k}_v"] = vel
+        out[f"s{k}_iters"] = st["iterations"]
+        out[f"s{k}_relres"] = st["rel_residual"]
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    return out
+
+
+if __name__ == "__main__":
+    for n in CASES:
+        make(n)
+        print("wrote", n)
