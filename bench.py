@@ -1,0 +1,366 @@
+"""Benchmark of the GB300 dual-particle SPH projection.
+
+Workload (default): the isolated projection benchmark, 128^3 = 2,097,152 fluid
+particles at spacing 0.01 with U(+-0.1 spacing) jitter, N(0, 0.1^2) velocities,
+two boundary layers on all faces (202,816 particles), dt = 5e-4 with gravity,
+CG relative tolerance 1e-5.  One step = DualParticleSphLiquid::advance(dt):
+advection, rho_i, gravity + viscosity, virtual generation, projection (CG), G_i.
+
+Metric: projection steps/s at 2M particles.  ``value`` is device time (CUDA
+events on the library's stream) with the state resident in HBM; ``e2e`` runs the
+same steps through the public API with host FP64 buffers (pinned), the
+host->device copy of each step's particle state and the device->host read of
+its result inside the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl swc|reference]
+
+--impl reference times the reference algorithm's CPU implementation (the FP64
+OpenMP restatement in oracle/, all host threads) on a bounded sample of the
+same workload, scaled to the full particle count.
+Under torchrun each rank runs an independent replica (the path does not
+shard); value = all ranks' steps / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "sand-water-coupling_gb300"))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "projection steps/s at 2M particles (CG to 1e-5 relative residual)"
+UNIT = "steps/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 3 + k and
+                          s[3 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend=backend)
+        return dist, rank, ws
+    return None, rank, ws
+
+
+def reduce_max(dist, value):
+    if dist is None:
+        return value
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_reference(args, n_full, sample_n=48, steps=None, warmup=None):
+    """The reference algorithm's CPU implementation (oracle port, all host threads)
+    on a bounded n^3 sample of the benchmark block; steps/s scaled to n_full particles."""
+    from oracle import oracle as orc
+    from swc import scenes
+
+    orc.build()
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    s = scenes.projection_block_3d(n=sample_n, seed=args.seed)
+    o = orc.Oracle(s)
+    o.initialize()
+    for _ in range(warmup):
+        o.advance(s.dt)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.advance(s.dt)
+    dt = time.perf_counter() - t0
+    sps_sample = steps / dt
+    value = sps_sample * s.n_particles / n_full
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} advance steps of the {sample_n}^3 = {s.n_particles} particle block "
+                      f"({sps_sample:.3f} steps/s), scaled by {s.n_particles}/{n_full} particles",
+            "seconds": dt}
+
+
+def run_reference_arm(args):
+    dist, rank, ws = dist_setup()
+    if rank != 0:
+        return
+    n_full = args.n**3
+    cb = cpu_reference(args, n_full, sample_n=args.cpu_sample, steps=args.steps, warmup=args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / cb["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": workload_config(args),
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args):
+    return {"workload": f"isolated projection block {args.n}^3 = {args.n**3} fluid particles, "
+                        f"{(args.n + 4)**3 - args.n**3} boundary, spacing 0.01, dt 5e-4, tol 1e-5",
+            "particles": args.n**3, "steps_per_replica": args.steps, "warm_start": args.warm_start,
+            "l2": "inputs larger than L2 (particle + node state > 129 MB per step)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def run_gpu_arm(args):
+    import torch
+
+    import swc
+    from swc import _lib, scenes
+
+    dist, rank, ws = dist_setup()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    scene = scenes.projection_block_3d(n=args.n, seed=args.seed + rank)
+    stream = torch.cuda.Stream()
+
+    def make(warm):
+        liq = swc.DualParticleSphLiquid(scene, warm_start=warm, tolerance=1e-5)
+        liq.setStream(stream.cuda_stream)
+        liq.initialize()
+        return liq
+
+    liq = make(args.warm_start)
+    for _ in range(args.warmup):
+        liq.advance(scene.dt)
+    torch.cuda.synchronize()
+    barrier(dist)
+    iters = []
+    with ClockSampler(dev) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(args.steps):
+            st = liq.advance(scene.dt)
+            iters.append(st["cg_iterations"])
+            if st["status"] != 0:
+                raise RuntimeError(f"step failed: {st}")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    barrier(dist)
+    ms = e0.elapsed_time(e1)
+    ms_max = reduce_max(dist, ms)
+    value = ws * args.steps / (ms_max / 1e3)
+    nv = st["n_virtual"]
+    if args.profile_run:
+        # minimal run for profiler captures: the timed steps only
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "steps": args.steps, "ms_per_step": ms_max / args.steps,
+                              "cg_iterations_mean": float(np.mean(iters)), "n_virtual": nv}), flush=True)
+        liq.close()
+        return
+
+    # per-phase device time of one step (profiling events)
+    liq.setProfiling(True)
+    liq.advance(scene.dt)
+    phases = liq.phaseTimes()
+    liq.setProfiling(False)
+
+    # dominant kernels timed live (CUDA events on the library stream)
+    hbm, peak_kind = peaks()
+    kern = {}
+    for which, name in ((0, "cg_spmv"), (1, "cg_update"), (2, "virtual_gather"), (3, "pressure_gradient"),
+                        (4, "density"), (5, "forces")):
+        kern[name] = liq.timeKernel(which, 20)
+    n, nb = scene.n_particles, scene.n_boundary
+    # algorithmic bytes per launch (each array touched once per pass)
+    alg = {
+        "cg_spmv": 24 * nv,  # reads r, d_prev, V, alpha_hat; writes d, q (FP32)
+        "cg_update": 24 * nv,  # reads x, r, d, q; writes x, r
+        "virtual_gather": 32 * (n + nb) + 16 * nv,  # particle pos/vel once; V, D, rho, flag out
+        "pressure_gradient": 32 * n + 8 * nv + 48 * nb,  # pos, vel r/w; V, p; boundary pos/vel/nrm
+        "density": 16 * n + 4 * n + 4 * n,
+        "forces": 32 * n + 16 * n,
+    }
+    cg_ms = kern["cg_spmv"] + kern["cg_update"]
+    dominant = max(("cg_spmv", "virtual_gather", "pressure_gradient"),
+                   key=lambda k: kern[k] * (np.mean(iters) if k == "cg_spmv" else 1))
+    ach = alg[dominant] / (kern[dominant] / 1e3) / 1e9
+    roofline = {"kernel": dominant, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                "frac": ach / hbm, "peak_source": peak_kind, "traffic": None,
+                "per_kernel_ms": kern, "per_kernel_GBps": {k: alg[k] / (kern[k] / 1e3) / 1e9 for k in kern},
+                "cg_iteration_ms": cg_ms}
+
+    # end-to-end through the public API with pinned host buffers
+    L = _lib.load()
+    dim = 3
+    nbytes = n * dim * 8
+    hx_p = L.swc_host_alloc(nbytes)
+    hv_p = L.swc_host_alloc(nbytes)
+    hx = np.frombuffer((C.c_double * (n * dim)).from_address(hx_p), dtype=np.float64).reshape(n, dim)
+    hv = np.frombuffer((C.c_double * (n * dim)).from_address(hv_p), dtype=np.float64).reshape(n, dim)
+    x0, v0 = liq.getParticles()
+    hx[:] = x0
+    hv[:] = v0
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    stt = _lib.Stats()
+    for _ in range(2):
+        L.swc_set_particles(liq.h, dp(hx), dp(hv), n)
+        L.swc_advance(liq.h, scene.dt, C.byref(stt))
+        L.swc_get_particles(liq.h, dp(hx), dp(hv), n)
+    torch.cuda.synchronize()
+    barrier(dist)
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        rc = L.swc_set_particles(liq.h, dp(hx), dp(hv), n)
+        rc |= L.swc_advance(liq.h, scene.dt, C.byref(stt))
+        rc |= L.swc_get_particles(liq.h, dp(hx), dp(hv), n)
+        if rc:
+            raise RuntimeError("e2e step failed")
+    f1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = reduce_max(dist, f0.elapsed_time(f1))
+    e2e = {"value": ws * args.steps / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
+           "d2h_bytes_per_step": 2 * nbytes}
+    L.swc_host_free(hx_p)
+    L.swc_host_free(hv_p)
+
+    # plain-CG comparison forms (same scene, same steps)
+    forms = {}
+    if args.compare_forms:
+        for warm in ("prefix", "node", "zero"):
+            if warm == args.warm_start:
+                continue
+            l2 = make(warm)
+            for _ in range(args.warmup):
+                l2.advance(scene.dt)
+            torch.cuda.synchronize()
+            g0 = torch.cuda.Event(enable_timing=True)
+            g1 = torch.cuda.Event(enable_timing=True)
+            its = []
+            g0.record(stream)
+            for _ in range(args.steps):
+                its.append(l2.advance(scene.dt)["cg_iterations"])
+            g1.record(stream)
+            torch.cuda.synchronize()
+            forms[warm] = {"steps_per_s": args.steps / (g0.elapsed_time(g1) / 1e3),
+                           "cg_iterations_mean": float(np.mean(its))}
+            l2.close()
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_reference(args, n, sample_n=args.cpu_sample, steps=args.cpu_steps, warmup=1)
+        cpu.pop("seconds", None)
+
+    # kernels launched per step: binning 8, density 1, forces 1, generation 6, warm start 1,
+    # CG init 1 + 2 per iteration, gradient 1, export 1
+    launches_per_step = 21 + 2 * float(np.mean(iters))
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 CG reductions)",
+                "data": "synthetic (seeded)", "config": workload_config(args),
+                "wall_s_timed": wall, "cg_iterations_mean": float(np.mean(iters)), "n_virtual": nv,
+                "phases_ms": phases, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clk.summary(), "gpu_launches": int(round(launches_per_step * args.steps)),
+                "forms": forms}
+        print(json.dumps(line), flush=True)
+    liq.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="swc", choices=["swc", "reference"])
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--warm-start", dest="warm_start", default="node", choices=["prefix", "node", "zero", "learned"])
+    ap.add_argument("--cpu-sample", dest="cpu_sample", type=int, default=48)
+    ap.add_argument("--cpu-steps", dest="cpu_steps", type=int, default=3)
+    ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
+    ap.add_argument("--compare-forms", dest="compare_forms", type=int, default=1)
+    ap.add_argument("--profile-run", dest="profile_run", action="store_true",
+                    help="only the timed steps (for profiler captures); prints a reduced line")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        if args.steps > 10:
+            args.steps = 10  # each reference step is seconds of CPU work
+        run_reference_arm(args)
+    else:
+        run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -147,6 +147,15 @@ int swc_set_pressure(swc_ctx * ctx, const double * p, int64_t n);
 /* y = A x with the operator of the last projection (reference order, length N_v). */
 int swc_apply_operator(swc_ctx * ctx, const double * x, double * y, int64_t n);
 
+/* Neighbour ids of query points (FP64, nq x dim) found by the product's cell
+ * search, for parity checks of the neighbour sets (ParticlesNearbySearcher.cpp:20-35
+ * semantics: strict |x_j - q|^2 < R^2).  which: 0 real particles within h
+ * (original ids), 1 boundary particles within h (original ids), 2 active virtual
+ * nodes within H (node ids).  Call with ids = NULL for the counts, then with
+ * CSR offsets (exclusive scan of counts) to receive the ids. */
+int swc_debug_neighbors(swc_ctx * ctx, int which, int64_t nq, const double * q, int64_t * counts,
+                        const int64_t * offsets, int64_t * ids);
+
 /* Device time of the kernels of the last advance/project by phase (ms):
  * [0] binning, [1] densities, [2] forces, [3] virtual generation (gather +
  * compaction + alpha_hat), [4] warm start, [5] CG, [6] pressure gradient,

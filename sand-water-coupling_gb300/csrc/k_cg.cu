@@ -1,0 +1,413 @@
+// k_cg.cu -- matrix-free virtual Laplacian and CG of the dual-particle SPH
+// projection (reference: VirtualParticle::calculateCoef / solveLinearSystem,
+// Cores/Structures/VirtualParticle.cpp:149-169,105-108, and the Eigen CG behind
+// Cores/Solvers/IterativeSolver.h:21-40).
+//
+// Because virtual particles sit on lattice nodes, alpha_IJ = c(|k|^2) V_J with a
+// radial coefficient table c, so
+//     (A v)_I = alpha_hat_I v_I + sum_{0 < |k|^2 < 16} c(|k|^2) (V v)_{I+k}
+// on active rows; inactive rows are identity rows with zero right-hand side and
+// zero start, so CG over whole bricks is CG over the active set.
+//
+// Kernels: one CTA per brick (row-stencil kernels: one thread per brick x-row,
+// 8 outputs along x in 3D), the V-weighted halo tile staged in shared memory
+// with 16-byte loads.  The search-direction update d_i = r_i + beta d_{i-1} is
+// fused into the SpMV (recomputed for the halo), and x/r are updated in one
+// streaming pass; dot products use exact FP32 products summed in float-float
+// below the warp and FP64 above, reduced deterministically.
+#include "swc_kernels.h"
+#include "swc_tiles.cuh"
+
+namespace swc {
+
+template<int DIM> struct KG {
+    static constexpr int NT = RowGeom<DIM>::NT;         // rows per brick
+    static constexpr int BT = NT < 32 ? 32 : NT;        // threads per block
+};
+constexpr int kUT = 256;  // threads per block of the streaming update
+
+__device__ __forceinline__ float4 ld4(const float * a, long long s) { return *reinterpret_cast<const float4 *>(a + s); }
+__device__ __forceinline__ void st4(float * a, long long s, float4 v) { *reinterpret_cast<float4 *>(a + s) = v; }
+__device__ __forceinline__ float4 mul4(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+__device__ __forceinline__ float4 fma4(float s, float4 a, float4 b) {
+    return make_float4(fmaf(s, a.x, b.x), fmaf(s, a.y, b.y), fmaf(s, a.z, b.z), fmaf(s, a.w, b.w));
+}
+__device__ __forceinline__ float comp(const float4 & v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
+__device__ __forceinline__ unsigned char compb(const uchar4 & v, int j) {
+    return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w;
+}
+
+// Slot of the first node of brick row (ly, lz).
+template<int DIM> __device__ __forceinline__ long long row_base(int b, int ly, int lz) {
+    using G = BrickGeom<DIM>;
+    return (long long) b * G::BN + G::BX * (ly + G::BY * lz);
+}
+
+// alpha_hat_I = max(-sum_J alpha_IJ, alpha0) (calculateCoef, VirtualParticle.cpp:149-169);
+// optionally the number of active virtual neighbours within H (self included).
+template<int DIM>
+__global__ void __launch_bounds__(KG<DIM>::BT) k_ahat(Lattice L, Phys P, const int * __restrict__ blist,
+                                                      const int * __restrict__ bcount,
+                                                      const unsigned char * __restrict__ bflag, NodeArrays N,
+                                                      Stencil S, unsigned short * __restrict__ nvirt) {
+    using G = BrickGeom<DIM>;
+    __shared__ __align__(16) float tile[G::TILE];
+    const int nb = *bcount;
+    const int t = threadIdx.x, ly = t % G::BY, lz = t / G::BY;
+    Stencil ones;
+#pragma unroll
+    for (int k = 0; k < 16; k++) ones.c[k] = 1.f;
+    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
+        const int b   = blist[bi];
+        const int3 bc = brick_coords(L, b);
+        __syncthreads();
+        load_tile4<DIM>(L, bflag, bc, tile, [&](long long s) { return ld4(N.V, s); });
+        __syncthreads();
+        if (t < KG<DIM>::NT) {
+            float acc[G::BX];
+            stencil_row<DIM>(tile, ly, lz, S, acc);
+            const long long base = row_base<DIM>(b, ly, lz);
+#pragma unroll
+            for (int k = 0; k < G::BX / 4; k++) {
+                const uchar4 f = *reinterpret_cast<const uchar4 *>(N.flag + base + 4 * k);
+                float4 a;
+                a.x = f.x ? fmaxf(-acc[4 * k], P.alpha0) : 1.f;
+                a.y = f.y ? fmaxf(-acc[4 * k + 1], P.alpha0) : 1.f;
+                a.z = f.z ? fmaxf(-acc[4 * k + 2], P.alpha0) : 1.f;
+                a.w = f.w ? fmaxf(-acc[4 * k + 3], P.alpha0) : 1.f;
+                st4(N.ahat, base + 4 * k, a);
+            }
+        }
+        if (nvirt) {
+            // V_J > 0 exactly on active nodes: count them with a unit stencil
+            __syncthreads();
+            load_tile4<DIM>(L, bflag, bc, tile, [&](long long s) {
+                const float4 v = ld4(N.V, s);
+                return make_float4(v.x > 0.f, v.y > 0.f, v.z > 0.f, v.w > 0.f);
+            });
+            __syncthreads();
+            if (t < KG<DIM>::NT) {
+                float acc[G::BX];
+                stencil_row<DIM>(tile, ly, lz, ones, acc);
+                const long long base = row_base<DIM>(b, ly, lz);
+#pragma unroll
+                for (int i = 0; i < G::BX; i++)
+                    nvirt[base + i] = N.flag[base + i] ? (unsigned short) (acc[i] + 1.5f) : 0;
+            }
+        }
+    }
+}
+
+// y = A v (test hook).
+template<int DIM>
+__global__ void __launch_bounds__(KG<DIM>::BT) k_apply_operator(Lattice L, const int * __restrict__ blist,
+                                                                const int * __restrict__ bcount,
+                                                                const unsigned char * __restrict__ bflag, NodeArrays N,
+                                                                Stencil S, const float * __restrict__ in,
+                                                                float * __restrict__ out) {
+    using G = BrickGeom<DIM>;
+    __shared__ __align__(16) float tile[G::TILE];
+    const int nb = *bcount;
+    const int t = threadIdx.x, ly = t % G::BY, lz = t / G::BY;
+    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
+        const int b   = blist[bi];
+        const int3 bc = brick_coords(L, b);
+        __syncthreads();
+        load_tile4<DIM>(L, bflag, bc, tile, [&](long long s) { return mul4(ld4(N.V, s), ld4(in, s)); });
+        __syncthreads();
+        if (t < KG<DIM>::NT) {
+            float acc[G::BX];
+            stencil_row<DIM>(tile, ly, lz, S, acc);
+            const long long base = row_base<DIM>(b, ly, lz);
+#pragma unroll
+            for (int k = 0; k < G::BX / 4; k++) {
+                const float4 v = ld4(in, base + 4 * k), a = ld4(N.ahat, base + 4 * k);
+                const uchar4 f = *reinterpret_cast<const uchar4 *>(N.flag + base + 4 * k);
+                float4 o;
+                o.x = f.x ? fmaf(a.x, v.x, acc[4 * k]) : v.x;
+                o.y = f.y ? fmaf(a.y, v.y, acc[4 * k + 1]) : v.y;
+                o.z = f.z ? fmaf(a.z, v.z, acc[4 * k + 2]) : v.z;
+                o.w = f.w ? fmaf(a.w, v.w, acc[4 * k + 3]) : v.w;
+                st4(out, base + 4 * k, o);
+            }
+        }
+    }
+}
+
+// CG start: r = b - A x0, d0 = r, |r|^2, |b|^2, threshold and iteration cap
+// (Eigen's stopping rule: |r|^2 < max(tol, eps/|b|)^2 |b|^2, cap 2 N_v).
+template<int DIM>
+__global__ void __launch_bounds__(KG<DIM>::BT) k_cg_init(Lattice L, const int * __restrict__ blist,
+                                                         const int * __restrict__ bcount,
+                                                         const unsigned char * __restrict__ bflag, NodeArrays N,
+                                                         Stencil S, CgState * cg, double * __restrict__ partials,
+                                                         double tol, int max_iterations, const int * __restrict__ nv) {
+    using G = BrickGeom<DIM>;
+    constexpr int BT = KG<DIM>::BT;
+    __shared__ __align__(16) float tile[G::TILE];
+    __shared__ double red[BT / 32 + 1];
+    __shared__ int last;
+    const int nb = *bcount;
+    const int t = threadIdx.x, ly = t % G::BY, lz = t / G::BY;
+    FF rr{0.f, 0.f}, bb{0.f, 0.f};
+    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
+        const int b   = blist[bi];
+        const int3 bc = brick_coords(L, b);
+        __syncthreads();
+        load_tile4<DIM>(L, bflag, bc, tile, [&](long long s) { return mul4(ld4(N.V, s), ld4(N.x, s)); });
+        __syncthreads();
+        if (t < KG<DIM>::NT) {
+            float acc[G::BX];
+            stencil_row<DIM>(tile, ly, lz, S, acc);
+            const long long base = row_base<DIM>(b, ly, lz);
+#pragma unroll
+            for (int k = 0; k < G::BX / 4; k++) {
+                const float4 xv = ld4(N.x, base + 4 * k), a = ld4(N.ahat, base + 4 * k), bv = ld4(N.D, base + 4 * k);
+                const uchar4 f = *reinterpret_cast<const uchar4 *>(N.flag + base + 4 * k);
+                float r[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const float q = compb(f, j) ? fmaf(comp(a, j), comp(xv, j), acc[4 * k + j]) : comp(xv, j);
+                    r[j]          = comp(bv, j) - q;
+                    ff_add_prod(rr, r[j], r[j]);
+                    ff_add_prod(bb, comp(bv, j), comp(bv, j));
+                }
+                const float4 r4 = make_float4(r[0], r[1], r[2], r[3]);
+                st4(N.r, base + 4 * k, r4);
+                st4(N.d0, base + 4 * k, r4);
+            }
+        }
+    }
+    double part[2] = {block_sum_ff<BT>(rr, red), 0.0};
+    part[1]        = block_sum_ff<BT>(bb, red);
+    double tot[2];
+    if (grid_reduce<BT, 2>(part, partials, &cg->ticket[0], tot, red, &last) && threadIdx.x == 0) {
+        const double srr = tot[0], sbb = tot[1];
+        cg->bb      = sbb;
+        cg->rr      = srr;
+        cg->rr0     = srr;
+        cg->rr_prev = 0;
+        cg->pq      = 0;
+        cg->iter    = 0;
+        const int n  = *nv;
+        cg->max_iter = max_iterations >= 0 ? max_iterations : 2 * n;
+        const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
+        if (n == 0 || sbb == 0.0) {
+            cg->threshold = 0;
+            cg->done      = sbb == 0.0 ? 4 : 1;  // 4: zero right-hand side -> x = 0
+        } else {
+            const double tt = fmax(tol, eps / sqrt(sbb));
+            cg->threshold   = fmax(tt * tt * sbb, dmin);
+            cg->done        = srr < cg->threshold ? 1 : (srr != srr ? 3 : 0);
+            if (cg->done == 0 && cg->max_iter <= 0) cg->done = 2;
+        }
+    }
+}
+
+// Iteration part 1: d_i = r_i + beta d_{i-1} (i > 0; recomputed for the halo),
+// q = A d_i, pq = d_i . q.
+template<int DIM>
+__global__ void __launch_bounds__(KG<DIM>::BT) k_cg_spmv(Lattice L, const int * __restrict__ blist,
+                                                         const int * __restrict__ bcount,
+                                                         const unsigned char * __restrict__ bflag, NodeArrays N,
+                                                         Stencil S, CgState * cg, double * __restrict__ partials) {
+    using G = BrickGeom<DIM>;
+    constexpr int BT = KG<DIM>::BT;
+    __shared__ __align__(16) float tile[G::TILE];
+    __shared__ double red[BT / 32 + 1];
+    __shared__ int last;
+    if (cg->done) return;
+    const int it      = cg->iter;
+    const float beta  = it == 0 ? 0.f : float(cg->rr / cg->rr_prev);
+    const float * dpv = (it & 1) ? N.d0 : N.d1;  // d_{i-1}
+    float * dcur      = (it & 1) ? N.d1 : N.d0;  // d_i
+    const int nb      = *bcount;
+    const int t = threadIdx.x, ly = t % G::BY, lz = t / G::BY;
+    FF pq{0.f, 0.f};
+    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
+        const int b   = blist[bi];
+        const int3 bc = brick_coords(L, b);
+        __syncthreads();
+        if (it == 0)
+            load_tile4<DIM>(L, bflag, bc, tile, [&](long long s) { return mul4(ld4(N.V, s), ld4(dcur, s)); });
+        else
+            load_tile4<DIM>(L, bflag, bc, tile,
+                            [&](long long s) { return mul4(ld4(N.V, s), fma4(beta, ld4(dpv, s), ld4(N.r, s))); });
+        __syncthreads();
+        if (t < KG<DIM>::NT) {
+            float acc[G::BX];
+            stencil_row<DIM>(tile, ly, lz, S, acc);
+            const long long base = row_base<DIM>(b, ly, lz);
+#pragma unroll
+            for (int k = 0; k < G::BX / 4; k++) {
+                float4 dv;
+                if (it == 0) dv = ld4(dcur, base + 4 * k);
+                else {
+                    dv = fma4(beta, ld4(dpv, base + 4 * k), ld4(N.r, base + 4 * k));
+                    st4(dcur, base + 4 * k, dv);
+                }
+                const float4 a = ld4(N.ahat, base + 4 * k);
+                const uchar4 f = *reinterpret_cast<const uchar4 *>(N.flag + base + 4 * k);
+                float q[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    q[j] = compb(f, j) ? fmaf(comp(a, j), comp(dv, j), acc[4 * k + j]) : comp(dv, j);
+                    ff_add_prod(pq, comp(dv, j), q[j]);
+                }
+                st4(N.q, base + 4 * k, make_float4(q[0], q[1], q[2], q[3]));
+            }
+        }
+    }
+    double part[1] = {block_sum_ff<BT>(pq, red)};
+    double tot[1];
+    if (grid_reduce<BT, 1>(part, partials, &cg->ticket[1], tot, red, &last) && threadIdx.x == 0) {
+        cg->pq = tot[0];
+        if (!(tot[0] != 0.0) || tot[0] != tot[0]) cg->done = 3;
+    }
+}
+
+// Iteration part 2: alpha = rr / pq; x += alpha d_i; r -= alpha q; rr = r.r;
+// convergence test |r|^2 < threshold (16-byte streaming).
+template<int DIM>
+__global__ void __launch_bounds__(kUT) k_cg_update(const int * __restrict__ blist, const int * __restrict__ bcount,
+                                                   NodeArrays N, CgState * cg, double * __restrict__ partials) {
+    using G = BrickGeom<DIM>;
+    constexpr int Q = G::BN / 4;
+    __shared__ double red[kUT / 32 + 1];
+    __shared__ int last;
+    if (cg->done) return;
+    const int it      = cg->iter;
+    const float alpha = float(cg->rr / cg->pq);
+    const float * dc  = (it & 1) ? N.d1 : N.d0;
+    const long long total = (long long) (*bcount) * Q;
+    FF rr{0.f, 0.f};
+    for (long long i = blockIdx.x * (long long) kUT + threadIdx.x; i < total; i += (long long) gridDim.x * kUT) {
+        const long long s = (long long) blist[i / Q] * G::BN + 4 * (i % Q);
+        const float4 d = ld4(dc, s), q = ld4(N.q, s);
+        float4 x = ld4(N.x, s), r = ld4(N.r, s);
+        x = fma4(alpha, d, x);
+        r = fma4(-alpha, q, r);
+        st4(N.x, s, x);
+        st4(N.r, s, r);
+        ff_add_prod(rr, r.x, r.x);
+        ff_add_prod(rr, r.y, r.y);
+        ff_add_prod(rr, r.z, r.z);
+        ff_add_prod(rr, r.w, r.w);
+    }
+    double part[1] = {block_sum_ff<kUT>(rr, red)};
+    double tot[1];
+    if (grid_reduce<kUT, 1>(part, partials, &cg->ticket[2], tot, red, &last) && threadIdx.x == 0) {
+        const double s = tot[0];
+        cg->rr_prev    = cg->rr;
+        cg->rr         = s;
+        cg->iter       = it + 1;
+        if (s != s) cg->done = 3;
+        else if (s < cg->threshold) cg->done = 1;
+        else if (it + 1 >= cg->max_iter) cg->done = 2;
+    }
+}
+
+// True residual |b - A x|^2 and |b|^2 (FP64, out2[0], out2[1]).
+template<int DIM>
+__global__ void __launch_bounds__(KG<DIM>::BT) k_true_residual(Lattice L, const int * __restrict__ blist,
+                                                               const int * __restrict__ bcount,
+                                                               const unsigned char * __restrict__ bflag, NodeArrays N,
+                                                               Stencil S, CgState * cg, double * __restrict__ partials,
+                                                               double * __restrict__ out2) {
+    using G = BrickGeom<DIM>;
+    constexpr int BT = KG<DIM>::BT;
+    __shared__ __align__(16) float tile[G::TILE];
+    __shared__ double red[BT / 32 + 1];
+    __shared__ int last;
+    const int nb = *bcount;
+    const int t = threadIdx.x, ly = t % G::BY, lz = t / G::BY;
+    double rr = 0, bb = 0;
+    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
+        const int b   = blist[bi];
+        const int3 bc = brick_coords(L, b);
+        __syncthreads();
+        load_tile4<DIM>(L, bflag, bc, tile, [&](long long s) { return mul4(ld4(N.V, s), ld4(N.x, s)); });
+        __syncthreads();
+        if (t < KG<DIM>::NT) {
+            float acc[G::BX];
+            stencil_row<DIM>(tile, ly, lz, S, acc);
+            const long long base = row_base<DIM>(b, ly, lz);
+#pragma unroll
+            for (int i = 0; i < G::BX; i++) {
+                if (!N.flag[base + i]) continue;
+                const double q = double(N.ahat[base + i]) * N.x[base + i] + double(acc[i]);
+                const double r = double(N.D[base + i]) - q;
+                rr += r * r;
+                bb += double(N.D[base + i]) * N.D[base + i];
+            }
+        }
+    }
+    double part[2] = {block_sum_double<BT>(rr, red), 0.0};
+    part[1]        = block_sum_double<BT>(bb, red);
+    double tot[2];
+    if (grid_reduce<BT, 2>(part, partials, &cg->ticket[3], tot, red, &last) && threadIdx.x == 0) {
+        out2[0] = tot[0];
+        out2[1] = tot[1];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers (sgrid: blocks of the row-stencil kernels; ugrid: of the update)
+// ---------------------------------------------------------------------------
+template<int DIM>
+void launch_ahat(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
+                 unsigned short * nvirt, int sgrid, cudaStream_t st) {
+    k_ahat<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, P, B.list, B.count, B.flag, N, S, nvirt);
+}
+template<int DIM>
+void launch_apply_operator(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
+                           const float * in, float * out, int sgrid, cudaStream_t st) {
+    k_apply_operator<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, B.list, B.count, B.flag, N, S, in, out);
+}
+template<int DIM>
+void launch_cg_init(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
+                    double * partials, double tol, int max_iterations, const int * nv, int sgrid, cudaStream_t st) {
+    k_cg_init<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, B.list, B.count, B.flag, N, S, cg, partials, tol, max_iterations,
+                                                  nv);
+}
+template<int DIM>
+void launch_cg_spmv(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
+                    double * partials, int sgrid, cudaStream_t st) {
+    k_cg_spmv<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, B.list, B.count, B.flag, N, S, cg, partials);
+}
+template<int DIM>
+void launch_cg_update(const BrickArrays & B, const NodeArrays & N, CgState * cg, double * partials, int ugrid,
+                      cudaStream_t st) {
+    k_cg_update<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N, cg, partials);
+}
+template<int DIM>
+void launch_cg_iteration(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
+                         CgState * cg, double * partials, int sgrid, int ugrid, cudaStream_t st) {
+    launch_cg_spmv<DIM>(L, B, N, S, cg, partials, sgrid, st);
+    launch_cg_update<DIM>(B, N, cg, partials, ugrid, st);
+}
+template<int DIM>
+void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
+                          CgState * cg, double * partials, double * out2, int sgrid, cudaStream_t st) {
+    k_true_residual<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, B.list, B.count, B.flag, N, S, cg, partials, out2);
+}
+
+#define SWC_INST(D)                                                                                                    \
+    template void launch_ahat<D>(const Lattice &, const Phys &, const BrickArrays &, const NodeArrays &,               \
+                                 const Stencil &, unsigned short *, int, cudaStream_t);                                \
+    template void launch_apply_operator<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,   \
+                                           const float *, float *, int, cudaStream_t);                                 \
+    template void launch_cg_init<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,         \
+                                    CgState *, double *, double, int, const int *, int, cudaStream_t);                 \
+    template void launch_cg_spmv<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,         \
+                                    CgState *, double *, int, cudaStream_t);                                           \
+    template void launch_cg_update<D>(const BrickArrays &, const NodeArrays &, CgState *, double *, int, cudaStream_t); \
+    template void launch_cg_iteration<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,    \
+                                         CgState *, double *, int, int, cudaStream_t);                                 \
+    template void launch_true_residual<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,   \
+                                          CgState *, double *, double *, int, cudaStream_t);
+SWC_INST(2)
+SWC_INST(3)
+#undef SWC_INST
+
+}  // namespace swc

@@ -5,10 +5,10 @@
 // search-direction update, and the x/r update), all with deterministic
 // FP64 reductions.
 #include "swc_kernels.h"
+#include "swc_tiles.cuh"
 
 namespace swc {
 
-constexpr int kNT = 256;  // threads per block of the brick kernels
 
 // ---------------------------------------------------------------------------
 // Active-brick list (single CTA, ascending brick id).
@@ -49,11 +49,6 @@ __global__ void __launch_bounds__(1024) k_brick_list(const unsigned char * __res
     if (threadIdx.x == 0) *count = carry;
 }
 
-// Brick coordinates of brick id b.
-__device__ __forceinline__ int3 brick_coords(const Lattice & L, int b) {
-    return make_int3(b % L.bnx, (b / L.bnx) % L.bny, b / (L.bnx * L.bny));
-}
-
 // ---------------------------------------------------------------------------
 // Fused virtual gather.  For every node of an active brick, one pass over the
 // real and boundary particles within h gives (reference VirtualParticle.cpp):
@@ -66,18 +61,20 @@ __device__ __forceinline__ int3 brick_coords(const Lattice & L, int b) {
 // (boundary: m_b, rho_b, V_b) except weight, rho_I and V_I (real only).
 // ---------------------------------------------------------------------------
 template<int DIM>
-__global__ void __launch_bounds__(kNT) k_node_gather(Lattice L, Phys P, const int * __restrict__ blist,
+__global__ void __launch_bounds__(kNT, 3) k_node_gather(Lattice L, Phys P, const int * __restrict__ blist,
                                                      const int * __restrict__ bcount, NodeArrays N,
                                                      const float4 * __restrict__ pos, const float4 * __restrict__ vel,
                                                      const int * __restrict__ cellStart,
                                                      const float4 * __restrict__ bpos,
                                                      const float4 * __restrict__ bvel,
-                                                     const int * __restrict__ bcellStart) {
+                                                     const int * __restrict__ bcellStart,
+                                                     const unsigned char * __restrict__ bnear) {
     using G      = BrickGeom<DIM>;
     const int nb = *bcount;
     for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
         const int b    = blist[bi];
         const int3 bc  = brick_coords(L, b);
+        const int npass = bnear[b] ? 2 : 1;  // boundary particles only near walls
         for (int l = threadIdx.x; l < G::BN; l += kNT) {
             const int lx = l % G::BX, ly = (l / G::BX) % G::BY, lz = l / (G::BX * G::BY);
             const int x = bc.x * G::BX + lx, y = bc.y * G::BY + ly, z = bc.z * G::BZ + lz;
@@ -99,7 +96,7 @@ __global__ void __launch_bounds__(kNT) k_node_gather(Lattice L, Phys P, const in
             const int cy0 = max(y + P.cell_lo, 0), cy1 = min(y + P.cell_hi, L.ny - 1);
             const int cz0 = DIM == 3 ? max(z + P.cell_lo, 0) : 0, cz1 = DIM == 3 ? min(z + P.cell_hi, L.nz - 1) : 0;
 #pragma unroll 1
-            for (int pass = 0; pass < 2; pass++) {
+            for (int pass = 0; pass < npass; pass++) {
                 const int * cs   = pass == 0 ? cellStart : bcellStart;
                 const float4 * X = pass == 0 ? pos : bpos;
                 const float4 * U = pass == 0 ? vel : bvel;
@@ -113,11 +110,11 @@ __global__ void __launch_bounds__(kNT) k_node_gather(Lattice L, Phys P, const in
                             const float r2 = dx * dx + dy * dy + dz * dz;
                             if (r2 >= P.h2) continue;
                             const float4 u = U[j];
-                            const float r  = sqrtf(r2);
-                            const float w  = kW(r, P.inv_h, P.c0h);
+                            float w, gsc;
+                            kernel_and_grad(r2, P.inv_h, P.c0h, P.c1h, w, gsc);
                             if (pass == 0) {
                                 wsum += w;
-                                rhoI += kW(r, P.inv_H, P.c0H);
+                                rhoI += kW(r2 * rsqrtf(fmaxf(r2, 1e-30f)), P.inv_H, P.c0H);
                                 VI += p.w * p.w * w;
                                 cnt++;
                             }
@@ -126,14 +123,13 @@ __global__ void __launch_bounds__(kNT) k_node_gather(Lattice L, Phys P, const in
                             uy += mw * u.y;
                             uz += mw * u.z;
                             bw += p.w * w;
-                            if (r > 0.f) {
-                                const float c  = -kdW(r, P.inv_h, P.c1h) / r * p.w;
-                                const float cx = c * dx, cy_ = c * dy, cz_ = c * dz;
-                                dvg += u.x * cx + u.y * cy_ + u.z * cz_;
-                                gx += cx;
-                                gy += cy_;
-                                gz += cz_;
-                            }
+                            // g_j = -W'_h(r) (x_I - x_j) / r, zero at r = 0 (W'(0) = 0)
+                            const float c  = gsc * p.w;
+                            const float cx = c * dx, cy_ = c * dy, cz_ = c * dz;
+                            dvg += u.x * cx + u.y * cy_ + u.z * cz_;
+                            gx += cx;
+                            gy += cy_;
+                            gz += cz_;
                         }
                     }
             }
@@ -191,104 +187,6 @@ __global__ void __launch_bounds__(kNT) k_segment_count(Lattice L, const int * __
 #pragma unroll
             for (int k = 0; k < G::BX; k++) c += f[k];
             seg[((long long) z * L.ny + y) * L.bnx + bc.x] = c;
-        }
-    }
-}
-
-template<int DIM>
-__device__ __forceinline__ long long compact_index(const Lattice & L, const int * __restrict__ seg_off,
-                                                   const unsigned char * __restrict__ flag, int b, int bx, int x,
-                                                   int y, int z, int l) {
-    using G       = BrickGeom<DIM>;
-    const int lx  = l % G::BX;
-    long long I   = seg_off[((long long) z * L.ny + y) * L.bnx + bx];
-    const unsigned char * f = flag + (long long) b * G::BN + (l - lx);
-    for (int k = 0; k < lx; k++) I += f[k];
-    return I;
-}
-
-// ---------------------------------------------------------------------------
-// Halo tile loading and the radial stencil.
-// ---------------------------------------------------------------------------
-template<int DIM, class Get>
-__device__ __forceinline__ void load_tile(const Lattice & L, const unsigned char * __restrict__ bflag, int3 bc,
-                                          float * tile, Get get) {
-    using G       = BrickGeom<DIM>;
-    constexpr int NT = G::TX * G::TY * G::TZ;
-    for (int t = threadIdx.x; t < NT; t += kNT) {
-        const int tx = t % G::TX, ty = (t / G::TX) % G::TY, tz = t / (G::TX * G::TY);
-        const int x = bc.x * G::BX + tx - G::HALO, y = bc.y * G::BY + ty - G::HALO;
-        const int z = DIM == 3 ? bc.z * G::BZ + tz - G::HALO : 0;
-        float v = 0.f;
-        if (x >= 0 && x < L.nx && y >= 0 && y < L.ny && (DIM == 2 || (z >= 0 && z < L.nz))) {
-            const int nbx = x / G::BX, nby = y / G::BY, nbz = DIM == 3 ? z / G::BZ : 0;
-            const int nbk = nbx + L.bnx * (nby + L.bny * nbz);
-            if (bflag[nbk])
-                v = get((long long) nbk * G::BN + (x - nbx * G::BX) + G::BX * ((y - nby * G::BY) + G::BY * (z - nbz * G::BZ)));
-        }
-        tile[tx + G::PX * (ty + G::TY * tz)] = v;
-    }
-}
-
-template<int DIM> __device__ __forceinline__ int tile_center(int l) {
-    using G      = BrickGeom<DIM>;
-    const int lx = l % G::BX, ly = (l / G::BX) % G::BY, lz = l / (G::BX * G::BY);
-    return (lx + G::HALO) + G::PX * ((ly + G::HALO) + G::TY * (DIM == 3 ? lz + G::HALO : 0));
-}
-
-// sum over offsets 0 < |k|^2 < 16 of c(|k|^2) * tile[center + k]
-template<int DIM> __device__ __forceinline__ float stencil_apply(const float * tile, int c, const Stencil & S) {
-    using G   = BrickGeom<DIM>;
-    float acc = 0.f;
-    constexpr int ZR = DIM == 3 ? 3 : 0;
-#pragma unroll
-    for (int dz = -ZR; dz <= ZR; dz++)
-#pragma unroll
-        for (int dy = -3; dy <= 3; dy++)
-#pragma unroll
-            for (int dx = -3; dx <= 3; dx++) {
-                const int r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 > 0 && r2 < 16) acc = fmaf(S.c[r2], tile[c + dx + G::PX * (dy + G::TY * dz)], acc);
-            }
-    return acc;
-}
-template<int DIM> __device__ __forceinline__ double stencil_apply_d(const float * tile, int c, const StencilD & S) {
-    using G    = BrickGeom<DIM>;
-    double acc = 0.0;
-    constexpr int ZR = DIM == 3 ? 3 : 0;
-#pragma unroll
-    for (int dz = -ZR; dz <= ZR; dz++)
-#pragma unroll
-        for (int dy = -3; dy <= 3; dy++)
-#pragma unroll
-            for (int dx = -3; dx <= 3; dx++) {
-                const int r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 > 0 && r2 < 16) acc += S.c[r2] * double(tile[c + dx + G::PX * (dy + G::TY * dz)]);
-            }
-    return acc;
-}
-
-// alpha_hat_I = max(-sum_J alpha_IJ, alpha0) with alpha_IJ = c(|k|^2) V_J
-// (VirtualParticle::calculateCoef, VirtualParticle.cpp:149-169); inactive rows
-// become identity rows (alpha_hat = 1, rhs 0, x 0) so the brick-dense CG equals
-// CG on the active set.
-template<int DIM>
-__global__ void __launch_bounds__(kNT) k_ahat(Lattice L, Phys P, const int * __restrict__ blist,
-                                              const int * __restrict__ bcount, const unsigned char * __restrict__ bflag,
-                                              NodeArrays N, Stencil S) {
-    using G = BrickGeom<DIM>;
-    __shared__ float tile[G::TILE];
-    const int nb = *bcount;
-    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
-        const int b   = blist[bi];
-        const int3 bc = brick_coords(L, b);
-        __syncthreads();
-        load_tile<DIM>(L, bflag, bc, tile, [&](long long s) { return N.V[s]; });
-        __syncthreads();
-        for (int l = threadIdx.x; l < G::BN; l += kNT) {
-            const long long s = (long long) b * G::BN + l;
-            const float sum   = -stencil_apply<DIM>(tile, tile_center<DIM>(l), S);
-            N.ahat[s]         = N.flag[s] ? fmaxf(sum, P.alpha0) : 1.f;
         }
     }
 }
@@ -438,262 +336,159 @@ __global__ void __launch_bounds__(kNT) k_zero_active(const int * __restrict__ bl
 }
 
 // ---------------------------------------------------------------------------
-// Matrix-free operator: (A v)_I = alpha_hat_I v_I + sum_{J != I} c(|k|^2) V_J v_J
-// on active rows, identity on inactive rows.
+// Pressure-gradient update (VirtualParticle::applyPressureGradient,
+// Cores/Structures/VirtualParticle.cpp:111-134):
+//   v_i += sum_{J in N_H(i)} V_J p_J gradW_H(x_i - x_J)
+//          - sum_{b in N_h(i)} V_b min(n_b.(v_i - v_b), 0) n_b W_h(x_i - x_b)
+// One CTA per brick holding particles: u = V p over the brick + 4-node halo is
+// staged in shared memory, distances are taken in lattice units (H = 4).
 // ---------------------------------------------------------------------------
-template<int DIM>
-__global__ void __launch_bounds__(kNT) k_apply_operator(Lattice L, const int * __restrict__ blist,
-                                                        const int * __restrict__ bcount,
-                                                        const unsigned char * __restrict__ bflag, NodeArrays N,
-                                                        Stencil S, const float * __restrict__ in,
-                                                        float * __restrict__ out) {
-    using G = BrickGeom<DIM>;
-    __shared__ float tile[G::TILE];
-    const int nb = *bcount;
-    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
-        const int b   = blist[bi];
-        const int3 bc = brick_coords(L, b);
-        __syncthreads();
-        load_tile<DIM>(L, bflag, bc, tile, [&](long long s) { return N.V[s] * in[s]; });
-        __syncthreads();
-        for (int l = threadIdx.x; l < G::BN; l += kNT) {
-            const long long s = (long long) b * G::BN + l;
-            const float v     = in[s];
-            out[s] = N.flag[s] ? fmaf(N.ahat[s], v, stencil_apply<DIM>(tile, tile_center<DIM>(l), S)) : v;
-        }
-    }
+
+// sum_J u_J gradW_H(d) for lattice offsets d (in node units) with |d| < 4:
+// gradientKernel = -W'_H(r) d / r (SmoothedParticles.h:96-98).
+// Zero for r2 >= 16 (outside the support); finite at r2 = 0 where it multiplies
+// a zero offset.
+__device__ __forceinline__ float grad_scale(float r2, float c1H) {
+    const float rinv = rsqrtf(fmaxf(r2, 1e-20f));
+    const float q    = 0.25f * r2 * rinv;
+    // -W'(r) / r_u with W' = c1 q (3q - 2) (q < 1/2) or -c1 (1 - q)^2 (q < 1), q = r_u / 4
+    const float t = 1.f - fminf(q, 1.f);
+    return q < 0.5f ? -0.25f * c1H * (3.f * q - 2.f) : c1H * t * t * rinv;
 }
 
-// ---------------------------------------------------------------------------
-// CG (textbook Hestenes-Stiefel, identity preconditioner; reference
-// Cores/Solvers/IterativeSolver.h:21-40 -> Eigen ConjugateGradient).
-// Scalars live in CgState on the device; every kernel returns immediately once
-// `done` is set, so a captured batch of iterations can overshoot harmlessly.
-// ---------------------------------------------------------------------------
+// Global-memory path for particles outside the staged tile (clamped in from
+// outside the node lattice).
 template<int DIM>
-__global__ void __launch_bounds__(kNT) k_cg_init(Lattice L, const int * __restrict__ blist,
-                                                 const int * __restrict__ bcount,
-                                                 const unsigned char * __restrict__ bflag, NodeArrays N, Stencil S,
-                                                 CgState * cg, double * __restrict__ partials, double tol,
-                                                 int max_iterations, const int * __restrict__ nv) {
-    using G = BrickGeom<DIM>;
-    __shared__ float tile[G::TILE];
-    __shared__ double red[kNT / 32];
-    __shared__ int last;
-    const int nb = *bcount;
-    FF rr{0.f, 0.f}, bb{0.f, 0.f};
-    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
-        const int b   = blist[bi];
-        const int3 bc = brick_coords(L, b);
-        __syncthreads();
-        load_tile<DIM>(L, bflag, bc, tile, [&](long long s) { return N.V[s] * N.x[s]; });
-        __syncthreads();
-        for (int l = threadIdx.x; l < G::BN; l += kNT) {
-            const long long s = (long long) b * G::BN + l;
-            const float xv    = N.x[s];
-            const float q = N.flag[s] ? fmaf(N.ahat[s], xv, stencil_apply<DIM>(tile, tile_center<DIM>(l), S)) : xv;
-            const float bv = N.D[s];
-            const float r  = bv - q;
-            N.r[s]  = r;
-            N.d0[s] = r;
-            ff_add_prod(rr, r, r);
-            ff_add_prod(bb, bv, bv);
-        }
-    }
-    // two reductions: reuse the machinery twice with separate partial slots
-    const double prr = block_sum_ff<kNT>(rr, red);
-    const double pbb = block_sum_ff<kNT>(bb, red);
-    if (threadIdx.x == 0) {
-        partials[blockIdx.x]             = prr;
-        partials[gridDim.x + blockIdx.x] = pbb;
-        __threadfence();
-        last = atomicAdd(&cg->ticket[0], 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        volatile double * vp = partials;
-        double srr = 0, sbb = 0;
-        for (unsigned int k = 0; k < gridDim.x; k++) srr += vp[k];
-        for (unsigned int k = 0; k < gridDim.x; k++) sbb += vp[gridDim.x + k];
-        cg->ticket[0] = 0u;
-        cg->bb        = sbb;
-        cg->rr        = srr;
-        cg->rr0       = srr;
-        cg->rr_prev   = 0;
-        cg->pq        = 0;
-        cg->iter      = 0;
-        const int n   = *nv;
-        cg->max_iter  = max_iterations >= 0 ? max_iterations : 2 * n;
-        const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
-        if (n == 0 || sbb == 0.0) {
-            cg->threshold = 0;
-            cg->done      = sbb == 0.0 ? 4 : 1;  // 4: zero right-hand side -> x = 0
-        } else {
-            const double t   = fmax(tol, eps / sqrt(sbb));
-            cg->threshold    = fmax(t * t * sbb, dmin);
-            cg->done         = srr < cg->threshold ? 1 : (srr != srr ? 3 : 0);
-            if (cg->done == 0 && cg->max_iter <= 0) cg->done = 2;
-        }
-    }
-}
-
-// Iteration part 1: d_i = r_i + beta d_{i-1} (i > 0; computed on the fly for the
-// halo), q = A d_i, pq = d_i . q.
-template<int DIM>
-__global__ void __launch_bounds__(kNT) k_cg_spmv(Lattice L, const int * __restrict__ blist,
-                                                 const int * __restrict__ bcount,
-                                                 const unsigned char * __restrict__ bflag, NodeArrays N, Stencil S,
-                                                 CgState * cg, double * __restrict__ partials) {
-    using G = BrickGeom<DIM>;
-    __shared__ float tile[G::TILE];
-    __shared__ double red[kNT / 32];
-    __shared__ int last;
-    if (cg->done) return;
-    const int it      = cg->iter;
-    const float beta  = it == 0 ? 0.f : float(cg->rr / cg->rr_prev);
-    const float * dpv = (it & 1) ? N.d0 : N.d1;  // d_{i-1}
-    float * dcur      = (it & 1) ? N.d1 : N.d0;  // d_i
-    const int nb      = *bcount;
-    FF pq{0.f, 0.f};
-    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
-        const int b   = blist[bi];
-        const int3 bc = brick_coords(L, b);
-        __syncthreads();
-        if (it == 0)
-            load_tile<DIM>(L, bflag, bc, tile, [&](long long s) { return N.V[s] * dcur[s]; });
-        else
-            load_tile<DIM>(L, bflag, bc, tile, [&](long long s) { return N.V[s] * fmaf(beta, dpv[s], N.r[s]); });
-        __syncthreads();
-        for (int l = threadIdx.x; l < G::BN; l += kNT) {
-            const long long s = (long long) b * G::BN + l;
-            float dv;
-            if (it == 0) dv = dcur[s];
-            else {
-                dv      = fmaf(beta, dpv[s], N.r[s]);
-                dcur[s] = dv;
+__device__ float3 gradient_virtual_global(const Lattice & L, const Phys & P, const unsigned char * __restrict__ bflag,
+                                          const NodeArrays & N, float4 q) {
+    using G  = BrickGeom<DIM>;
+    float3 f = make_float3(0.f, 0.f, 0.f);
+    const float ux = (q.x - L.ox) * L.inv_dx, uy = (q.y - L.oy) * L.inv_dx, uz = DIM == 3 ? (q.z - L.oz) * L.inv_dx : 0.f;
+    const int y0 = max(__float2int_ru(uy - 4.f), 0), y1 = min(__float2int_rd(uy + 4.f), L.ny - 1);
+    int z0 = 0, z1 = 0;
+    if (DIM == 3) z0 = max(__float2int_ru(uz - 4.f), 0), z1 = min(__float2int_rd(uz + 4.f), L.nz - 1);
+    for (int kz = z0; kz <= z1; kz++) {
+        const float dz = DIM == 3 ? uz - kz : 0.f;
+        for (int ky = y0; ky <= y1; ky++) {
+            const float dy  = uy - ky;
+            const float rem = 16.f - dy * dy - dz * dz;
+            if (rem <= 0.f) continue;
+            const float rn = sqrtf(rem);
+            const int x0 = max(__float2int_ru(ux - rn), 0), x1 = min(__float2int_rd(ux + rn), L.nx - 1);
+            for (int kx = x0; kx <= x1; kx++) {
+                const int brick = kx / G::BX + L.bnx * (ky / G::BY + L.bny * (DIM == 3 ? kz / G::BZ : 0));
+                if (!bflag[brick]) continue;
+                const long long s = node_slot<DIM>(L, kx, ky, kz);
+                const float u     = N.V[s] * N.x[s];
+                const float dx    = ux - kx;
+                const float r2    = dx * dx + dy * dy + dz * dz;
+                if (u == 0.f || r2 >= 16.f || r2 <= 0.f) continue;
+                const float g = grad_scale(r2, P.c1H) * u;
+                f.x += g * dx;
+                f.y += g * dy;
+                f.z += g * dz;
             }
-            const float q = N.flag[s] ? fmaf(N.ahat[s], dv, stencil_apply<DIM>(tile, tile_center<DIM>(l), S)) : dv;
-            N.q[s]        = q;
-            ff_add_prod(pq, dv, q);
         }
     }
-    const double part = block_sum_ff<kNT>(pq, red);
-    if (threadIdx.x == 0) {
-        partials[blockIdx.x] = part;
-        __threadfence();
-        last = atomicAdd(&cg->ticket[1], 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        volatile double * vp = partials;
-        double s = 0;
-        for (unsigned int k = 0; k < gridDim.x; k++) s += vp[k];
-        cg->ticket[1] = 0u;
-        cg->pq        = s;
-        if (!(s != 0.0) || s != s) cg->done = 3;
-    }
+    return f;
 }
 
-// Iteration part 2: alpha = rr / pq; x += alpha d_i; r -= alpha q; rr = r.r;
-// convergence test |r|^2 < threshold.
 template<int DIM>
-__global__ void __launch_bounds__(kNT) k_cg_update(const int * __restrict__ blist, const int * __restrict__ bcount,
-                                                   NodeArrays N, CgState * cg, double * __restrict__ partials) {
-    using G = BrickGeom<DIM>;
-    __shared__ double red[kNT / 32];
-    __shared__ int last;
-    if (cg->done) return;
-    const int it      = cg->iter;
-    const float alpha = float(cg->rr / cg->pq);
-    const float * dc  = (it & 1) ? N.d1 : N.d0;
-    const int nb      = *bcount;
-    FF rr{0.f, 0.f};
-    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
-        const long long base = (long long) blist[bi] * G::BN;
-        for (int l = threadIdx.x; l < G::BN; l += kNT) {
-            const long long s = base + l;
-            N.x[s]            = fmaf(alpha, dc[s], N.x[s]);
-            const float r     = fmaf(-alpha, N.q[s], N.r[s]);
-            N.r[s]            = r;
-            ff_add_prod(rr, r, r);
-        }
-    }
-    const double part = block_sum_ff<kNT>(rr, red);
-    if (threadIdx.x == 0) {
-        partials[blockIdx.x] = part;
-        __threadfence();
-        last = atomicAdd(&cg->ticket[2], 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        volatile double * vp = partials;
-        double s = 0;
-        for (unsigned int k = 0; k < gridDim.x; k++) s += vp[k];
-        cg->ticket[2] = 0u;
-        cg->rr_prev   = cg->rr;
-        cg->rr        = s;
-        cg->iter      = it + 1;
-        if (s != s) cg->done = 3;
-        else if (s < cg->threshold) cg->done = 1;
-        else if (it + 1 >= cg->max_iter) cg->done = 2;
-    }
-}
-
-// True residual |b - A x|^2 and |b|^2 (FP64 out2[0], out2[1]).
-template<int DIM>
-__global__ void __launch_bounds__(kNT) k_true_residual(Lattice L, const int * __restrict__ blist,
-                                                       const int * __restrict__ bcount,
-                                                       const unsigned char * __restrict__ bflag, NodeArrays N,
-                                                       Stencil S, double * __restrict__ partials,
-                                                       unsigned int * __restrict__ ticket, double * __restrict__ out2) {
+__global__ void __launch_bounds__(kNT) k_pressure_gradient(Lattice L, Phys P, const unsigned char * __restrict__ bflag,
+                                                           NodeArrays N, const int * __restrict__ plist,
+                                                           const int * __restrict__ pcount,
+                                                           const unsigned char * __restrict__ bnear,
+                                                           const float4 * __restrict__ pos, float4 * __restrict__ vel,
+                                                           const int * __restrict__ cellStart,
+                                                           const float4 * __restrict__ bpos,
+                                                           const float4 * __restrict__ bvel,
+                                                           const float4 * __restrict__ bnrm,
+                                                           const int * __restrict__ bcellStart) {
     using G = BrickGeom<DIM>;
     __shared__ float tile[G::TILE];
-    __shared__ double red[kNT / 32];
-    __shared__ int last;
-    const int nb = *bcount;
-    double rr = 0, bb = 0;
+    constexpr int ROWS = G::BY * G::BZ;        // cell rows of a brick
+    constexpr int PER_ROW = kNT / ROWS;       // threads per row
+    const int nb = *pcount;
     for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
-        const int b   = blist[bi];
+        const int b   = plist[bi];
         const int3 bc = brick_coords(L, b);
         __syncthreads();
         load_tile<DIM>(L, bflag, bc, tile, [&](long long s) { return N.V[s] * N.x[s]; });
         __syncthreads();
-        for (int l = threadIdx.x; l < G::BN; l += kNT) {
-            const long long s = (long long) b * G::BN + l;
-            if (!N.flag[s]) continue;
-            const double q = double(N.ahat[s]) * N.x[s] + double(stencil_apply<DIM>(tile, tile_center<DIM>(l), S));
-            const double r = double(N.D[s]) - q;
-            rr += r * r;
-            bb += double(N.D[s]) * N.D[s];
+        const bool walls = bnear[b] != 0;
+        const int row    = threadIdx.x % ROWS, sub = threadIdx.x / ROWS;
+        const int ly = row % G::BY, lz = row / G::BY;
+        const int y = bc.y * G::BY + ly, z = bc.z * G::BZ + lz;
+        if (y >= L.ny || (DIM == 3 && z >= L.nz)) continue;
+        const int x0 = bc.x * G::BX, x1 = min(x0 + G::BX, L.nx);
+        const long long rbase = (long long) L.nx * (y + (long long) L.ny * z);
+        const int jb = cellStart[rbase + x0], je = cellStart[rbase + x1];
+        // tile origin (node coordinates of tile index 0)
+        const float tox = float(x0 - G::HALO), toy = float(bc.y * G::BY - G::HALO);
+        const float toz = DIM == 3 ? float(bc.z * G::BZ - G::HALO) : 0.f;
+        for (int j = jb + sub; j < je; j += PER_ROW) {
+            const float4 q  = pos[j];
+            const float4 vi = vel[j];
+            const float ux = (q.x - L.ox) * L.inv_dx - tox, uy = (q.y - L.oy) * L.inv_dx - toy;
+            const float uz = DIM == 3 ? (q.z - L.oz) * L.inv_dx - toz : 0.f;
+            float3 f = make_float3(0.f, 0.f, 0.f);
+            const bool inside = ux > 3.f && ux < float(G::TX) - 4.f && uy > 3.f && uy < float(G::TY) - 4.f &&
+                                (DIM == 2 || (uz > 3.f && uz < float(G::TZ) - 4.f));
+            if (inside) {
+                // nodes within H lie in the 8-node x-window floor(ux) - 3 .. floor(ux) + 4 of each row
+                const int kz0 = DIM == 3 ? __float2int_ru(uz - 4.f) : 0, kz1 = DIM == 3 ? __float2int_rd(uz + 4.f) : 0;
+                const int ky0 = __float2int_ru(uy - 4.f), ky1 = __float2int_rd(uy + 4.f);
+                const int kxb  = __float2int_rd(ux) - 3;
+                const float dx0 = ux - float(kxb);
+                for (int kz = kz0; kz <= kz1; kz++) {
+                    const float dz = DIM == 3 ? uz - kz : 0.f;
+                    for (int ky = ky0; ky <= ky1; ky++) {
+                        const float dy   = uy - ky;
+                        const float dyz2 = fmaf(dy, dy, dz * dz);
+                        if (dyz2 >= 16.f) continue;
+                        const float * trow = tile + G::PX * (ky + G::TY * kz) + kxb;
+                        float sx = 0.f, sg = 0.f;  // sum g dx and sum g over the row
+#pragma unroll
+                        for (int i = 0; i < 8; i++) {
+                            const float dx = dx0 - float(i);
+                            const float g  = grad_scale(fmaf(dx, dx, dyz2), P.c1H) * trow[i];
+                            sx = fmaf(g, dx, sx);
+                            sg += g;
+                        }
+                        f.x += sx;
+                        f.y = fmaf(dy, sg, f.y);
+                        f.z = fmaf(dz, sg, f.z);
+                    }
+                }
+            } else {
+                f = gradient_virtual_global<DIM>(L, P, bflag, N, q);
+            }
+            if (walls) {
+                const float3 w = wall_term<DIM>(L, P, bcellStart, bpos, bvel, bnrm, q, vi);
+                f.x += w.x;
+                f.y += w.y;
+                f.z += w.z;
+            }
+            float4 o = vi;
+            o.x += f.x;
+            o.y += f.y;
+            if (DIM == 3) o.z += f.z;
+            vel[j] = o;
         }
-    }
-    const double prr = block_sum_double<kNT>(rr, red);
-    const double pbb = block_sum_double<kNT>(bb, red);
-    if (threadIdx.x == 0) {
-        partials[blockIdx.x]             = prr;
-        partials[gridDim.x + blockIdx.x] = pbb;
-        __threadfence();
-        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        volatile double * vp = partials;
-        double a = 0, c = 0;
-        for (unsigned int k = 0; k < gridDim.x; k++) a += vp[k];
-        for (unsigned int k = 0; k < gridDim.x; k++) c += vp[gridDim.x + k];
-        out2[0] = a;
-        out2[1] = c;
-        *ticket = 0u;
     }
 }
 
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
+template<int DIM>
+void launch_pressure_gradient(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
+                              const int * plist, const int * pcount, const unsigned char * bnear, const float4 * pos,
+                              float4 * vel, const int * cellStart, const float4 * bpos, const float4 * bvel,
+                              const float4 * bnrm, const int * bcellStart, int grid, cudaStream_t st) {
+    k_pressure_gradient<DIM><<<grid, kNT, 0, st>>>(L, P, B.flag, N, plist, pcount, bnear, pos, vel, cellStart, bpos,
+                                                   bvel, bnrm, bcellStart);
+}
 void launch_brick_list(const unsigned char * bflag, int nbricks, int * list, int * count, cudaStream_t st) {
     k_brick_list<<<1, 1024, 0, st>>>(bflag, nbricks, list, count);
 }
@@ -701,8 +496,10 @@ void launch_brick_list(const unsigned char * bflag, int nbricks, int * list, int
 template<int DIM>
 void launch_node_gather(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
                         const float4 * pos, const float4 * vel, const int * cellStart, const float4 * bpos,
-                        const float4 * bvel, const int * bcellStart, int grid, cudaStream_t st) {
-    k_node_gather<DIM><<<grid, kNT, 0, st>>>(L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel, bcellStart);
+                        const float4 * bvel, const int * bcellStart, const unsigned char * bnear, int grid,
+                        cudaStream_t st) {
+    k_node_gather<DIM><<<grid, kNT, 0, st>>>(L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel, bcellStart,
+                                             bnear);
 }
 
 template<int DIM>
@@ -713,11 +510,6 @@ void launch_segments(const Lattice & L, const BrickArrays & B, const NodeArrays 
     launch_scan(B.seg, B.nseg, B.seg_off, tiles, st);
 }
 
-template<int DIM>
-void launch_ahat(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
-                 int grid, cudaStream_t st) {
-    k_ahat<DIM><<<grid, kNT, 0, st>>>(L, P, B.list, B.count, B.flag, N, S);
-}
 
 template<int DIM>
 void launch_diag_max_f64(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const StencilD & S,
@@ -753,52 +545,21 @@ void launch_zero_active(const Lattice & L, const BrickArrays & B, float * a, int
     k_zero_active<DIM><<<grid, kNT, 0, st>>>(B.list, B.count, a);
 }
 
-template<int DIM>
-void launch_apply_operator(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
-                           const float * in, float * out, int grid, cudaStream_t st) {
-    k_apply_operator<DIM><<<grid, kNT, 0, st>>>(L, B.list, B.count, B.flag, N, S, in, out);
-}
 
-template<int DIM>
-void launch_cg_init(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
-                    double * partials, double tol, int max_iterations, const int * nv, int grid, cudaStream_t st) {
-    k_cg_init<DIM><<<grid, kNT, 0, st>>>(L, B.list, B.count, B.flag, N, S, cg, partials, tol, max_iterations, nv);
-}
 
-template<int DIM>
-void launch_cg_iteration(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
-                         CgState * cg, double * partials, int grid, cudaStream_t st) {
-    k_cg_spmv<DIM><<<grid, kNT, 0, st>>>(L, B.list, B.count, B.flag, N, S, cg, partials);
-    k_cg_update<DIM><<<grid, kNT, 0, st>>>(B.list, B.count, N, cg, partials);
-}
 
-template<int DIM>
-void launch_cg_spmv(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
-                    double * partials, int grid, cudaStream_t st) {
-    k_cg_spmv<DIM><<<grid, kNT, 0, st>>>(L, B.list, B.count, B.flag, N, S, cg, partials);
-}
-template<int DIM>
-void launch_cg_update(const BrickArrays & B, const NodeArrays & N, CgState * cg, double * partials, int grid,
-                      cudaStream_t st) {
-    k_cg_update<DIM><<<grid, kNT, 0, st>>>(B.list, B.count, N, cg, partials);
-}
 
-template<int DIM>
-void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
-                          double * partials, double * out2, int grid, cudaStream_t st) {
-    // ticket lives just past the two partial arrays
-    unsigned int * ticket = reinterpret_cast<unsigned int *>(partials + 2 * grid);
-    k_true_residual<DIM><<<grid, kNT, 0, st>>>(L, B.list, B.count, B.flag, N, S, partials, ticket, out2);
-}
 
 #define SWC_INST(D)                                                                                                    \
     template void launch_node_gather<D>(const Lattice &, const Phys &, const BrickArrays &, const NodeArrays &,        \
                                         const float4 *, const float4 *, const int *, const float4 *, const float4 *,   \
-                                        const int *, int, cudaStream_t);                                               \
+                                        const int *, const unsigned char *, int, cudaStream_t);                        \
+    template void launch_pressure_gradient<D>(const Lattice &, const Phys &, const BrickArrays &, const NodeArrays &,  \
+                                              const int *, const int *, const unsigned char *, const float4 *,         \
+                                              float4 *, const int *, const float4 *, const float4 *, const float4 *,   \
+                                              const int *, int, cudaStream_t);                                         \
     template void launch_segments<D>(const Lattice &, const BrickArrays &, const NodeArrays &, int *, int,             \
                                      cudaStream_t);                                                                    \
-    template void launch_ahat<D>(const Lattice &, const Phys &, const BrickArrays &, const NodeArrays &,               \
-                                 const Stencil &, int, cudaStream_t);                                                  \
     template void launch_diag_max_f64<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const StencilD &,   \
                                          unsigned long long *, int, cudaStream_t);                                     \
     template void launch_warm_start<D>(const Lattice &, const BrickArrays &, const NodeArrays &, int, const float *,   \
@@ -808,18 +569,7 @@ void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeAr
                                            unsigned short *, int, cudaStream_t);                                       \
     template void launch_compact_import<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const double *,   \
                                            float *, int, cudaStream_t);                                                \
-    template void launch_zero_active<D>(const Lattice &, const BrickArrays &, float *, int, cudaStream_t);             \
-    template void launch_apply_operator<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,   \
-                                           const float *, float *, int, cudaStream_t);                                 \
-    template void launch_cg_init<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,         \
-                                    CgState *, double *, double, int, const int *, int, cudaStream_t);                 \
-    template void launch_cg_iteration<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,    \
-                                         CgState *, double *, int, cudaStream_t);                                      \
-    template void launch_cg_spmv<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,         \
-                                    CgState *, double *, int, cudaStream_t);                                           \
-    template void launch_cg_update<D>(const BrickArrays &, const NodeArrays &, CgState *, double *, int, cudaStream_t); \
-    template void launch_true_residual<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,   \
-                                          double *, double *, int, cudaStream_t);
+    template void launch_zero_active<D>(const Lattice &, const BrickArrays &, float *, int, cudaStream_t);
 SWC_INST(2)
 SWC_INST(3)
 #undef SWC_INST

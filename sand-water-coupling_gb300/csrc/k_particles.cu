@@ -118,39 +118,6 @@ __global__ void k_permute(const int * __restrict__ perm, long long n, const floa
     }
 }
 
-// ---------------------------------------------------------------------------
-// Neighbour iteration over cells for a query point and radius R (particle
-// queries): rows pruned by their slab distance, x-range per row from the
-// remaining radius.
-// ---------------------------------------------------------------------------
-template<int DIM, class F>
-__device__ __forceinline__ void for_each_in_radius(const Lattice & L, const int * __restrict__ cellStart,
-                                                   float qx, float qy, float qz, float R, float R2, F && f) {
-    const int cy0 = clampi(__float2int_rd((qy - R - L.oy) * L.inv_dx), 0, L.ny - 1);
-    const int cy1 = clampi(__float2int_rd((qy + R - L.oy) * L.inv_dx), 0, L.ny - 1);
-    int cz0 = 0, cz1 = 0;
-    if (DIM == 3) {
-        cz0 = clampi(__float2int_rd((qz - R - L.oz) * L.inv_dx), 0, L.nz - 1);
-        cz1 = clampi(__float2int_rd((qz + R - L.oz) * L.inv_dx), 0, L.nz - 1);
-    }
-    for (int cz = cz0; cz <= cz1; cz++) {
-        const float dz  = DIM == 3 ? slab_dist(qz, cz, L.nz, L.oz, L.dx) : 0.f;
-        const float rz2 = R2 - dz * dz;
-        if (rz2 <= 0.f) continue;
-        for (int cy = cy0; cy <= cy1; cy++) {
-            const float dy  = slab_dist(qy, cy, L.ny, L.oy, L.dx);
-            const float rem = rz2 - dy * dy;
-            if (rem <= 0.f) continue;
-            const float rx = sqrtf(rem) * 1.000001f + 1e-7f * L.dx;
-            const int cx0  = clampi(__float2int_rd((qx - rx - L.ox) * L.inv_dx), 0, L.nx - 1);
-            const int cx1  = clampi(__float2int_rd((qx + rx - L.ox) * L.inv_dx), 0, L.nx - 1);
-            const long long row = (long long) L.nx * (cy + (long long) L.ny * cz);
-            const int b = cellStart[row + cx0], e = cellStart[row + cx1 + 1];
-            for (int j = b; j < e; j++) f(j);
-        }
-    }
-}
-
 // rho_i = m sum_j W_h(x_i - x_j)  (SmoothedParticles::computeDensities,
 // Cores/Structures/SmoothedParticles.cpp:25-31).  Writes vel.w = m / rho_i and rho_i.
 template<int DIM>
@@ -164,7 +131,7 @@ __global__ void __launch_bounds__(256) k_density(const float4 * __restrict__ pos
             const float4 p = pos[j];
             const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < P.h2) s += kW(sqrtf(r2), P.inv_h, P.c0h);
+            if (r2 < P.h2) s += kW(r2 * rsqrtf(fmaxf(r2, 1e-30f)), P.inv_h, P.c0h);
         });
         const float rho = mass * s;
         if (rho_out) rho_out[i] = rho;
@@ -199,10 +166,12 @@ __global__ void __launch_bounds__(256) k_forces(const float4 * __restrict__ pos,
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 < P.h2 && r2 > 0.f) {
                     const float4 vj = vel[j];
-                    const float r   = sqrtf(r2);
-                    const float s   = ((vj.x - vi.x) * dx + (vj.y - vi.y) * dy + (vj.z - vi.z) * dz) / r2;
+                    float w, gsc;
+                    kernel_and_grad(r2, P.inv_h, P.c0h, P.c1h, w, gsc);
+                    const float rinv = rsqrtf(r2);
+                    const float s = ((vj.x - vi.x) * dx + (vj.y - vi.y) * dy + (vj.z - vi.z) * dz) * (rinv * rinv);
                     // gradientKernel(x_j - x_i) = -W'(r) (x_j - x_i)/r, divided by rho_j = m / vel.w
-                    const float g = -kdW(r, P.inv_h, P.c1h) / r * s * (vj.w / P.mass);
+                    const float g = gsc * s * (vj.w * P.inv_mass);
                     lx += g * dx;
                     ly += g * dy;
                     lz += g * dz;
@@ -235,7 +204,7 @@ __global__ void __launch_bounds__(256) k_boundary_density(float4 * __restrict__ 
             const float4 p = bpos[j];
             const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < P.h2) s += kW(sqrtf(r2), P.inv_h, P.c0h);
+            if (r2 < P.h2) s += kW(r2 * rsqrtf(fmaxf(r2, 1e-30f)), P.inv_h, P.c0h);
         });
         const float rho = P.bmass * s;
         if (rho_out) rho_out[i] = rho;
@@ -246,12 +215,18 @@ __global__ void __launch_bounds__(256) k_boundary_density(float4 * __restrict__ 
 
 // Mark every brick that holds a node within h of a real particle (only those
 // nodes can have a positive weight, VirtualParticle.cpp:50-56).
+// `pflag` (optional) marks the brick of the particle's own cell: the bricks the
+// brick-tiled particle kernels visit.
 template<int DIM>
 __global__ void k_mark_bricks(const float4 * __restrict__ pos, long long n, Lattice L, Phys P,
-                              unsigned char * __restrict__ bflag) {
+                              unsigned char * __restrict__ bflag, unsigned char * __restrict__ pflag) {
     using G = BrickGeom<DIM>;
     for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
         const float4 p = pos[i];
+        if (pflag) {
+            const int3 c = cell_of<DIM>(L, p.x, p.y, p.z);
+            pflag[c.x / G::BX + L.bnx * (c.y / G::BY + L.bny * (c.z / G::BZ))] = 1;
+        }
         const int x0 = clampi(__float2int_ru((p.x - P.h - L.ox) * L.inv_dx), 0, L.nx - 1);
         const int x1 = clampi(__float2int_rd((p.x + P.h - L.ox) * L.inv_dx), 0, L.nx - 1);
         const int y0 = clampi(__float2int_ru((p.y - P.h - L.oy) * L.inv_dx), 0, L.ny - 1);
@@ -268,78 +243,6 @@ __global__ void k_mark_bricks(const float4 * __restrict__ pos, long long n, Latt
         for (int bz = bz0; bz <= bz1; bz++)
             for (int by = by0; by <= by1; by++)
                 for (int bx = bx0; bx <= bx1; bx++) bflag[bx + L.bnx * (by + L.bny * bz)] = 1;
-    }
-}
-
-// Pressure-gradient update (VirtualParticle::applyPressureGradient,
-// Cores/Structures/VirtualParticle.cpp:111-134):
-//   v_i += sum_{J in N_H(i)} V_J p_J gradW_H(x_i - x_J)
-//          - sum_{b in N_h(i)} V_b min(n_b.(v_i - v_b), 0) n_b W_h(x_i - x_b)
-template<int DIM>
-__global__ void __launch_bounds__(256) k_pressure_gradient(
-    const float4 * __restrict__ pos, float4 * __restrict__ vel, long long n, Lattice L, Phys P,
-    const unsigned char * __restrict__ bflag, const float * __restrict__ nodeV, const float * __restrict__ nodeP,
-    const float4 * __restrict__ bpos, const float4 * __restrict__ bvel, const float4 * __restrict__ bnrm,
-    const int * __restrict__ bcellStart) {
-    using G = BrickGeom<DIM>;
-    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
-        const float4 q  = pos[i];
-        const float4 vi = vel[i];
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        // virtual nodes within H: node coordinates k with |x_i - x_k| < H
-        const float ux = (q.x - L.ox) * L.inv_dx, uy = (q.y - L.oy) * L.inv_dx, uz = (q.z - L.oz) * L.inv_dx;
-        const float Hn = P.H * L.inv_dx;  // support in node units
-        const int y0 = max(__float2int_ru(uy - Hn), 0), y1 = min(__float2int_rd(uy + Hn), L.ny - 1);
-        int z0 = 0, z1 = 0;
-        if (DIM == 3) z0 = max(__float2int_ru(uz - Hn), 0), z1 = min(__float2int_rd(uz + Hn), L.nz - 1);
-        for (int kz = z0; kz <= z1; kz++) {
-            const float zn = L.oz + kz * L.dx;
-            const float dz = DIM == 3 ? q.z - zn : 0.f;
-            for (int ky = y0; ky <= y1; ky++) {
-                const float yn  = L.oy + ky * L.dx;
-                const float dy  = q.y - yn;
-                const float rem = P.H2 - dy * dy - dz * dz;
-                if (rem <= 0.f) continue;
-                const float rn = sqrtf(rem) * L.inv_dx;
-                const int x0 = max(__float2int_ru(ux - rn), 0), x1 = min(__float2int_rd(ux + rn), L.nx - 1);
-                for (int kx = x0; kx <= x1; kx++) {
-                    const int brick = kx / G::BX + L.bnx * (ky / G::BY + L.bny * (DIM == 3 ? kz / G::BZ : 0));
-                    if (!bflag[brick]) continue;
-                    const long long s = node_slot<DIM>(L, kx, ky, kz);
-                    const float u     = nodeV[s] * nodeP[s];
-                    if (u == 0.f) continue;
-                    const float dx = q.x - (L.ox + kx * L.dx);
-                    const float r2 = dx * dx + dy * dy + dz * dz;
-                    if (r2 >= P.H2 || r2 <= 0.f) continue;
-                    const float r = sqrtf(r2);
-                    const float g = -kdW(r, P.inv_H, P.c1H) / r * u;
-                    fx += g * dx;
-                    fy += g * dy;
-                    fz += g * dz;
-                }
-            }
-        }
-        // boundary friction-free wall term
-        for_each_in_radius<DIM>(L, bcellStart, q.x, q.y, q.z, P.h, P.h2, [&](int j) {
-            const float4 p = bpos[j];
-            const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < P.h2) {
-                const float4 nb = bnrm[j];
-                const float4 vb = bvel[j];
-                const float vn  = fminf(nb.x * (vi.x - vb.x) + nb.y * (vi.y - vb.y) + nb.z * (vi.z - vb.z), 0.f);
-                const float w   = kW(sqrtf(r2), P.inv_h, P.c0h);
-                const float c   = p.w * vn * w;
-                fx -= c * nb.x;
-                fy -= c * nb.y;
-                fz -= c * nb.z;
-            }
-        });
-        float4 o = vi;
-        o.x += fx;
-        o.y += fy;
-        if (DIM == 3) o.z += fz;
-        vel[i] = o;
     }
 }
 
@@ -396,6 +299,67 @@ __global__ void k_set_moving(float4 * __restrict__ bnrm, const unsigned char * _
                              const int * __restrict__ bid, long long nb) {
     for (long long s = blockIdx.x * (long long) blockDim.x + threadIdx.x; s < nb; s += (long long) gridDim.x * blockDim.x)
         bnrm[s].w = moving[bid[s]] ? 1.f : 0.f;
+}
+
+
+// Neighbour ids of arbitrary query points with the product's cell search
+// (parity checks): FP32 distances, FP64 re-test within 1e-5 h^2 of the support
+// edge so the strict |d|^2 < R^2 test matches an FP64 evaluation.
+// which: 0 real (original ids), 1 boundary (original ids), 2 active virtual
+// nodes within H (node ids).  ids == nullptr: counts only.
+template<int DIM>
+__global__ void k_debug_neighbors(int which, long long nq, const double * __restrict__ q, Lattice L, Phys P,
+                                  const float4 * __restrict__ pos, const int * __restrict__ id,
+                                  const int * __restrict__ cellStart, const unsigned char * __restrict__ bflag,
+                                  const unsigned char * __restrict__ nflag, long long * __restrict__ counts,
+                                  const long long * __restrict__ offsets, long long * __restrict__ ids) {
+    using G = BrickGeom<DIM>;
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < nq; t += (long long) gridDim.x * blockDim.x) {
+        const double qx = q[t * DIM], qy = q[t * DIM + 1], qz = DIM == 3 ? q[t * DIM + 2] : 0.0;
+        const float fx = float(qx), fy = float(qy), fz = float(qz);
+        long long c = 0;
+        const long long o = offsets ? offsets[t] : 0;
+        auto accept = [&](float px, float py, float pz, double R2d, float R2f) {
+            const float dx = fx - px, dy = fy - py, dz = fz - pz;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (fabsf(r2 - R2f) > 1e-5f * R2f) return r2 < R2f;
+            const double ex = qx - double(px), ey = qy - double(py), ez = DIM == 3 ? qz - double(pz) : 0.0;
+            return ex * ex + ey * ey + ez * ez < R2d;
+        };
+        if (which < 2) {
+            const double R2d = P.h_d * P.h_d;
+            for_each_in_radius<DIM>(L, cellStart, fx, fy, fz, P.h * 1.0001f, P.h2 * 1.0002f, [&](int j) {
+                const float4 p = pos[j];
+                if (accept(p.x, p.y, p.z, R2d, P.h2)) {
+                    if (ids) ids[o + c] = id[j];
+                    c++;
+                }
+            });
+        } else {
+            const double Hd = 4.0 * L.dx_d, R2d = Hd * Hd;
+            const float Hn = P.H * L.inv_dx * 1.0001f;
+            const float ux = (fx - L.ox) * L.inv_dx, uy = (fy - L.oy) * L.inv_dx, uz = (fz - L.oz) * L.inv_dx;
+            const int x0 = max(__float2int_rd(ux - Hn), 0), x1 = min(__float2int_ru(ux + Hn), L.nx - 1);
+            const int y0 = max(__float2int_rd(uy - Hn), 0), y1 = min(__float2int_ru(uy + Hn), L.ny - 1);
+            int z0 = 0, z1 = 0;
+            if (DIM == 3) z0 = max(__float2int_rd(uz - Hn), 0), z1 = min(__float2int_ru(uz + Hn), L.nz - 1);
+            for (int kz = z0; kz <= z1; kz++)
+                for (int ky = y0; ky <= y1; ky++)
+                    for (int kx = x0; kx <= x1; kx++) {
+                        const int brick = kx / G::BX + L.bnx * (ky / G::BY + L.bny * (DIM == 3 ? kz / G::BZ : 0));
+                        if (!bflag[brick] || !nflag[node_slot<DIM>(L, kx, ky, kz)]) continue;
+                        // FP64 node position, as the reference computes it
+                        const double nx = L.ox_d + kx * L.dx_d, ny = L.oy_d + ky * L.dx_d,
+                                     nz = DIM == 3 ? L.oz_d + kz * L.dx_d : 0.0;
+                        const double ex = qx - nx, ey = qy - ny, ez = qz - nz;
+                        if (ex * ex + ey * ey + ez * ez < R2d) {
+                            if (ids) ids[o + c] = (long long) kx + (long long) L.nx * (ky + (long long) L.ny * kz);
+                            c++;
+                        }
+                    }
+        }
+        counts[t] = c;
+    }
 }
 
 // Max over a positive float array (ordered as int bits).
@@ -586,18 +550,10 @@ void launch_boundary_density(float4 * bpos, float4 * bvel, float * rho, long lon
 }
 template<int DIM>
 void launch_mark_bricks(const float4 * pos, long long n, const Lattice & L, const Phys & P, unsigned char * bflag,
-                        cudaStream_t st) {
+                        unsigned char * pflag, cudaStream_t st) {
     cudaMemsetAsync(bflag, 0, L.nbricks, st);
-    if (n > 0) k_mark_bricks<DIM><<<grid_for(n, 256), 256, 0, st>>>(pos, n, L, P, bflag);
-}
-template<int DIM>
-void launch_pressure_gradient(const float4 * pos, float4 * vel, long long n, const Lattice & L, const Phys & P,
-                              const unsigned char * bflag, const float * nodeV, const float * nodeP,
-                              const float4 * bpos, const float4 * bvel, const float4 * bnrm, const int * bcellStart,
-                              cudaStream_t st) {
-    if (n > 0)
-        k_pressure_gradient<DIM><<<grid_for(n, 256, 1 << 20), 256, 0, st>>>(pos, vel, n, L, P, bflag, nodeV, nodeP,
-                                                                              bpos, bvel, bnrm, bcellStart);
+    if (pflag) cudaMemsetAsync(pflag, 0, L.nbricks, st);
+    if (n > 0) k_mark_bricks<DIM><<<grid_for(n, 256), 256, 0, st>>>(pos, n, L, P, bflag, pflag);
 }
 void launch_rotate_boundary(float4 * bpos, float4 * bvel, float4 * bnrm, long long nb, float cx, float cz,
                             float omega, float dt, cudaStream_t st) {
@@ -621,6 +577,17 @@ void launch_max_positive(const float * a, long long n, int * out_bits, cudaStrea
     if (n > 0) k_max_positive<<<grid_for(n, 256), 256, 0, st>>>(a, n, out_bits);
 }
 
+
+template<int DIM>
+void launch_debug_neighbors(int which, long long nq, const double * q, const Lattice & L, const Phys & P,
+                            const float4 * pos, const int * id, const int * cellStart, const unsigned char * bflag,
+                            const unsigned char * nflag, long long * counts, const long long * offsets, long long * ids,
+                            cudaStream_t st) {
+    if (nq > 0)
+        k_debug_neighbors<DIM><<<grid_for(nq, 128), 128, 0, st>>>(which, nq, q, L, P, pos, id, cellStart, bflag, nflag,
+                                                                   counts, offsets, ids);
+}
+
 #define SWC_INST(D)                                                                                                    \
     template void launch_bin<D>(const Lattice &, long long, float4 *, float4 *, float4 *, int *, SortScratch &, int *, \
                                 cudaStream_t);                                                                         \
@@ -631,10 +598,12 @@ void launch_max_positive(const float * a, long long n, int * out_bits, cudaStrea
     template void launch_boundary_density<D>(float4 *, float4 *, float *, long long, const Lattice &, const Phys &,    \
                                              const int *, cudaStream_t);                                               \
     template void launch_mark_bricks<D>(const float4 *, long long, const Lattice &, const Phys &, unsigned char *,     \
+                                        unsigned char *,                                                               \
                                         cudaStream_t);                                                                 \
-    template void launch_pressure_gradient<D>(const float4 *, float4 *, long long, const Lattice &, const Phys &,      \
-                                              const unsigned char *, const float *, const float *, const float4 *,     \
-                                              const float4 *, const float4 *, const int *, cudaStream_t);
+    template void launch_debug_neighbors<D>(int, long long, const double *, const Lattice &, const Phys &,            \
+                                            const float4 *, const int *, const int *, const unsigned char *,           \
+                                            const unsigned char *, long long *, const long long *, long long *,        \
+                                            cudaStream_t);
 SWC_INST(2)
 SWC_INST(3)
 #undef SWC_INST

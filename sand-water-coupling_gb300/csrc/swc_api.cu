@@ -38,7 +38,8 @@ struct swc_ctx {
     Phys            P{};
     Stencil         S{};
     StencilD        SD{};
-    int             grid = 1;  // persistent grid of the brick kernels
+    int             grid  = 1;  // persistent grid of the 256-thread brick kernels
+    int             sgrid = 1;  // persistent grid of the row-stencil kernels (one brick per block)
     std::string     err;
 
     // real particles (sorted by cell)
@@ -66,6 +67,10 @@ struct swc_ctx {
     // lattice
     NodeArrays  N{};
     BrickArrays B{};
+    unsigned char * pflag = nullptr;  // bricks holding real particles (own cell)
+    int *           plist = nullptr;
+    int *           pcount = nullptr;
+    unsigned char * bnear = nullptr;  // bricks within reach of boundary particles
     float *     pcomp = nullptr;
     int *       nv_prev = nullptr;
     int *       scan_tiles = nullptr;
@@ -174,6 +179,7 @@ void setup_phys(swc_ctx * c) {
     P.inv_h_d = 1 / h;
     P.c0h_d   = std::numbers::inv_pi * (1 / (h * h)) * (dim == 2 ? 40.0 / 7 : 8 * (1 / h));
     P.mass    = float(s.mass);
+    P.inv_mass = float(1.0 / s.mass);
     P.bmass   = float(s.boundary_mass);
     P.rho0    = float(c->rho0 > 0 ? c->rho0 : 1.0);
     P.kappa   = float(c->kappa);
@@ -203,6 +209,7 @@ template<int DIM> int run_bin_real(swc_ctx * c) {
 }
 template<int DIM> int run_bin_boundary(swc_ctx * c) {
     launch_bin<DIM>(c->L, c->nb, c->bpos, c->bvel, c->bnrm, c->bid, c->sortB, c->bcellStart, c->stream);
+    launch_mark_bricks<DIM>(c->bpos, c->nb, c->L, c->P, c->bnear, nullptr, c->stream);
     return SWC_OK;
 }
 
@@ -213,12 +220,13 @@ inline void mark(swc_ctx * c, int k) {
 // Virtual generation: active bricks, fused gather, reference-order compaction,
 // alpha_hat (VirtualParticle::generateParticles + calculateCoef diagonal).
 template<int DIM> void run_generate(swc_ctx * c, bool with_ahat) {
-    launch_mark_bricks<DIM>(c->pos, c->n, c->L, c->P, c->B.flag, c->stream);
+    launch_mark_bricks<DIM>(c->pos, c->n, c->L, c->P, c->B.flag, c->pflag, c->stream);
     launch_brick_list(c->B.flag, c->L.nbricks, c->B.list, c->B.count, c->stream);
+    launch_brick_list(c->pflag, c->L.nbricks, c->plist, c->pcount, c->stream);
     launch_node_gather<DIM>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel, c->bcellStart,
-                            c->grid, c->stream);
+                            c->bnear, c->grid, c->stream);
     launch_segments<DIM>(c->L, c->B, c->N, c->scan_tiles, c->grid, c->stream);
-    if (with_ahat) launch_ahat<DIM>(c->L, c->P, c->B, c->N, c->S, c->grid, c->stream);
+    if (with_ahat) launch_ahat<DIM>(c->L, c->P, c->B, c->N, c->S, c->N.nvirt, c->sgrid, c->stream);
 }
 
 int capture_graphs(swc_ctx * c) {
@@ -227,8 +235,9 @@ int capture_graphs(swc_ctx * c) {
         cudaGraph_t g  = nullptr;
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         for (int i = 0; i < reps; i++) {
-            if (c->dim == 2) launch_cg_iteration<2>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->grid, c->stream);
-            else launch_cg_iteration<3>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->grid, c->stream);
+            if (c->dim == 2)
+                launch_cg_iteration<2>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->sgrid, c->grid, c->stream);
+            else launch_cg_iteration<3>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->sgrid, c->grid, c->stream);
         }
         CK(cudaStreamEndCapture(c->stream, &g));
         cudaGraphExec_t ge = nullptr;
@@ -249,7 +258,7 @@ template<int DIM> int run_cg(swc_ctx * c, swc_stats * st) {
         if (rc) return rc;
     }
     launch_cg_init<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->opts.tolerance, c->opts.max_iterations, nv,
-                        c->grid, c->stream);
+                        c->sgrid, c->stream);
     CK(cudaMemcpyAsync(&c->hcg->st, c->cg, sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&c->hcg->nv, nv, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&c->hcg->nbricks, c->B.count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -282,7 +291,7 @@ template<int DIM> int run_cg(swc_ctx * c, swc_stats * st) {
         st->status               = status;
     }
     if (c->opts.compute_true_residual && st) {
-        launch_true_residual<DIM>(c->L, c->B, c->N, c->S, c->partials, c->res2, c->grid, c->stream);
+        launch_true_residual<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->res2, c->sgrid, c->stream);
         double r2[2];
         CK(cudaMemcpyAsync(r2, c->res2, sizeof(r2), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
@@ -302,9 +311,16 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     int rc = run_cg<DIM>(c, st);
     if (rc != SWC_OK && rc != SWC_CG_NOT_CONVERGED && rc != SWC_NAN_DETECTED) return rc;
     const int cg_status = rc;
+    if (cg_status == SWC_NAN_DETECTED) {
+        // report, leave the velocities unprojected and drop the poisoned warm start
+        launch_zero_active<DIM>(c->L, c->B, c->N.x, c->grid, c->stream);
+        CK(cudaMemsetAsync(c->nv_prev, 0, sizeof(int), c->stream));
+        for (int k = 6; k <= 8; k++) mark(c, k);
+        return cg_status;
+    }
     mark(c, 6);
-    launch_pressure_gradient<DIM>(c->pos, c->vel, c->n, c->L, c->P, c->B.flag, c->N.V, c->N.x, c->bpos, c->bvel,
-                                  c->bnrm, c->bcellStart, c->stream);
+    launch_pressure_gradient<DIM>(c->L, c->P, c->B, c->N, c->plist, c->pcount, c->bnear, c->pos, c->vel,
+                                  c->cellStart, c->bpos, c->bvel, c->bnrm, c->bcellStart, c->grid, c->stream);
     mark(c, 7);
     // p in reference order (next step's prefix warm start) and N_v for it
     launch_compact_export<DIM>(c->L, c->B, c->N, c->pcomp, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
@@ -497,7 +513,9 @@ int swc_create(const swc_scene * s, const swc_solver_opts * o, swc_ctx ** out) {
         delete c;
         return SWC_BAD_ARG;
     }
-    c->grid = std::max(1, std::min(L.nbricks, c->num_sms * 8));
+    c->grid  = std::max(1, std::min(L.nbricks, c->num_sms * 8));
+    c->sgrid = std::max(1, std::min(L.nbricks, c->num_sms * 10));
+    const size_t npart = 2 * size_t(std::max(c->grid, c->sgrid)) + 8;
     setup_phys(c);
     int rc = SWC_OK;
     const size_t slots = size_t(L.nbricks) * bx * by * bz;
@@ -513,21 +531,24 @@ int swc_create(const swc_scene * s, const swc_solver_opts * o, swc_ctx ** out) {
         (rc = dalloc(c, &c->N.q, slots)) || (rc = dalloc(c, &c->N.d0, slots)) || (rc = dalloc(c, &c->N.d1, slots)))
         return fail(rc);
     if (c->opts.keep_virtual_velocity && (rc = dalloc(c, &c->N.vbar, slots))) return fail(rc);
-    if (c->opts.keep_features && (rc = dalloc(c, &c->N.nreal, slots))) return fail(rc);
+    if (c->opts.keep_features && ((rc = dalloc(c, &c->N.nreal, slots)) || (rc = dalloc(c, &c->N.nvirt, slots))))
+        return fail(rc);
     c->B.nseg = (long long) L.ny * L.nz * L.bnx;
     if ((rc = dalloc(c, &c->B.flag, L.nbricks)) || (rc = dalloc(c, &c->B.flag_prev, L.nbricks)) ||
         (rc = dalloc(c, &c->B.list, L.nbricks)) || (rc = dalloc(c, &c->B.count, 1)) ||
-        (rc = dalloc(c, &c->B.seg, c->B.nseg)) || (rc = dalloc(c, &c->B.seg_off, c->B.nseg + 1)))
+        (rc = dalloc(c, &c->B.seg, c->B.nseg)) || (rc = dalloc(c, &c->B.seg_off, c->B.nseg + 1)) ||
+        (rc = dalloc(c, &c->pflag, L.nbricks)) || (rc = dalloc(c, &c->plist, L.nbricks)) ||
+        (rc = dalloc(c, &c->pcount, 1)) || (rc = dalloc(c, &c->bnear, L.nbricks)))
         return fail(rc);
     if ((rc = dalloc(c, &c->pcomp, size_t(L.ncells))) || (rc = dalloc(c, &c->nv_prev, 1)) ||
         (rc = dalloc(c, &c->scan_tiles, scan_tile_count(std::max<long long>(c->B.nseg, L.ncells) + 1) + 2)) ||
-        (rc = dalloc(c, &c->cg, 1)) || (rc = dalloc(c, &c->partials, 2 * size_t(c->grid) + 8)) ||
+        (rc = dalloc(c, &c->cg, 1)) || (rc = dalloc(c, &c->partials, npart)) ||
         (rc = dalloc(c, &c->diag_bits, 1)) || (rc = dalloc(c, &c->max_bits, 1)) || (rc = dalloc(c, &c->res2, 2)) ||
         (rc = dalloc(c, &c->cellStart, L.ncells + 1)) || (rc = dalloc(c, &c->bcellStart, L.ncells + 1)))
         return fail(rc);
     if (cudaMallocHost(reinterpret_cast<void **>(&c->hcg), sizeof(HostCg)) != cudaSuccess) return fail(SWC_OUT_OF_MEMORY);
     cudaMemsetAsync(c->cg, 0, sizeof(CgState), c->stream);
-    cudaMemsetAsync(c->partials, 0, sizeof(double) * (2 * size_t(c->grid) + 8), c->stream);
+    cudaMemsetAsync(c->partials, 0, sizeof(double) * npart, c->stream);
     cudaMemsetAsync(c->B.flag, 0, L.nbricks, c->stream);
     cudaMemsetAsync(c->B.flag_prev, 0, L.nbricks, c->stream);
     cudaMemsetAsync(c->N.flag, 0, slots, c->stream);
@@ -577,12 +598,17 @@ void swc_destroy(swc_ctx * c) {
     dfree(c->N.d1);
     dfree(c->N.vbar);
     dfree(c->N.nreal);
+    dfree(c->N.nvirt);
     dfree(c->B.flag);
     dfree(c->B.flag_prev);
     dfree(c->B.list);
     dfree(c->B.count);
     dfree(c->B.seg);
     dfree(c->B.seg_off);
+    dfree(c->pflag);
+    dfree(c->plist);
+    dfree(c->pcount);
+    dfree(c->bnear);
     dfree(c->pcomp);
     dfree(c->nv_prev);
     dfree(c->scan_tiles);
@@ -631,7 +657,7 @@ int swc_set_solver_opts(swc_ctx * c, const swc_solver_opts * o) {
         c->g1 = c->g8 = nullptr;
     }
     if (need_vbar && (rc = dalloc(c, &c->N.vbar, slots))) return rc;
-    if (need_feat && (rc = dalloc(c, &c->N.nreal, slots))) return rc;
+    if (need_feat && ((rc = dalloc(c, &c->N.nreal, slots)) || (rc = dalloc(c, &c->N.nvirt, slots)))) return rc;
     return SWC_OK;
 }
 
@@ -891,14 +917,14 @@ int swc_apply_operator(swc_ctx * c, const double * x, double * y, int64_t n) {
     // brick-layout vector: reuse compact export machinery through a temporary NodeArrays view
     if (c->dim == 2) {
         launch_compact_import<2>(c->L, c->B, c->N, d_in, t_in, c->grid, c->stream);
-        launch_apply_operator<2>(c->L, c->B, c->N, c->S, t_in, t_out, c->grid, c->stream);
+        launch_apply_operator<2>(c->L, c->B, c->N, c->S, t_in, t_out, c->sgrid, c->stream);
         NodeArrays T = c->N;
         T.x          = t_out;
         launch_compact_export<2>(c->L, c->B, T, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, d_out,
                                  nullptr, c->grid, c->stream);
     } else {
         launch_compact_import<3>(c->L, c->B, c->N, d_in, t_in, c->grid, c->stream);
-        launch_apply_operator<3>(c->L, c->B, c->N, c->S, t_in, t_out, c->grid, c->stream);
+        launch_apply_operator<3>(c->L, c->B, c->N, c->S, t_in, t_out, c->sgrid, c->stream);
         NodeArrays T = c->N;
         T.x          = t_out;
         launch_compact_export<3>(c->L, c->B, T, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, d_out,
@@ -910,6 +936,41 @@ int swc_apply_operator(swc_ctx * c, const double * x, double * y, int64_t n) {
     cudaFree(d_out);
     cudaFree(t_in);
     cudaFree(t_out);
+    CK(cudaGetLastError());
+    return SWC_OK;
+}
+
+int swc_debug_neighbors(swc_ctx * c, int which, int64_t nq, const double * q, int64_t * counts,
+                        const int64_t * offsets, int64_t * ids) {
+    if (!valid_ctx(c) || which < 0 || which > 2 || nq < 0 || (nq > 0 && (!q || !counts))) return SWC_BAD_ARG;
+    if (ids && !offsets) return SWC_BAD_ARG;
+    if (nq == 0) return SWC_OK;
+    int64_t total = 0;
+    if (ids) total = offsets[nq - 1] + counts[nq - 1];
+    double * dq = nullptr;
+    long long *dc = nullptr, *doff = nullptr, *dids = nullptr;
+    CK(cudaMalloc(&dq, sizeof(double) * nq * c->dim));
+    CK(cudaMalloc(&dc, sizeof(long long) * nq));
+    if (ids) {
+        CK(cudaMalloc(&doff, sizeof(long long) * nq));
+        CK(cudaMalloc(&dids, sizeof(long long) * std::max<int64_t>(total, 1)));
+        cudaMemcpy(doff, offsets, sizeof(long long) * nq, cudaMemcpyHostToDevice);
+    }
+    cudaMemcpy(dq, q, sizeof(double) * nq * c->dim, cudaMemcpyHostToDevice);
+    const float4 * P  = which == 0 ? c->pos : c->bpos;
+    const int * ID    = which == 0 ? c->id : c->bid;
+    const int * CS    = which == 0 ? c->cellStart : c->bcellStart;
+    if (c->dim == 2)
+        launch_debug_neighbors<2>(which, nq, dq, c->L, c->P, P, ID, CS, c->B.flag, c->N.flag, dc, doff, dids, c->stream);
+    else
+        launch_debug_neighbors<3>(which, nq, dq, c->L, c->P, P, ID, CS, c->B.flag, c->N.flag, dc, doff, dids, c->stream);
+    cudaStreamSynchronize(c->stream);
+    cudaMemcpy(counts, dc, sizeof(long long) * nq, cudaMemcpyDeviceToHost);
+    if (ids && total > 0) cudaMemcpy(ids, dids, sizeof(long long) * total, cudaMemcpyDeviceToHost);
+    cudaFree(dq);
+    cudaFree(dc);
+    cudaFree(doff);
+    cudaFree(dids);
     CK(cudaGetLastError());
     return SWC_OK;
 }
@@ -955,15 +1016,16 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
     auto launch = [&]() {
         if (c->dim == 3) {
             switch (which) {
-            case 0: launch_cg_spmv<3>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->grid, c->stream); break;
+            case 0: launch_cg_spmv<3>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->sgrid, c->stream); break;
             case 1: launch_cg_update<3>(c->B, c->N, c->cg, c->partials, c->grid, c->stream); break;
             case 2:
                 launch_node_gather<3>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel,
-                                      c->bcellStart, c->grid, c->stream);
+                                      c->bcellStart, c->bnear, c->grid, c->stream);
                 break;
             case 3:
-                launch_pressure_gradient<3>(c->pos, c->vel, c->n, c->L, c->P, c->B.flag, c->N.V, c->N.x, c->bpos,
-                                            c->bvel, c->bnrm, c->bcellStart, c->stream);
+                launch_pressure_gradient<3>(c->L, c->P, c->B, c->N, c->plist, c->pcount, c->bnear, c->pos, c->vel,
+                                            c->cellStart, c->bpos, c->bvel, c->bnrm, c->bcellStart, c->grid,
+                                            c->stream);
                 break;
             case 4: launch_density<3>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->stream); break;
             case 5: launch_forces<3>(c->pos, c->vel, c->vel2, c->n, c->L, c->P, c->cellStart, 0.f, c->stream); break;
@@ -972,7 +1034,7 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
             switch (which) {
             case 2:
                 launch_node_gather<2>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel,
-                                      c->bcellStart, c->grid, c->stream);
+                                      c->bcellStart, c->bnear, c->grid, c->stream);
                 break;
             case 4: launch_density<2>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->stream); break;
             default: break;

@@ -26,7 +26,7 @@ template<> struct BrickGeom<3> {
     static constexpr int BX = 8, BY = 8, BZ = 8, BN = 512;
     static constexpr int HALO = 4;                                    // virtual stencil reach (|k|^2 < 16)
     static constexpr int TX = BX + 2 * HALO, TY = BY + 2 * HALO, TZ = BZ + 2 * HALO;
-    static constexpr int PX = 24;                                     // padded row pitch (conflict-free)
+    static constexpr int PX = 20;  // row pitch: 16-byte aligned rows, conflict-free LDS.128 for 8 rows
     static constexpr int PXY = PX * TY;
     static constexpr int TILE = PXY * TZ;
 };
@@ -55,7 +55,7 @@ struct Phys {
     float h, h2, inv_h, c0h, c1h;   // real / boundary kernel, support h = 4 r
     float H, H2, inv_H, c0H, c1H;   // virtual kernel, support H = 4 * grid spacing
     double h_d, inv_h_d, c0h_d;     // FP64 copies for the activation re-test
-    float mass, bmass;
+    float mass, bmass, inv_mass;
     float rho0, kappa, alpha0;
     int   cell_lo, cell_hi;         // node-centred cell window for a radius-h query
     float gx, gy, gz;               // gravity
@@ -80,6 +80,17 @@ __device__ __forceinline__ float kdW(float r, float inv_h, float c1) {
     if (x < 0.5f) return c1 * x * (3.f * x - 2.f);
     if (x < 1.f) return -c1 * (1.f - x) * (1.f - x);
     return 0.f;
+}
+// W_h(r) and -W'_h(r)/r from r^2 without a division: with q = r/h,
+// -W'/r = -c1 (3q - 2)/h for q < 1/2 and c1 (1 - q)^2 / r otherwise; at r = 0 the
+// factor stays finite and multiplies a zero offset (gradientKernel(0) = 0).
+__device__ __forceinline__ void kernel_and_grad(float r2, float inv_h, float c0, float c1, float & w, float & gsc) {
+    const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
+    const float q    = r2 * rinv * inv_h;
+    const float t    = 1.f - q;
+    const bool inner = q < 0.5f;
+    w   = inner ? c0 * (6.f * q * q * (q - 1.f) + 1.f) : (q < 1.f ? c0 * 2.f * t * t * t : 0.f);
+    gsc = inner ? -c1 * inv_h * (3.f * q - 2.f) : (q < 1.f ? c1 * t * t * rinv : 0.f);
 }
 __device__ __forceinline__ double kW_d(double r, double inv_h, double c0) {
     const double x = r * inv_h;
@@ -132,27 +143,47 @@ template<int NT> __device__ __forceinline__ double block_sum_ff(FF a, double * s
     return block_sum_double<NT>(v, sm);
 }
 
-// Last-block-done reduction: every block writes `part` to partials[blockIdx.x];
-// the block that finishes last sums all partials in fixed order (deterministic)
-// and returns true with the total in *out (thread 0 only).
-__device__ __forceinline__ bool last_block_reduce(double part, double * partials, unsigned int * ticket,
-                                                  double * out, int * is_last_sm) {
-    if (threadIdx.x == 0) {
-        partials[blockIdx.x] = part;
-        __threadfence();
-        const unsigned int t = atomicAdd(ticket, 1u);
-        *is_last_sm = (t == gridDim.x - 1);
-    }
+// Block-wide FP64 sum returned to every thread of the block.
+template<int NT> __device__ __forceinline__ double block_sum_double_all(double v, double * sm) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     __syncthreads();
-    if (!*is_last_sm) return false;
-    __threadfence();
+    if (l == 0) sm[w] = v;
+    __syncthreads();
     if (threadIdx.x == 0) {
         double s = 0;
-        volatile double * vp = partials;
-        for (unsigned int b = 0; b < gridDim.x; b++) s += vp[b];
-        *out    = s;
-        *ticket = 0u;
+        for (int i = 0; i < NT / 32; i++) s += sm[i];
+        sm[NT / 32] = s;
     }
+    __syncthreads();
+    return sm[NT / 32];
+}
+
+// Grid-wide deterministic reduction of NV values.  Thread 0 of every block
+// publishes its block's values part[k] at partials[k * gridDim.x + blockIdx.x];
+// the block that arrives last sums each value over all blocks with all of its
+// threads in a fixed order and returns true with the totals in out[k] (every
+// thread of that block).  `sm` needs NT/32 + 1 doubles, `flag` is a shared int.
+template<int NT, int NV>
+__device__ __forceinline__ bool grid_reduce(const double (&part)[NV], double * partials, unsigned int * ticket,
+                                            double (&out)[NV], double * sm, int * flag) {
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) partials[k * gridDim.x + blockIdx.x] = part[k];
+        __threadfence();
+        *flag = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!*flag) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        double s = 0;
+        for (unsigned int i = threadIdx.x; i < gridDim.x; i += NT) s += __ldcg(partials + k * gridDim.x + i);
+        out[k] = block_sum_double_all<NT>(s, sm);
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
     return true;
 }
 
@@ -190,6 +221,62 @@ __device__ __forceinline__ float slab_dist(float q, int c, int n, float o, float
     const float lo = (c == 0) ? -3.0e38f : o + c * dx;
     const float hi = (c == n - 1) ? 3.0e38f : o + (c + 1) * dx;
     return q < lo ? lo - q : (q > hi ? q - hi : 0.f);
+}
+
+// Neighbour iteration over cells for a query point and radius R (particle
+// queries): rows pruned by their slab distance, x-range per row from the
+// remaining radius; f(j) for every particle j of the visited cells.
+template<int DIM, class F>
+__device__ __forceinline__ void for_each_in_radius(const Lattice & L, const int * __restrict__ cellStart,
+                                                   float qx, float qy, float qz, float R, float R2, F && f) {
+    const int cy0 = clampi(__float2int_rd((qy - R - L.oy) * L.inv_dx), 0, L.ny - 1);
+    const int cy1 = clampi(__float2int_rd((qy + R - L.oy) * L.inv_dx), 0, L.ny - 1);
+    int cz0 = 0, cz1 = 0;
+    if (DIM == 3) {
+        cz0 = clampi(__float2int_rd((qz - R - L.oz) * L.inv_dx), 0, L.nz - 1);
+        cz1 = clampi(__float2int_rd((qz + R - L.oz) * L.inv_dx), 0, L.nz - 1);
+    }
+    for (int cz = cz0; cz <= cz1; cz++) {
+        const float dz  = DIM == 3 ? slab_dist(qz, cz, L.nz, L.oz, L.dx) : 0.f;
+        const float rz2 = R2 - dz * dz;
+        if (rz2 <= 0.f) continue;
+        for (int cy = cy0; cy <= cy1; cy++) {
+            const float dy  = slab_dist(qy, cy, L.ny, L.oy, L.dx);
+            const float rem = rz2 - dy * dy;
+            if (rem <= 0.f) continue;
+            const float rx = sqrtf(rem) * 1.000001f + 1e-7f * L.dx;
+            const int cx0  = clampi(__float2int_rd((qx - rx - L.ox) * L.inv_dx), 0, L.nx - 1);
+            const int cx1  = clampi(__float2int_rd((qx + rx - L.ox) * L.inv_dx), 0, L.nx - 1);
+            const long long row = (long long) L.nx * (cy + (long long) L.ny * cz);
+            const int b = cellStart[row + cx0], e = cellStart[row + cx1 + 1];
+            for (int j = b; j < e; j++) f(j);
+        }
+    }
+}
+
+// Friction-free wall term of the pressure-gradient update for particle
+// (q, vi): - sum_b V_b min(n_b.(v_i - v_b), 0) n_b W_h(x_i - x_b)
+// (VirtualParticle::applyPressureGradient, Cores/Structures/VirtualParticle.cpp:122-128).
+template<int DIM>
+__device__ __forceinline__ float3 wall_term(const Lattice & L, const Phys & P, const int * __restrict__ bcellStart,
+                                            const float4 * __restrict__ bpos, const float4 * __restrict__ bvel,
+                                            const float4 * __restrict__ bnrm, float4 q, float4 vi) {
+    float3 f = make_float3(0.f, 0.f, 0.f);
+    for_each_in_radius<DIM>(L, bcellStart, q.x, q.y, q.z, P.h, P.h2, [&](int j) {
+        const float4 p = bpos[j];
+        const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 < P.h2) {
+            const float4 nb = bnrm[j];
+            const float4 vb = bvel[j];
+            const float vn  = fminf(nb.x * (vi.x - vb.x) + nb.y * (vi.y - vb.y) + nb.z * (vi.z - vb.z), 0.f);
+            const float c   = p.w * vn * kW(sqrtf(r2), P.inv_h, P.c0h);
+            f.x -= c * nb.x;
+            f.y -= c * nb.y;
+            f.z -= c * nb.z;
+        }
+    });
+    return f;
 }
 
 // --------------------------------------------------------------------------

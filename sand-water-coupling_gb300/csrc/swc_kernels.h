@@ -37,6 +37,7 @@ struct NodeArrays {
     float *         d1        = nullptr;
     float4 *        vbar      = nullptr;  // optional: virtual velocity (debug / export)
     unsigned short * nreal    = nullptr;  // optional: real neighbours within h
+    unsigned short * nvirt    = nullptr;  // optional: active virtual neighbours within H (self included)
 };
 
 struct BrickArrays {
@@ -82,25 +83,33 @@ void launch_boundary_density(float4 * bpos, float4 * bvel, float * rho, long lon
                              const Phys & P, const int * bcellStart, cudaStream_t st);
 template<int DIM>
 void launch_mark_bricks(const float4 * pos, long long n, const Lattice & L, const Phys & P, unsigned char * bflag,
-                        cudaStream_t st);
+                        unsigned char * pflag, cudaStream_t st);
 template<int DIM>
-void launch_pressure_gradient(const float4 * pos, float4 * vel, long long n, const Lattice & L, const Phys & P,
-                              const unsigned char * bflag, const float * nodeV, const float * nodeP,
-                              const float4 * bpos, const float4 * bvel, const float4 * bnrm, const int * bcellStart,
-                              cudaStream_t st);
+void launch_debug_neighbors(int which, long long nq, const double * q, const Lattice & L, const Phys & P,
+                            const float4 * pos, const int * id, const int * cellStart, const unsigned char * bflag,
+                            const unsigned char * nflag, long long * counts, const long long * offsets, long long * ids,
+                            cudaStream_t st);
 
 // ---- k_nodes.cu ----
 void launch_brick_list(const unsigned char * bflag, int nbricks, int * list, int * count, cudaStream_t st);
 template<int DIM>
 void launch_node_gather(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
                         const float4 * pos, const float4 * vel, const int * cellStart, const float4 * bpos,
-                        const float4 * bvel, const int * bcellStart, int grid, cudaStream_t st);
+                        const float4 * bvel, const int * bcellStart, const unsigned char * bnear, int grid,
+                        cudaStream_t st);
+// Pressure-gradient update over the bricks that hold particles (plist / pcount),
+// node field staged per brick in shared memory; bnear flags bricks near walls.
+template<int DIM>
+void launch_pressure_gradient(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
+                              const int * plist, const int * pcount, const unsigned char * bnear, const float4 * pos,
+                              float4 * vel, const int * cellStart, const float4 * bpos, const float4 * bvel,
+                              const float4 * bnrm, const int * bcellStart, int grid, cudaStream_t st);
 template<int DIM>
 void launch_segments(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int * tiles, int grid,
                      cudaStream_t st);
 template<int DIM>
 void launch_ahat(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
-                 int grid, cudaStream_t st);
+                 unsigned short * nvirt, int sgrid, cudaStream_t st);
 template<int DIM>
 void launch_diag_max_f64(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const StencilD & S,
                          unsigned long long * out_bits, int grid, cudaStream_t st);
@@ -116,19 +125,19 @@ void launch_compact_export(const Lattice & L, const BrickArrays & B, const NodeA
 // CG
 template<int DIM>
 void launch_cg_init(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
-                    double * partials, double tol, int max_iterations, const int * nv, int grid, cudaStream_t st);
+                    double * partials, double tol, int max_iterations, const int * nv, int sgrid, cudaStream_t st);
 template<int DIM>
 void launch_cg_iteration(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
-                         CgState * cg, double * partials, int grid, cudaStream_t st);
+                         CgState * cg, double * partials, int sgrid, int ugrid, cudaStream_t st);
 template<int DIM>
 void launch_cg_spmv(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
-                    double * partials, int grid, cudaStream_t st);
+                    double * partials, int sgrid, cudaStream_t st);
 template<int DIM>
-void launch_cg_update(const BrickArrays & B, const NodeArrays & N, CgState * cg, double * partials, int grid,
+void launch_cg_update(const BrickArrays & B, const NodeArrays & N, CgState * cg, double * partials, int ugrid,
                       cudaStream_t st);
 template<int DIM>
 void launch_apply_operator(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
-                           const float * in, float * out, int grid, cudaStream_t st);
+                           const float * in, float * out, int sgrid, cudaStream_t st);
 template<int DIM>
 void launch_zero_active(const Lattice & L, const BrickArrays & B, float * a, int grid, cudaStream_t st);
 template<int DIM>
@@ -136,6 +145,6 @@ void launch_compact_import(const Lattice & L, const BrickArrays & B, const NodeA
                            float * out, int grid, cudaStream_t st);
 template<int DIM>
 void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
-                          double * partials, double * out2, int grid, cudaStream_t st);
+                          CgState * cg, double * partials, double * out2, int sgrid, cudaStream_t st);
 
 }  // namespace swc

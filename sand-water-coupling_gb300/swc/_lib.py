@@ -102,6 +102,7 @@ SIGNATURES = {
     "swc_get_virtual": (C.c_int, [_P, _I64, _D, _D, _D, _D, _D, _D, C.c_int64]),
     "swc_set_pressure": (C.c_int, [_P, _D, C.c_int64]),
     "swc_apply_operator": (C.c_int, [_P, _D, _D, C.c_int64]),
+    "swc_debug_neighbors": (C.c_int, [_P, C.c_int, C.c_int64, _D, _I64, _I64, _I64]),
     "swc_set_profiling": (C.c_int, [_P, C.c_int]),
     "swc_get_phase_times": (C.c_int, [_P, _D, C.c_int]),
     "swc_time_kernel": (C.c_int, [_P, C.c_int, C.c_int, _D]),

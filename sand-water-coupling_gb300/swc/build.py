@@ -71,6 +71,28 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
     return LIB_PATH
 
 
+EXAMPLES_DIR = os.path.join(PKG_ROOT, "examples")
+EXAMPLES_BIN = os.path.join(BUILD_DIR, "examples")
+
+
+def build_examples(force: bool = False) -> list:
+    """C++ callers of include/swc/DualParticleSphLiquid.hpp, linked against the library."""
+    lib = build()
+    os.makedirs(EXAMPLES_BIN, exist_ok=True)
+    out = []
+    for src in sorted(glob.glob(os.path.join(EXAMPLES_DIR, "*.cpp"))):
+        exe = os.path.join(EXAMPLES_BIN, os.path.splitext(os.path.basename(src))[0])
+        if force or not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(src),
+                                                                            os.path.getmtime(lib)):
+            cmd = [os.environ.get("CXX", "g++"), "-std=c++20", "-O2", "-I", os.path.join(REPO_ROOT, "include"), src,
+                   "-L", os.path.dirname(lib), "-lswc_gb300", f"-Wl,-rpath,{os.path.dirname(lib)}", "-o", exe]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"example build failed: {os.path.basename(src)}\n{r.stderr[-3000:]}")
+        out.append(exe)
+    return out
+
+
 if __name__ == "__main__":
     import sys
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -231,6 +231,24 @@ class DualParticleSphLiquid:
         self._check(self.L.swc_apply_operator(self.h, _dp(x), _dp(y), x.shape[0]), "swc_apply_operator")
         return y
 
+    def neighbors(self, which, queries):
+        """Sorted neighbour ids per query point (product cell search; see swc_debug_neighbors)."""
+        w = {"real": 0, "boundary": 1, "virtual": 2}[which]
+        q = _f64(queries)
+        nq = q.shape[0]
+        counts = np.zeros(nq, dtype=np.int64)
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int64))
+        self._check(self.L.swc_debug_neighbors(self.h, w, nq, _dp(q), ip(counts), None, None), "swc_debug_neighbors")
+        offsets = np.zeros(nq + 1, dtype=np.int64)
+        offsets[1:] = np.cumsum(counts)
+        ids = np.zeros(max(1, int(offsets[-1])), dtype=np.int64)
+        self._check(self.L.swc_debug_neighbors(self.h, w, nq, _dp(q), ip(counts), ip(offsets), ip(ids)),
+                    "swc_debug_neighbors")
+        ids = ids[: offsets[-1]]
+        for t in range(nq):
+            ids[offsets[t]:offsets[t + 1]].sort()
+        return counts, offsets, ids
+
     def setProfiling(self, on=True):
         self._check(self.L.swc_set_profiling(self.h, 1 if on else 0), "swc_set_profiling")
 

@@ -1,0 +1,240 @@
+"""GPU parity: the CUDA path (through the C ABI) against the FP64 oracle.
+
+Inputs are rounded through float32 first so both sides see identical values.
+Per-projection replay: before each compared step the oracle is handed the GPU's
+state (positions, velocities, per-particle volumes, boundary volumes, rho0,
+alpha0, kappa), so each comparison measures one step of the path and not the
+divergence of two chaotic trajectories.
+
+Tolerances (FP32 state and kernel sums vs FP64):
+  neighbour sets and the active virtual set: identical
+  rho_i, V_i, rho_I, V_I, alpha_hat: 2e-5 relative (element-wise)
+  D_I: 1e-4 of max |D|
+  post-projection velocity: 1e-4 relative (norm), the path's stated bar
+"""
+import numpy as np
+import pytest
+
+from swc import scenes
+
+pytestmark = pytest.mark.gpu
+
+TOL_V = 1e-4
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def make_pair(swc_mod, oracle_mod, scene, **kw):
+    s = scene.rounded_to_float32()
+    liq = swc_mod.DualParticleSphLiquid(s, keep_virtual_velocity=True, keep_features=True, **kw)
+    liq.initialize()
+    ref = oracle_mod.Oracle(s, tolerance=kw.get("tolerance"))
+    ref.initialize()
+    return s, liq, ref
+
+
+def sync_oracle(liq, ref):
+    """Hand the GPU's state to the oracle (replay)."""
+    x, v = liq.getParticles()
+    ref.set_particles(x, v)
+    _, vol = liq.realInfo()
+    ref.set_volumes(vol)
+    rb, vb = liq.boundaryInfo()
+    ref.set_boundary_info(rb, vb)
+    sc = liq.scalars()
+    ref.set_scalars(sc["rho0"], sc["alpha0"], sc["kappa"])
+
+
+SCENES = {
+    "dam_break_2d": lambda: scenes.dam_break_2d(seed=0),
+    "block_3d_n16": lambda: scenes.projection_block_3d(n=16, seed=1),
+    "block_3d_n24": lambda: scenes.projection_block_3d(n=24, seed=2),
+    "dam_break_3d_small": lambda: scenes.dam_break_3d(seed=3, cells=(24, 12, 12), domain=(0.4, 0.2, 0.2)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_initialize_parity(swc_mod, oracle_mod, name):
+    s, liq, ref = make_pair(swc_mod, oracle_mod, SCENES[name]())
+    rg, vg = liq.realInfo()
+    rr, vr = ref.real_info()
+    np.testing.assert_allclose(rg, rr, rtol=2e-5)
+    np.testing.assert_allclose(vg, vr, rtol=2e-5)
+    brg, bvg = liq.boundaryInfo()
+    brr, bvr = ref.boundary_info()
+    np.testing.assert_allclose(brg, brr, rtol=2e-5)
+    np.testing.assert_allclose(bvg, bvr, rtol=2e-5)
+    g, o = liq.scalars(), ref.scalars()
+    assert g["rho0"] == pytest.approx(o["rho0"], rel=2e-5)
+    assert g["alpha0"] == pytest.approx(o["alpha0"], rel=2e-5)
+    assert g["kappa"] == pytest.approx(o["kappa"], rel=1e-12)
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_projection_step_parity(swc_mod, oracle_mod, name):
+    s, liq, ref = make_pair(swc_mod, oracle_mod, SCENES[name]())
+    for step in range(3):
+        sync_oracle(liq, ref)
+        gp = liq.virtual()["p"] if step else np.zeros(0)
+        ref.set_pressure(gp)  # same warm start (reference prefix semantics)
+        st = liq.advance(s.dt)
+        ref.advance(s.dt)
+        assert st["status"] == 0
+        gv = liq.virtual(with_vbar=True)
+        ov = ref.virtual()
+        assert np.array_equal(gv["node"], ov["node"]), "active virtual sets differ"
+        np.testing.assert_allclose(gv["rho"], ov["rho"], rtol=2e-5, atol=1e-6 * np.abs(ov["rho"]).max())
+        np.testing.assert_allclose(gv["vol"], ov["vol"], rtol=2e-5, atol=1e-6 * np.abs(ov["vol"]).max())
+        np.testing.assert_allclose(gv["alpha_hat"], ov["alpha_hat"], rtol=2e-5)
+        np.testing.assert_allclose(gv["div"], ov["div"], rtol=0, atol=1e-4 * np.abs(ov["div"]).max())
+        assert rel(gv["vbar"], ov["vbar"]) < 1e-4
+        x, v = liq.getParticles()
+        xr, vr = ref.particles()
+        np.testing.assert_allclose(x, xr, rtol=0, atol=1e-6)
+        assert rel(v, vr) < TOL_V, (step, rel(v, vr))
+        # the GPU pressure solves the oracle's FP64 system to the CG tolerance
+        res = np.linalg.norm(ov["div"] - ref.apply_operator(gv["p"])) / np.linalg.norm(ov["div"])
+        assert res < 20 * s.tolerance + 1e-5, res
+
+
+@pytest.mark.parametrize("name", ["dam_break_2d", "block_3d_n16"])
+def test_neighbour_sets_exact(swc_mod, oracle_mod, name):
+    s, liq, ref = make_pair(swc_mod, oracle_mod, SCENES[name]())
+    sync_oracle(liq, ref)
+    liq.advance(s.dt)
+    ref.advance(s.dt)
+    x, _ = liq.getParticles()
+    rng = np.random.default_rng(0)
+    # queries: real particles, virtual node positions, and random points near the fluid
+    v = liq.virtual()
+    q_nodes = liq.nodePositions(v["node"][rng.choice(len(v["node"]), size=min(400, len(v["node"])), replace=False)])
+    q_rand = x[rng.choice(len(x), 300)] + rng.uniform(-0.02, 0.02, size=(300, s.dim))
+    q_real = x[rng.choice(len(x), 300)]
+    for which in ("real", "boundary", "virtual"):
+        for q in (q_real, q_nodes, q_rand):
+            cg, og, ig = liq.neighbors(which, q)
+            co, oo, io = ref.neighbors(which, q)
+            assert np.array_equal(cg, co), which
+            if which == "virtual":
+                node_ids = ref.virtual()["node"]
+                io = node_ids[io]
+                for t in range(len(q)):
+                    io[oo[t]:oo[t + 1]].sort()
+            assert np.array_equal(ig, io), which
+
+
+def test_apply_operator_parity(swc_mod, oracle_mod):
+    s, liq, ref = make_pair(swc_mod, oracle_mod, SCENES["block_3d_n24"]())
+    sync_oracle(liq, ref)
+    ref.set_pressure(np.zeros(0))
+    liq.advance(s.dt)
+    ref.advance(s.dt)
+    n = liq.numVirtual()
+    x = np.random.default_rng(1).normal(size=n).astype(np.float32).astype(np.float64)
+    yg = liq.applyOperator(x)
+    yo = ref.apply_operator(x)
+    assert rel(yg, yo) < 2e-6
+
+
+@pytest.mark.parametrize("name", ["dam_break_2d_small", "projection_block_3d_n8"])
+def test_against_golden_fixture(swc_mod, name):
+    import os
+    import sys
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.join(here, "golden"))
+    import make_golden
+
+    g = np.load(os.path.join(here, "golden", name + ".npz"))
+    build, steps = make_golden.CASES[name]
+    s = build().rounded_to_float32()
+    liq = swc_mod.DualParticleSphLiquid(s)
+    liq.initialize()
+    rho, vol = liq.realInfo()
+    np.testing.assert_allclose(rho, g["init_rho"], rtol=2e-5)
+    np.testing.assert_allclose(vol, g["init_vol"], rtol=2e-5)
+    assert liq.scalars()["alpha0"] == pytest.approx(float(g["alpha0"]), rel=2e-5)
+    for k in range(steps):
+        liq.advance(s.dt)
+        v = liq.virtual()
+        assert np.array_equal(v["node"], g[f"s{k}_node"])
+        np.testing.assert_allclose(v["alpha_hat"], g[f"s{k}_alpha_hat"], rtol=5e-5)
+        x, vel = liq.getParticles()
+        np.testing.assert_allclose(x, g[f"s{k}_x"], rtol=0, atol=1e-6)
+        assert rel(vel, g[f"s{k}_v"]) < 5 * TOL_V
+
+
+def test_warm_start_modes_agree(swc_mod, oracle_mod):
+    base = SCENES["block_3d_n24"]().rounded_to_float32()
+    results = {}
+    for mode in ("prefix", "node", "zero"):
+        liq = swc_mod.DualParticleSphLiquid(base, warm_start=mode, compute_true_residual=True)
+        liq.initialize()
+        for _ in range(3):
+            st = liq.advance(base.dt)
+            assert st["status"] == 0 and st["true_rel_residual"] < 5 * base.tolerance
+        results[mode] = (liq.getParticles()[1], st["cg_iterations"])
+    for mode in ("node", "zero"):
+        assert rel(results[mode][0], results["prefix"][0]) < 1e-4
+    assert results["node"][1] <= results["zero"][1]
+
+
+def test_deterministic_repeat(swc_mod):
+    s = SCENES["block_3d_n16"]().rounded_to_float32()
+    outs = []
+    for _ in range(2):
+        liq = swc_mod.DualParticleSphLiquid(s)
+        liq.initialize()
+        for _ in range(3):
+            liq.advance(s.dt)
+        outs.append(liq.getParticles())
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_status_codes(swc_mod):
+    s = SCENES["block_3d_n16"]().rounded_to_float32()
+    liq = swc_mod.DualParticleSphLiquid(s, max_iterations=1, tolerance=1e-12)
+    liq.initialize()
+    st = liq.advance(s.dt)
+    assert st["status"] == 1 and st["cg_iterations"] == 1  # SWC_CG_NOT_CONVERGED, no exit
+    liq2 = swc_mod.DualParticleSphLiquid(s, raise_on_nonconvergence=True, max_iterations=1, tolerance=1e-12)
+    liq2.initialize()
+    with pytest.raises(swc_mod.SwcError):
+        liq2.advance(s.dt)
+    # NaN velocities: detected and reported, the context stays usable
+    liq3 = swc_mod.DualParticleSphLiquid(s)
+    liq3.initialize()
+    x, v = liq3.getParticles()
+    v[5, 0] = np.nan
+    liq3.setParticles(x, v)
+    with pytest.raises(swc_mod.SwcError) as e:
+        liq3.project()
+    assert e.value.status == 2
+    v[5, 0] = 0.0
+    liq3.setParticles(x, v)
+    assert liq3.project()["status"] == 0
+    with pytest.raises(swc_mod.SwcError):
+        liq3.setParticles(x[:10], v[:10])  # count change after initialize
+
+
+def test_frame_roundtrip(swc_mod, tmp_path):
+    s = SCENES["dam_break_2d"]().rounded_to_float32()
+    a = swc_mod.DualParticleSphLiquid(s)
+    a.initialize()
+    for _ in range(3):
+        a.advance(s.dt)
+    a.saveFrame(str(tmp_path / "3"))
+    a.writeFrame(str(tmp_path / "3"))
+    a.writeDescription(str(tmp_path / "description.yaml"))
+    b = swc_mod.DualParticleSphLiquid(s)
+    b.loadFrame(str(tmp_path / "3"))
+    a.advance(s.dt)
+    b.advance(s.dt)
+    xa, va = a.getParticles()
+    xb, vb = b.getParticles()
+    np.testing.assert_array_equal(xa, xb)
+    assert rel(vb, va) < 1e-5
+    n = np.frombuffer((tmp_path / "3" / "particles.mesh").read_bytes()[:4], dtype=np.uint32)[0]
+    assert n == s.n_particles
