@@ -167,6 +167,47 @@ int swc_get_phase_times(swc_ctx * ctx, double * ms, int n);
  * 4: density, 5: forces); writes the mean ms per launch. */
 int swc_time_kernel(swc_ctx * ctx, int which, int reps, double * mean_ms);
 
+/* ---- Learned CG warm start (no counterpart in the reference) -------------
+ * A per-virtual-particle MLP 6 -> 64 -> 64 -> 1 (SiLU), BF16 tensor-core
+ * forward with FP32 accumulation, predicts the change of each node's pressure
+ * from the previous step.  Features of active node I (raw, before the
+ * normalisation carried with the network):
+ *   f0 = D_I / sD            f1 = alpha_hat_I / alpha0    f2 = nreal_I / 32
+ *   f3 = nvirt_I / 251 (45 in 2D)   f4 = p_prev_I alpha_hat_I / sD   f5 = rho_I / rho0
+ * with sD the RMS of D over active nodes, p_prev the previous pressure of the
+ * same node (0 for new nodes), nreal / nvirt the real particles within h and
+ * active virtual particles within H (self included).  Target / prediction:
+ *   t = (p_I - p_prev_I) alpha_hat_I / sD,  warm start p0_I = p_prev_I + t sD / alpha_hat_I.
+ * Parameters (SWC_MLP_PARAMS floats): W1[64][6], b1[64], W2[64][64], b2[64], w3[64], b3.
+ * Normalisation (SWC_MLP_NORM floats): feature mean[6], feature std[6], target mean, target std. */
+#define SWC_MLP_PARAMS 4673
+#define SWC_MLP_NORM 14
+/* Network used by SWC_WARM_LEARNED.  Each learned solve computes the initial
+ * residual of both the prediction and the node-mapped previous pressure and
+ * starts CG from the smaller (stats.warm_start_used tells which). */
+int swc_set_mlp(swc_ctx * ctx, const float * params, const float * norm);
+/* Training data of the last projection (needs keep_features): features
+ * (n x 6, reference order) and targets (n) as defined above.  Returns the
+ * count in *n (<= capacity). */
+int swc_get_features(swc_ctx * ctx, float * features, float * targets, int64_t capacity, int64_t * n);
+
+/* Device-side training of the network (forward on tensor cores, FP32 backward,
+ * Adam with FP32 master weights).  The dataset lives in device memory. */
+typedef struct swc_trainer swc_trainer;
+int  swc_trainer_create(int64_t capacity, int32_t batch, swc_trainer ** out);
+void swc_trainer_destroy(swc_trainer * tr);
+int  swc_trainer_add(swc_trainer * tr, const float * features, const float * targets, int64_t n);
+int  swc_trainer_set_params(swc_trainer * tr, const float * params, const float * norm);
+int  swc_trainer_get_params(swc_trainer * tr, float * params, float * norm);
+/* `epochs` passes over the shuffled dataset (seeded); epoch_loss[e] = mean squared
+ * error of the normalised output after epoch e. */
+int  swc_trainer_fit(swc_trainer * tr, int32_t epochs, float lr, uint64_t seed, float * epoch_loss);
+/* Stateless helpers on host arrays (run on the GPU): predictions, and the loss
+ * gradient for one batch. */
+int swc_mlp_forward(const float * params, const float * norm, const float * features, int64_t n, float * out);
+int swc_mlp_gradient(const float * params, const float * norm, const float * features, const float * targets,
+                     int64_t n, float * grad, float * loss);
+
 /* Pinned host memory helpers for callers that stream state every step. */
 void * swc_host_alloc(size_t bytes);
 void   swc_host_free(void * p);

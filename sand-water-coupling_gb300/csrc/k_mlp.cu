@@ -1,0 +1,538 @@
+// k_mlp.cu -- learned CG warm start: a per-virtual-particle MLP 6 -> 64 -> 64 -> 1
+// (SiLU) predicting the pressure change of a node from local features.  No
+// counterpart in the reference; CG still iterates to the same tolerance and the
+// node-mapped previous pressure is kept whenever the prediction starts from a
+// larger residual.
+//
+// Forward pass on the 5th-generation tensor cores: M = 128 rows (nodes) per tile,
+// BF16 operands staged in shared memory in the K-major no-swizzle canonical
+// layout (8-row x 16-byte core matrices), tcgen05.mma kind::f16 issued by one
+// thread with FP32 accumulators in TMEM (64 + 64 columns), completion tracked by
+// an mbarrier, accumulators read back with tcgen05.ld for the FP32 epilogues
+// (bias, SiLU, final 64-wide dot).  Every wait is bounded: on timeout the kernel
+// records an error, frees its TMEM and returns.
+//
+// Training: the same forward kernel (saving pre-activations), an FP32 backward
+// pass and Adam (FP32 master weights), all deterministic.
+#include <cuda_bf16.h>
+
+#include "swc_kernels.h"
+
+namespace swc {
+
+// ---------------------------------------------------------------------------
+// PTX helpers (tcgen05 / TMEM / mbarrier).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void * p) { return uint32_t(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t * dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// D (TMEM) = A * B (+ D when accumulate), A/B described in shared memory.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t * mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_init(uint64_t * mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t * mbar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(mbar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t * mbar, uint32_t parity) {
+    for (int i = 0; i < (1 << 22); i++)
+        if (mbar_try_wait(mbar, parity)) return true;
+    return false;
+}
+
+// 16 consecutive FP32 columns of this thread's TMEM lane (warp w reads lanes 32w..32w+31).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major, no swizzle; LBO = byte step between
+// core matrices along K, SBO = byte step between 8-row groups.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return uint64_t((saddr & 0x3FFFFu) >> 4) | (uint64_t(lbo >> 4) << 16) | (uint64_t(sbo >> 4) << 32) |
+           (uint64_t(1) << 46);
+}
+// Instruction descriptor, kind::f16: BF16 A and B (K-major), FP32 accumulate, M = 128, N = 64.
+constexpr uint32_t kIdescM128N64 = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+// Byte offset of element (r, k) of a K-major bf16 matrix with `kdim` columns.
+__device__ __forceinline__ uint32_t canon_off(int r, int k, int kdim) {
+    return uint32_t((r >> 3) * (kdim / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float dsilu(float z) {
+    const float s = 1.f / (1.f + __expf(-z));
+    return s * (1.f + z * (1.f - s));
+}
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+constexpr int kMlpIn = 6, kMlpH = 64;
+constexpr int kMlpParams = kMlpH * kMlpIn + kMlpH + kMlpH * kMlpH + kMlpH + kMlpH + 1;
+constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kMlpH * kMlpIn, kOffW2 = kOffB1 + kMlpH, kOffB2 = kOffW2 + kMlpH * kMlpH,
+              kOffW3 = kOffB2 + kMlpH, kOffB3 = kOffW3 + kMlpH;
+constexpr int kMlpNT = 128;  // threads = rows per tile
+
+// Per-node raw features (see the host documentation of swc_get_features).
+struct FeatScale {
+    float inv_sD, inv_alpha0, inv_rho0, inv_nreal, inv_nvirt;
+};
+
+__device__ __forceinline__ void node_features(const NodeArrays & N, long long s, const FeatScale & F, float (&f)[6]) {
+    const float ah = N.ahat[s];
+    f[0] = N.D[s] * F.inv_sD;
+    f[1] = ah * F.inv_alpha0;
+    f[2] = (N.nreal ? float(N.nreal[s]) : 0.f) * F.inv_nreal;
+    f[3] = (N.nvirt ? float(N.nvirt[s]) : 0.f) * F.inv_nvirt;
+    f[4] = N.x[s] * ah * F.inv_sD;  // x holds the node-mapped previous pressure here
+    f[5] = N.rho[s] * F.inv_rho0;
+}
+
+// Modes of the forward kernel.
+enum { kMlpFromArray = 0, kMlpFromNodes = 1 };
+
+// params: FP32 vector (layout above); norm: f_mean[6], f_std[6], t_mean, t_std.
+// kMlpFromArray: rows of feat[n][6] -> out[n] (prediction t); optional saves of
+//   z1, z2 (pre-activations) and h1 (bf16-rounded) for training.
+// kMlpFromNodes: rows = active nodes (slot_of[I]); writes the warm start
+//   x[s] = p_prev + t * sD / alpha_hat into N.x (and feat_out when non-null).
+__global__ void __launch_bounds__(kMlpNT) k_mlp_forward(int mode, long long n, const float * __restrict__ params,
+                                                        const float * __restrict__ norm,
+                                                        const float * __restrict__ feat, float * __restrict__ out,
+                                                        float * __restrict__ z1s, float * __restrict__ h1s,
+                                                        float * __restrict__ z2s, NodeArrays N,
+                                                        const int * __restrict__ slot_of, const int * __restrict__ nv,
+                                                        const CgState * __restrict__ cg, FeatScale F0,
+                                                        float * __restrict__ feat_out, int * __restrict__ err) {
+    __shared__ __align__(1024) uint8_t sw1[kMlpH * 16 * 2];   // W1 [64 x 16] bf16 (K padded 6 -> 16)
+    __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpH * 2];  // W2 [64 x 64]
+    __shared__ __align__(1024) uint8_t sx[kMlpNT * 16 * 2];    // X  [128 x 16]
+    __shared__ __align__(1024) uint8_t sh[kMlpNT * kMlpH * 2];  // H1 [128 x 64]
+    __shared__ float sb1[kMlpH], sb2[kMlpH], sw3[kMlpH], snorm[14];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    if (warp == 0) {
+        tmem_alloc(&tmem_base, 128);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        mbar_init(&mbar, 1);
+        s_fail = 0;
+    }
+    // weights -> bf16 canonical layouts
+    for (int e = tid; e < kMlpH * 16; e += kMlpNT) {
+        const int r = e / 16, k = e % 16;
+        const float w = k < kMlpIn ? params[kOffW1 + r * kMlpIn + k] : 0.f;
+        *reinterpret_cast<__nv_bfloat16 *>(sw1 + canon_off(r, k, 16)) = __float2bfloat16_rn(w);
+    }
+    for (int e = tid; e < kMlpH * kMlpH; e += kMlpNT) {
+        const int r = e / kMlpH, k = e % kMlpH;
+        *reinterpret_cast<__nv_bfloat16 *>(sw2 + canon_off(r, k, kMlpH)) = __float2bfloat16_rn(params[kOffW2 + e]);
+    }
+    if (tid < kMlpH) {
+        sb1[tid] = params[kOffB1 + tid];
+        sb2[tid] = params[kOffB2 + tid];
+        sw3[tid] = params[kOffW3 + tid];
+    }
+    if (tid < 14) snorm[tid] = norm[tid];
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const float b3 = params[kOffB3];
+    const uint32_t tbase = tmem_base;
+    const uint32_t lane_off = uint32_t(warp * 32) << 16;
+    const uint64_t dW1 = smem_desc(smem_u32(sw1), 128, 256), dW2 = smem_desc(smem_u32(sw2), 128, 1024);
+    const uint64_t dX = smem_desc(smem_u32(sx), 128, 256), dH = smem_desc(smem_u32(sh), 128, 1024);
+
+    long long rows = n;
+    FeatScale F = F0;
+    if (mode == kMlpFromNodes) {
+        rows = *nv;
+        // sD = RMS of the right-hand side over active nodes
+        const double sD = rows > 0 ? sqrt(cg->bb / double(rows)) : 1.0;
+        F.inv_sD        = sD > 0 ? float(1.0 / sD) : 0.f;
+    }
+    uint32_t phase = 0;
+    const long long ntiles = (rows + kMlpNT - 1) / kMlpNT;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long row = tile * kMlpNT + tid;
+        const bool valid    = row < rows;
+        float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        long long s = 0;
+        if (valid) {
+            if (mode == kMlpFromArray) {
+#pragma unroll
+                for (int k = 0; k < 6; k++) f[k] = feat[row * 6 + k];
+            } else {
+                s = slot_of[row];
+                node_features(N, s, F, f);
+                if (feat_out) {
+#pragma unroll
+                    for (int k = 0; k < 6; k++) feat_out[row * 6 + k] = f[k];
+                }
+            }
+        }
+        // X row: normalised features in bf16, K padded to 16
+        float xn[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) xn[k] = valid ? (f[k] - snorm[k]) / snorm[6 + k] : 0.f;
+        uint4 c0 = make_uint4(pack_bf16(xn[0], xn[1]), pack_bf16(xn[2], xn[3]), pack_bf16(xn[4], xn[5]), 0u);
+        *reinterpret_cast<uint4 *>(sx + canon_off(tid, 0, 16)) = c0;
+        *reinterpret_cast<uint4 *>(sx + canon_off(tid, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            mma_bf16(tbase, dX, dW1, kIdescM128N64, 0u);
+            mma_commit(&mbar);
+        }
+        if (!mbar_wait(&mbar, phase)) s_fail = 1;
+        phase ^= 1u;
+        tc_fence_after();
+        // layer-1 epilogue: bias + SiLU -> H1 (bf16)
+#pragma unroll
+        for (int cblk = 0; cblk < 4; cblk++) {
+            float z[16];
+            tmem_ld16(tbase + lane_off + uint32_t(cblk * 16), z);
+            tmem_ld_wait();
+            uint32_t pk[8];
+#pragma unroll
+            for (int i = 0; i < 16; i += 2) {
+                const int c = cblk * 16 + i;
+                const float za = z[i] + sb1[c], zb = z[i + 1] + sb1[c + 1];
+                float ha = silu(za), hb = silu(zb);
+                if (z1s && valid) {
+                    z1s[row * kMlpH + c]     = za;
+                    z1s[row * kMlpH + c + 1] = zb;
+                }
+                pk[i / 2] = pack_bf16(ha, hb);
+                if (h1s && valid) {
+                    const __nv_bfloat162 hv = *reinterpret_cast<const __nv_bfloat162 *>(&pk[i / 2]);
+                    h1s[row * kMlpH + c]     = __bfloat162float(hv.x);
+                    h1s[row * kMlpH + c + 1] = __bfloat162float(hv.y);
+                }
+            }
+            *reinterpret_cast<uint4 *>(sh + canon_off(tid, cblk * 16, kMlpH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            *reinterpret_cast<uint4 *>(sh + canon_off(tid, cblk * 16 + 8, kMlpH)) =
+                make_uint4(pk[4], pk[5], pk[6], pk[7]);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+#pragma unroll
+            for (int j = 0; j < 4; j++)  // K = 64 in four K = 16 steps (2 core matrices = 256 B each)
+                mma_bf16(tbase + 64u, dH + uint64_t((j * 256) >> 4), dW2 + uint64_t((j * 256) >> 4), kIdescM128N64,
+                         j > 0 ? 1u : 0u);
+            mma_commit(&mbar);
+        }
+        if (!mbar_wait(&mbar, phase)) s_fail = 1;
+        phase ^= 1u;
+        tc_fence_after();
+        // layer-2 epilogue: bias + SiLU, final dot
+        float y = b3;
+#pragma unroll
+        for (int cblk = 0; cblk < 4; cblk++) {
+            float z[16];
+            tmem_ld16(tbase + lane_off + 64u + uint32_t(cblk * 16), z);
+            tmem_ld_wait();
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                const int c    = cblk * 16 + i;
+                const float zz = z[i] + sb2[c];
+                if (z2s && valid) z2s[row * kMlpH + c] = zz;
+                y = fmaf(sw3[c], silu(zz), y);
+            }
+        }
+        const float t = snorm[12] + snorm[13] * y;
+        if (valid) {
+            if (mode == kMlpFromArray) out[row] = t;
+            else {
+                const float ah = N.ahat[s];
+                const float pp = N.x[s];
+                N.x[s]         = pp + t / (F.inv_sD * ah);
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (s_fail) break;
+    }
+    __syncthreads();
+    if (s_fail && tid == 0) atomicExch(err, 1);
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tbase, 128);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Training: backward pass (FP32) and Adam.
+// Loss = mean over the batch of (y - (t - t_mean)/t_std)^2 on the normalised output.
+// ---------------------------------------------------------------------------
+// Per-row part: dz2 = 2 (y - ty)/B * w3 * silu'(z2); dz1 = (W2^T dz2) * silu'(z1).
+__global__ void __launch_bounds__(128) k_mlp_backward_rows(long long n, const float * __restrict__ params,
+                                                           const float * __restrict__ norm,
+                                                           const float * __restrict__ pred,
+                                                           const float * __restrict__ target,
+                                                           const float * __restrict__ z1s,
+                                                           const float * __restrict__ z2s, float * __restrict__ dz1,
+                                                           float * __restrict__ dz2, float * __restrict__ dy_out,
+                                                           float * __restrict__ sq_err) {
+    __shared__ float w2t[kMlpH][kMlpH + 1];
+    __shared__ float w3[kMlpH];
+    for (int e = threadIdx.x; e < kMlpH * kMlpH; e += blockDim.x) w2t[e % kMlpH][e / kMlpH] = params[kOffW2 + e];
+    if (threadIdx.x < kMlpH) w3[threadIdx.x] = params[kOffW3 + threadIdx.x];
+    __syncthreads();
+    const float tm = norm[12], ts = norm[13];
+    for (long long r = blockIdx.x * (long long) blockDim.x + threadIdx.x; r < n; r += (long long) gridDim.x * blockDim.x) {
+        const float y  = (pred[r] - tm) / ts;
+        const float ty = (target[r] - tm) / ts;
+        const float e  = y - ty;
+        sq_err[r]      = e * e;
+        const float dy = 2.f * e / float(n);
+        dy_out[r]      = dy;
+        float d2[kMlpH];
+#pragma unroll
+        for (int o = 0; o < kMlpH; o++) {
+            d2[o]                 = dy * w3[o] * dsilu(z2s[r * kMlpH + o]);
+            dz2[r * kMlpH + o]    = d2[o];
+        }
+#pragma unroll 4
+        for (int i = 0; i < kMlpH; i++) {
+            float a = 0.f;
+#pragma unroll
+            for (int o = 0; o < kMlpH; o++) a = fmaf(w2t[i][o], d2[o], a);  // (W2^T dz2)_i = sum_o W2[o][i] dz2[o]
+            dz1[r * kMlpH + i] = a * dsilu(z1s[r * kMlpH + i]);
+        }
+    }
+}
+
+// Weight gradients, one block per output unit o (rows summed in a fixed order):
+//   gW2[o][i] = sum_r dz2[r][o] h1[r][i]   gb2[o] = sum_r dz2[r][o]
+//   gW1[o][k] = sum_r dz1[r][o] x[r][k]    gb1[o] = sum_r dz1[r][o]
+//   gw3[o]    = sum_r dy[r] silu(z2[r][o]) gb3 = sum_r dy[r] (block 0)
+__global__ void __launch_bounds__(128) k_mlp_grad_weights(long long n, const float * __restrict__ norm,
+                                                          const float * __restrict__ feat,
+                                                          const float * __restrict__ h1s,
+                                                          const float * __restrict__ z2s,
+                                                          const float * __restrict__ dz1,
+                                                          const float * __restrict__ dz2,
+                                                          const float * __restrict__ dy, float * __restrict__ grad) {
+    const int o = blockIdx.x;
+    __shared__ float red[128][kMlpH + kMlpIn + 4];
+    float acc[kMlpH + kMlpIn + 4];
+#pragma unroll
+    for (int k = 0; k < kMlpH + kMlpIn + 4; k++) acc[k] = 0.f;
+    for (long long r = threadIdx.x; r < n; r += blockDim.x) {
+        const float g2 = dz2[r * kMlpH + o], g1 = dz1[r * kMlpH + o];
+#pragma unroll
+        for (int i = 0; i < kMlpH; i++) acc[i] = fmaf(g2, h1s[r * kMlpH + i], acc[i]);
+#pragma unroll
+        for (int k = 0; k < kMlpIn; k++) {
+            const float xk = (feat[r * kMlpIn + k] - norm[k]) / norm[kMlpIn + k];
+            acc[kMlpH + k] = fmaf(g1, __bfloat162float(__float2bfloat16_rn(xk)), acc[kMlpH + k]);
+        }
+        acc[kMlpH + kMlpIn] += g2;
+        acc[kMlpH + kMlpIn + 1] += g1;
+        acc[kMlpH + kMlpIn + 2] = fmaf(dy[r], silu(z2s[r * kMlpH + o]), acc[kMlpH + kMlpIn + 2]);
+        acc[kMlpH + kMlpIn + 3] += dy[r];
+    }
+#pragma unroll
+    for (int k = 0; k < kMlpH + kMlpIn + 4; k++) red[threadIdx.x][k] = acc[k];
+    __syncthreads();
+    for (int k = threadIdx.x; k < kMlpH + kMlpIn + 4; k += blockDim.x) {
+        float s = 0.f;
+        for (int t = 0; t < 128; t++) s += red[t][k];
+        if (k < kMlpH) grad[kOffW2 + o * kMlpH + k] = s;
+        else if (k < kMlpH + kMlpIn) grad[kOffW1 + o * kMlpIn + (k - kMlpH)] = s;
+        else if (k == kMlpH + kMlpIn) grad[kOffB2 + o] = s;
+        else if (k == kMlpH + kMlpIn + 1) grad[kOffB1 + o] = s;
+        else if (k == kMlpH + kMlpIn + 2) grad[kOffW3 + o] = s;
+        else if (o == 0) grad[kOffB3] = s;
+    }
+}
+
+// Adam (Kingma & Ba) with bias correction, FP32 master weights.
+__global__ void k_adam(float * __restrict__ p, const float * __restrict__ g, float * __restrict__ m,
+                       float * __restrict__ v, int count, float lr, float b1, float b2, float eps, float bc1,
+                       float bc2) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i]           = mi;
+        v[i]           = vi;
+        p[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    }
+}
+
+// Compact index -> slot of every active node (rows of the node-mode forward).
+template<int DIM>
+__global__ void __launch_bounds__(256) k_slot_of(Lattice L, const int * __restrict__ blist,
+                                                 const int * __restrict__ bcount, const int * __restrict__ seg_off,
+                                                 const unsigned char * __restrict__ flag, int * __restrict__ slot_of) {
+    using G      = BrickGeom<DIM>;
+    const int nb = *bcount;
+    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
+        const int b   = blist[bi];
+        const int bx  = b % L.bnx, by = (b / L.bnx) % L.bny, bz = b / (L.bnx * L.bny);
+        for (int l = threadIdx.x; l < G::BN; l += 256) {
+            const long long s = (long long) b * G::BN + l;
+            if (!flag[s]) continue;
+            const int lx = l % G::BX, ly = (l / G::BX) % G::BY, lz = l / (G::BX * G::BY);
+            const int y = by * G::BY + ly, z = bz * G::BZ + lz;
+            long long I = seg_off[((long long) z * L.ny + y) * L.bnx + bx];
+            for (int k = 0; k < lx; k++) I += flag[s - lx + k];
+            slot_of[I] = int(s);
+        }
+    }
+}
+
+// Target of the learned warm start for logging: (p - p_prev) alpha_hat / sD, with
+// p_prev the value kept in `prev` (node-mapped previous pressure).
+__global__ void k_mlp_targets(const int * __restrict__ nv, const int * __restrict__ slot_of,
+                              const float * __restrict__ x, const float * __restrict__ prev,
+                              const float * __restrict__ ahat, const CgState * __restrict__ cg,
+                              float * __restrict__ target) {
+    const long long rows = *nv;
+    const double sD = rows > 0 ? sqrt(cg->bb / double(rows)) : 1.0;
+    const float inv = sD > 0 ? float(1.0 / sD) : 0.f;
+    for (long long r = blockIdx.x * (long long) blockDim.x + threadIdx.x; r < rows; r += (long long) gridDim.x * blockDim.x) {
+        const long long s = slot_of[r];
+        target[r]         = (x[s] - prev[s]) * ahat[s] * inv;
+    }
+}
+
+// Features of every active node (training-data logging), x holding p_prev.
+__global__ void k_node_features(NodeArrays N, const int * __restrict__ slot_of, const int * __restrict__ nv,
+                                const CgState * __restrict__ cg, FeatScale F, float * __restrict__ feat_out) {
+    const long long rows = *nv;
+    const double sD      = rows > 0 ? sqrt(cg->bb / double(rows)) : 1.0;
+    F.inv_sD             = sD > 0 ? float(1.0 / sD) : 0.f;
+    for (long long r = blockIdx.x * (long long) blockDim.x + threadIdx.x; r < rows; r += (long long) gridDim.x * blockDim.x) {
+        float f[6];
+        node_features(N, slot_of[r], F, f);
+#pragma unroll
+        for (int k = 0; k < 6; k++) feat_out[r * 6 + k] = f[k];
+    }
+}
+
+// Batch gather for training: dst[i] = src[idx[i]] (6 features), dst_t[i] = src_t[idx[i]].
+__global__ void k_gather_rows(const float * __restrict__ src, const float * __restrict__ src_t,
+                              const int * __restrict__ idx, long long n, float * __restrict__ dst,
+                              float * __restrict__ dst_t) {
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        const long long j = idx[i];
+#pragma unroll
+        for (int k = 0; k < 6; k++) dst[i * 6 + k] = src[j * 6 + k];
+        dst_t[i] = src_t[j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+void launch_node_features(const NodeArrays & N, const int * slot_of, const int * nv, long long rows_max,
+                          const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal, float inv_nvirt,
+                          float * feat_out, cudaStream_t st) {
+    if (rows_max <= 0) return;
+    FeatScale F{0.f, inv_alpha0, inv_rho0, inv_nreal, inv_nvirt};
+    k_node_features<<<int(std::min<long long>((rows_max + 255) / 256, 152 * 8)), 256, 0, st>>>(N, slot_of, nv, cg, F,
+                                                                                             feat_out);
+}
+void launch_gather_rows(const float * src, const float * src_t, const int * idx, long long n, float * dst,
+                        float * dst_t, cudaStream_t st) {
+    if (n <= 0) return;
+    k_gather_rows<<<int(std::min<long long>((n + 255) / 256, 152 * 8)), 256, 0, st>>>(src, src_t, idx, n, dst, dst_t);
+}
+void launch_mlp_forward_array(long long n, const float * params, const float * norm, const float * feat, float * out,
+                              float * z1s, float * h1s, float * z2s, int * err, int grid, cudaStream_t st) {
+    if (n <= 0) return;
+    k_mlp_forward<<<grid, kMlpNT, 0, st>>>(kMlpFromArray, n, params, norm, feat, out, z1s, h1s, z2s, NodeArrays{},
+                                           nullptr, nullptr, nullptr, FeatScale{}, nullptr, err);
+}
+void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const int * slot_of,
+                              const int * nv, const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal,
+                              float inv_nvirt, float * feat_out, int * err, int grid, cudaStream_t st) {
+    FeatScale F{0.f, inv_alpha0, inv_rho0, inv_nreal, inv_nvirt};
+    k_mlp_forward<<<grid, kMlpNT, 0, st>>>(kMlpFromNodes, 0, params, norm, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                           N, slot_of, nv, cg, F, feat_out, err);
+}
+void launch_mlp_backward(long long n, const float * params, const float * norm, const float * feat,
+                         const float * pred, const float * target, const float * z1s, const float * h1s,
+                         const float * z2s, float * dz1, float * dz2, float * dy, float * sq_err, float * grad,
+                         cudaStream_t st) {
+    if (n <= 0) return;
+    const int g = int(std::min<long long>((n + 127) / 128, 152 * 8));
+    k_mlp_backward_rows<<<g, 128, 0, st>>>(n, params, norm, pred, target, z1s, z2s, dz1, dz2, dy, sq_err);
+    k_mlp_grad_weights<<<kMlpH, 128, 0, st>>>(n, norm, feat, h1s, z2s, dz1, dz2, dy, grad);
+}
+void launch_adam(float * p, const float * g, float * m, float * v, int count, float lr, float b1, float b2, float eps,
+                 float bc1, float bc2, cudaStream_t st) {
+    k_adam<<<(count + 255) / 256, 256, 0, st>>>(p, g, m, v, count, lr, b1, b2, eps, bc1, bc2);
+}
+template<int DIM>
+void launch_slot_of(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int * slot_of, int grid,
+                    cudaStream_t st) {
+    k_slot_of<DIM><<<grid, 256, 0, st>>>(L, B.list, B.count, B.seg_off, N.flag, slot_of);
+}
+void launch_mlp_targets(long long rows_max, const int * nv, const int * slot_of, const float * x, const float * prev,
+                        const float * ahat, const CgState * cg, float * target, cudaStream_t st) {
+    if (rows_max <= 0) return;
+    k_mlp_targets<<<int(std::min<long long>((rows_max + 255) / 256, 152 * 8)), 256, 0, st>>>(nv, slot_of, x, prev,
+                                                                                           ahat, cg, target);
+}
+template void launch_slot_of<2>(const Lattice &, const BrickArrays &, const NodeArrays &, int *, int, cudaStream_t);
+template void launch_slot_of<3>(const Lattice &, const BrickArrays &, const NodeArrays &, int *, int, cudaStream_t);
+
+}  // namespace swc

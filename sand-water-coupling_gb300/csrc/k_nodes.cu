@@ -349,11 +349,14 @@ __global__ void __launch_bounds__(kNT) k_zero_active(const int * __restrict__ bl
 // Zero for r2 >= 16 (outside the support); finite at r2 = 0 where it multiplies
 // a zero offset.
 __device__ __forceinline__ float grad_scale(float r2, float c1H) {
+    // -W'(r) / r_u with W' = c1 q (3q - 2) (q < 1/2) or -c1 (1 - q)^2 (q < 1), q = r_u / 4:
+    //   r_u < 2:       c1 (1/2 - 3 r_u / 16)
+    //   2 <= r_u < 4:  c1 (1 / r_u - 1/2 + r_u / 16)
     const float rinv = rsqrtf(fmaxf(r2, 1e-20f));
-    const float q    = 0.25f * r2 * rinv;
-    // -W'(r) / r_u with W' = c1 q (3q - 2) (q < 1/2) or -c1 (1 - q)^2 (q < 1), q = r_u / 4
-    const float t = 1.f - fminf(q, 1.f);
-    return q < 0.5f ? -0.25f * c1H * (3.f * q - 2.f) : c1H * t * t * rinv;
+    const float r    = r2 * rinv;
+    const float gin  = fmaf(-0.1875f, r, 0.5f);
+    const float gout = rinv + fmaf(0.0625f, r, -0.5f);
+    return c1H * (r2 < 4.f ? gin : (r2 < 16.f ? gout : 0.f));
 }
 
 // Global-memory path for particles outside the staged tile (clamped in from

@@ -71,6 +71,16 @@ struct swc_ctx {
     int *           plist = nullptr;
     int *           pcount = nullptr;
     unsigned char * bnear = nullptr;  // bricks within reach of boundary particles
+    // learned warm start / training-data logging
+    float * mlp_params = nullptr;  // SWC_MLP_PARAMS
+    float * mlp_norm   = nullptr;  // SWC_MLP_NORM
+    bool    mlp_ready  = false;
+    int *   mlp_err    = nullptr;
+    int *   slot_of    = nullptr;  // compact index -> slot
+    float * xprev      = nullptr;  // node-mapped previous pressure (brick layout)
+    float * feat_buf   = nullptr;  // logged features (reference order, 6 per node)
+    float * tgt_buf    = nullptr;  // logged targets
+    bool    features_valid = false;
     float *     pcomp = nullptr;
     int *       nv_prev = nullptr;
     int *       scan_tiles = nullptr;
@@ -155,6 +165,25 @@ void free_sort(SortScratch & S) {
     dfree(S.vel2);
     dfree(S.aux2);
     dfree(S.id2);
+}
+
+// Buffers of the learned warm start and of training-data logging (allocated on demand).
+int ensure_learn_buffers(swc_ctx * c) {
+    if (c->slot_of) return SWC_OK;
+    const size_t slots = size_t(c->L.nbricks) * (c->dim == 3 ? 512 : 256);
+    int rc;
+    if ((rc = dalloc(c, &c->mlp_err, 1)) || (rc = dalloc(c, &c->slot_of, size_t(c->L.ncells))) ||
+        (rc = dalloc(c, &c->xprev, slots)) || (rc = dalloc(c, &c->feat_buf, size_t(c->L.ncells) * 6)) ||
+        (rc = dalloc(c, &c->tgt_buf, size_t(c->L.ncells))))
+        return rc;
+    if (!c->N.nreal && (rc = dalloc(c, &c->N.nreal, slots))) return rc;
+    if (!c->N.nvirt && (rc = dalloc(c, &c->N.nvirt, slots))) return rc;
+    CK(cudaMemset(c->mlp_err, 0, sizeof(int)));
+    // the CG graphs captured the old NodeArrays (feature pointers): recapture
+    if (c->g1) cudaGraphExecDestroy(c->g1);
+    if (c->g8) cudaGraphExecDestroy(c->g8);
+    c->g1 = c->g8 = nullptr;
+    return SWC_OK;
 }
 
 void setup_phys(swc_ctx * c) {
@@ -250,19 +279,28 @@ int capture_graphs(swc_ctx * c) {
 }
 
 // CG solve from the warm start in N.x; fills stats.
-template<int DIM> int run_cg(swc_ctx * c, swc_stats * st) {
+// CG start from the current N.x; the device state is mirrored into hcg.
+template<int DIM> int cg_init_sync(swc_ctx * c) {
     const int * nv = c->B.seg_off + c->B.nseg;
-    if (!c->g1) {
-        CK(cudaStreamSynchronize(c->stream));
-        int rc = capture_graphs(c);
-        if (rc) return rc;
-    }
     launch_cg_init<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->opts.tolerance, c->opts.max_iterations, nv,
                         c->sgrid, c->stream);
     CK(cudaMemcpyAsync(&c->hcg->st, c->cg, sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&c->hcg->nv, nv, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&c->hcg->nbricks, c->B.count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    return SWC_OK;
+}
+
+template<int DIM> int run_cg(swc_ctx * c, swc_stats * st, bool initialized) {
+    if (!c->g1) {
+        CK(cudaStreamSynchronize(c->stream));
+        int rc = capture_graphs(c);
+        if (rc) return rc;
+    }
+    if (!initialized) {
+        int rc = cg_init_sync<DIM>(c);
+        if (rc) return rc;
+    }
     const double rr0 = c->hcg->st.rr0, bb = c->hcg->st.bb;
     int first        = c->opts.check_interval > 0 ? c->opts.check_interval : std::max(4, c->last_iters);
     while (!c->hcg->st.done) {
@@ -305,10 +343,56 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     mark(c, 3);
     run_generate<DIM>(c, true);
     mark(c, 4);
-    launch_warm_start<DIM>(c->L, c->B, c->N, c->opts.warm_start == SWC_WARM_LEARNED ? kWarmNode : c->opts.warm_start,
-                           c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
+    const int mode     = c->opts.warm_start;
+    const bool learned = mode == SWC_WARM_LEARNED && c->mlp_ready;
+    const bool logging = c->opts.keep_features != 0 && c->feat_buf;
+    const int * nv     = c->B.seg_off + c->B.nseg;
+    const size_t slots = size_t(c->L.nbricks) * BrickGeom<DIM>::BN;
+    int used           = mode == SWC_WARM_LEARNED ? SWC_WARM_NODE : mode;
+    bool initialized   = false;
+    if (learned || logging) {
+        // node-mapped previous pressure: the fallback, feature f4 and the target reference
+        launch_warm_start<DIM>(c->L, c->B, c->N, kWarmNode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
+        CK(cudaMemcpyAsync(c->xprev, c->N.x, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
+        launch_slot_of<DIM>(c->L, c->B, c->N, c->slot_of, c->grid, c->stream);
+        int rc = cg_init_sync<DIM>(c);  // |b|^2 for sD, initial residual of the node-mapped start
+        if (rc) return rc;
+        const double rr_node = c->hcg->st.rr0;
+        const float inv_a0 = float(1.0 / c->alpha0), inv_r0 = float(1.0 / c->rho0), inv_nr = 1.f / 32.f,
+                    inv_nv = DIM == 3 ? 1.f / 251.f : 1.f / 45.f;
+        if (logging)
+            launch_node_features(c->N, c->slot_of, nv, c->L.ncells, c->cg, inv_a0, inv_r0, inv_nr, inv_nv,
+                                 c->feat_buf, c->stream);
+        if (learned) {
+            launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->slot_of, nv, c->cg, inv_a0, inv_r0, inv_nr,
+                                     inv_nv, nullptr, c->mlp_err, c->num_sms * 2, c->stream);
+            if ((rc = cg_init_sync<DIM>(c))) return rc;
+            int err = 0;
+            CK(cudaMemcpy(&err, c->mlp_err, sizeof(int), cudaMemcpyDeviceToHost));
+            const double rr_mlp = c->hcg->st.rr0;
+            if (err || !(rr_mlp <= rr_node)) {
+                // the prediction starts from a larger residual (or failed): keep the node-mapped start
+                CK(cudaMemcpyAsync(c->N.x, c->xprev, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
+                if ((rc = cg_init_sync<DIM>(c))) return rc;
+                used = SWC_WARM_NODE;
+            } else used = SWC_WARM_LEARNED;
+            initialized = true;
+        } else if (mode == SWC_WARM_NODE || mode == SWC_WARM_LEARNED) {
+            initialized = true;
+        } else {
+            launch_warm_start<DIM>(c->L, c->B, c->N, mode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
+        }
+    } else {
+        launch_warm_start<DIM>(c->L, c->B, c->N, mode == SWC_WARM_LEARNED ? kWarmNode : mode, c->pcomp, c->nv_prev,
+                               nullptr, c->grid, c->stream);
+    }
     mark(c, 5);
-    int rc = run_cg<DIM>(c, st);
+    int rc = run_cg<DIM>(c, st, initialized);
+    if (st) st->warm_start_used = used;
+    if (logging && (rc == SWC_OK || rc == SWC_CG_NOT_CONVERGED)) {
+        launch_mlp_targets(c->L.ncells, nv, c->slot_of, c->N.x, c->xprev, c->N.ahat, c->cg, c->tgt_buf, c->stream);
+        c->features_valid = true;
+    }
     if (rc != SWC_OK && rc != SWC_CG_NOT_CONVERGED && rc != SWC_NAN_DETECTED) return rc;
     const int cg_status = rc;
     if (cg_status == SWC_NAN_DETECTED) {
@@ -328,7 +412,6 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     CK(cudaMemcpyAsync(c->nv_prev, c->B.seg_off + c->B.nseg, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
     mark(c, 8);
     if (st) {
-        st->warm_start_used = c->opts.warm_start == SWC_WARM_LEARNED ? SWC_WARM_NODE : c->opts.warm_start;
         st->n_particles     = c->n;
         st->n_boundary      = c->nb;
     }
@@ -531,8 +614,7 @@ int swc_create(const swc_scene * s, const swc_solver_opts * o, swc_ctx ** out) {
         (rc = dalloc(c, &c->N.q, slots)) || (rc = dalloc(c, &c->N.d0, slots)) || (rc = dalloc(c, &c->N.d1, slots)))
         return fail(rc);
     if (c->opts.keep_virtual_velocity && (rc = dalloc(c, &c->N.vbar, slots))) return fail(rc);
-    if (c->opts.keep_features && ((rc = dalloc(c, &c->N.nreal, slots)) || (rc = dalloc(c, &c->N.nvirt, slots))))
-        return fail(rc);
+    if (c->opts.keep_features && (rc = ensure_learn_buffers(c))) return fail(rc);
     c->B.nseg = (long long) L.ny * L.nz * L.bnx;
     if ((rc = dalloc(c, &c->B.flag, L.nbricks)) || (rc = dalloc(c, &c->B.flag_prev, L.nbricks)) ||
         (rc = dalloc(c, &c->B.list, L.nbricks)) || (rc = dalloc(c, &c->B.count, 1)) ||
@@ -599,6 +681,13 @@ void swc_destroy(swc_ctx * c) {
     dfree(c->N.vbar);
     dfree(c->N.nreal);
     dfree(c->N.nvirt);
+    dfree(c->mlp_params);
+    dfree(c->mlp_norm);
+    dfree(c->mlp_err);
+    dfree(c->slot_of);
+    dfree(c->xprev);
+    dfree(c->feat_buf);
+    dfree(c->tgt_buf);
     dfree(c->B.flag);
     dfree(c->B.flag_prev);
     dfree(c->B.list);
@@ -657,7 +746,7 @@ int swc_set_solver_opts(swc_ctx * c, const swc_solver_opts * o) {
         c->g1 = c->g8 = nullptr;
     }
     if (need_vbar && (rc = dalloc(c, &c->N.vbar, slots))) return rc;
-    if (need_feat && ((rc = dalloc(c, &c->N.nreal, slots)) || (rc = dalloc(c, &c->N.nvirt, slots)))) return rc;
+    if (need_feat && (rc = ensure_learn_buffers(c))) return rc;
     return SWC_OK;
 }
 
@@ -897,6 +986,37 @@ int swc_set_pressure(swc_ctx * c, const double * p, int64_t n) {
     if (n > 0) CK(cudaMemcpy(c->pcomp, f.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
     int ni = int(n);
     CK(cudaMemcpy(c->nv_prev, &ni, sizeof(int), cudaMemcpyHostToDevice));
+    return SWC_OK;
+}
+
+int swc_set_mlp(swc_ctx * c, const float * params, const float * norm) {
+    if (!valid_ctx(c) || !params || !norm) return SWC_BAD_ARG;
+    for (int k = 6; k < 12; k++)
+        if (!(norm[k] > 0)) return SWC_BAD_ARG;
+    if (!(norm[13] > 0)) return SWC_BAD_ARG;
+    int rc;
+    CK(cudaStreamSynchronize(c->stream));
+    if ((rc = ensure_learn_buffers(c))) return rc;
+    if (!c->mlp_params && ((rc = dalloc(c, &c->mlp_params, SWC_MLP_PARAMS)) || (rc = dalloc(c, &c->mlp_norm, SWC_MLP_NORM))))
+        return rc;
+    CK(cudaMemcpy(c->mlp_params, params, sizeof(float) * SWC_MLP_PARAMS, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->mlp_norm, norm, sizeof(float) * SWC_MLP_NORM, cudaMemcpyHostToDevice));
+    c->mlp_ready = true;
+    return SWC_OK;
+}
+
+int swc_get_features(swc_ctx * c, float * features, float * targets, int64_t capacity, int64_t * n) {
+    if (!valid_ctx(c) || !n) return SWC_BAD_ARG;
+    if (!c->features_valid) {
+        c->err = "no features logged (keep_features off or no projection yet)";
+        return SWC_BAD_ARG;
+    }
+    const int64_t nv = swc_num_virtual(c);
+    if (nv < 0) return SWC_CUDA_ERROR;
+    *n = nv;
+    if (capacity < nv) return SWC_BAD_ARG;
+    if (nv > 0 && features) CK(cudaMemcpy(features, c->feat_buf, sizeof(float) * 6 * nv, cudaMemcpyDeviceToHost));
+    if (nv > 0 && targets) CK(cudaMemcpy(targets, c->tgt_buf, sizeof(float) * nv, cudaMemcpyDeviceToHost));
     return SWC_OK;
 }
 

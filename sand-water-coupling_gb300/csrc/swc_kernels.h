@@ -147,4 +147,27 @@ template<int DIM>
 void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
                           CgState * cg, double * partials, double * out2, int sgrid, cudaStream_t st);
 
+// ---- k_mlp.cu (learned warm start) ----
+void launch_mlp_forward_array(long long n, const float * params, const float * norm, const float * feat, float * out,
+                              float * z1s, float * h1s, float * z2s, int * err, int grid, cudaStream_t st);
+void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const int * slot_of,
+                              const int * nv, const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal,
+                              float inv_nvirt, float * feat_out, int * err, int grid, cudaStream_t st);
+void launch_node_features(const NodeArrays & N, const int * slot_of, const int * nv, long long rows_max,
+                          const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal, float inv_nvirt,
+                          float * feat_out, cudaStream_t st);
+void launch_mlp_backward(long long n, const float * params, const float * norm, const float * feat,
+                         const float * pred, const float * target, const float * z1s, const float * h1s,
+                         const float * z2s, float * dz1, float * dz2, float * dy, float * sq_err, float * grad,
+                         cudaStream_t st);
+void launch_adam(float * p, const float * g, float * m, float * v, int count, float lr, float b1, float b2, float eps,
+                 float bc1, float bc2, cudaStream_t st);
+template<int DIM>
+void launch_slot_of(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int * slot_of, int grid,
+                    cudaStream_t st);
+void launch_mlp_targets(long long rows_max, const int * nv, const int * slot_of, const float * x, const float * prev,
+                        const float * ahat, const CgState * cg, float * target, cudaStream_t st);
+void launch_gather_rows(const float * src, const float * src_t, const int * idx, long long n, float * dst,
+                        float * dst_t, cudaStream_t st);
+
 }  // namespace swc

@@ -1,0 +1,233 @@
+// swc_learn.cu -- device-side training of the learned CG warm start and the
+// stateless forward / gradient helpers of the C ABI (include/swc.h).  The
+// dataset stays in device memory; every batch runs the tensor-core forward
+// (saving pre-activations), the FP32 backward and an Adam step.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/swc.h"
+#include "swc_kernels.h"
+
+using namespace swc;
+
+namespace {
+constexpr int kP = SWC_MLP_PARAMS, kN = SWC_MLP_NORM, kH = 64;
+}
+
+struct swc_trainer {
+    long long    cap = 0, n = 0;
+    int          batch = 4096;
+    cudaStream_t st = nullptr;
+    float *feat = nullptr, *tgt = nullptr;                       // dataset
+    float *params = nullptr, *norm = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr;
+    float *bfeat = nullptr, *btgt = nullptr, *pred = nullptr;    // batch
+    float *z1 = nullptr, *h1 = nullptr, *z2 = nullptr, *dz1 = nullptr, *dz2 = nullptr, *dy = nullptr, *sq = nullptr;
+    int *  idx = nullptr, *err = nullptr;
+    long long adam_t = 0;
+    int    grid = 152 * 2;
+};
+
+namespace {
+
+template<class T> bool talloc(T ** p, size_t count) {
+    return cudaMalloc(reinterpret_cast<void **>(p), sizeof(T) * std::max<size_t>(count, 1)) == cudaSuccess;
+}
+template<class T> void tfree(T *& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+int forward_batch(swc_trainer * t, const float * feat, long long n, float * out, bool save) {
+    launch_mlp_forward_array(n, t->params, t->norm, feat, out, save ? t->z1 : nullptr, save ? t->h1 : nullptr,
+                             save ? t->z2 : nullptr, t->err, t->grid, t->st);
+    return cudaGetLastError() == cudaSuccess ? SWC_OK : SWC_CUDA_ERROR;
+}
+
+int check_err(swc_trainer * t) {
+    int e = 0;
+    if (cudaMemcpyAsync(&e, t->err, sizeof(int), cudaMemcpyDeviceToHost, t->st) != cudaSuccess) return SWC_CUDA_ERROR;
+    if (cudaStreamSynchronize(t->st) != cudaSuccess) return SWC_CUDA_ERROR;
+    return e ? SWC_CUDA_ERROR : SWC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int swc_trainer_create(int64_t capacity, int32_t batch, swc_trainer ** out) {
+    if (!out || capacity <= 0 || batch <= 0) return SWC_BAD_ARG;
+    *out   = nullptr;
+    auto t = new swc_trainer();
+    t->cap   = capacity;
+    t->batch = batch;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    t->grid  = sms * 2;
+    const size_t B = size_t(batch);
+    bool ok = cudaStreamCreateWithFlags(&t->st, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && talloc(&t->feat, size_t(capacity) * 6) && talloc(&t->tgt, size_t(capacity)) && talloc(&t->params, kP) &&
+         talloc(&t->norm, kN) && talloc(&t->m, kP) && talloc(&t->v, kP) && talloc(&t->grad, kP) &&
+         talloc(&t->bfeat, B * 6) && talloc(&t->btgt, B) && talloc(&t->pred, B) && talloc(&t->z1, B * kH) &&
+         talloc(&t->h1, B * kH) && talloc(&t->z2, B * kH) && talloc(&t->dz1, B * kH) && talloc(&t->dz2, B * kH) &&
+         talloc(&t->dy, B) && talloc(&t->sq, B) && talloc(&t->idx, size_t(capacity)) && talloc(&t->err, 1);
+    if (!ok) {
+        swc_trainer_destroy(t);
+        return SWC_OUT_OF_MEMORY;
+    }
+    cudaMemsetAsync(t->m, 0, sizeof(float) * kP, t->st);
+    cudaMemsetAsync(t->v, 0, sizeof(float) * kP, t->st);
+    cudaMemsetAsync(t->err, 0, sizeof(int), t->st);
+    cudaStreamSynchronize(t->st);
+    *out = t;
+    return SWC_OK;
+}
+
+void swc_trainer_destroy(swc_trainer * t) {
+    if (!t) return;
+    if (t->st) cudaStreamSynchronize(t->st);
+    for (float ** p : {&t->feat, &t->tgt, &t->params, &t->norm, &t->m, &t->v, &t->grad, &t->bfeat, &t->btgt, &t->pred,
+                       &t->z1, &t->h1, &t->z2, &t->dz1, &t->dz2, &t->dy, &t->sq})
+        tfree(*p);
+    tfree(t->idx);
+    tfree(t->err);
+    if (t->st) cudaStreamDestroy(t->st);
+    delete t;
+}
+
+int swc_trainer_add(swc_trainer * t, const float * f, const float * y, int64_t n) {
+    if (!t || n < 0 || (n > 0 && (!f || !y))) return SWC_BAD_ARG;
+    if (t->n + n > t->cap) return SWC_BAD_ARG;
+    if (cudaMemcpyAsync(t->feat + t->n * 6, f, sizeof(float) * 6 * n, cudaMemcpyHostToDevice, t->st) != cudaSuccess ||
+        cudaMemcpyAsync(t->tgt + t->n, y, sizeof(float) * n, cudaMemcpyHostToDevice, t->st) != cudaSuccess)
+        return SWC_CUDA_ERROR;
+    cudaStreamSynchronize(t->st);
+    t->n += n;
+    return SWC_OK;
+}
+
+int swc_trainer_set_params(swc_trainer * t, const float * params, const float * norm) {
+    if (!t || !params || !norm) return SWC_BAD_ARG;
+    if (cudaMemcpy(t->params, params, sizeof(float) * kP, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(t->norm, norm, sizeof(float) * kN, cudaMemcpyHostToDevice) != cudaSuccess)
+        return SWC_CUDA_ERROR;
+    cudaMemset(t->m, 0, sizeof(float) * kP);
+    cudaMemset(t->v, 0, sizeof(float) * kP);
+    t->adam_t = 0;
+    return SWC_OK;
+}
+
+int swc_trainer_get_params(swc_trainer * t, float * params, float * norm) {
+    if (!t) return SWC_BAD_ARG;
+    if (params && cudaMemcpy(params, t->params, sizeof(float) * kP, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return SWC_CUDA_ERROR;
+    if (norm && cudaMemcpy(norm, t->norm, sizeof(float) * kN, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return SWC_CUDA_ERROR;
+    return SWC_OK;
+}
+
+int swc_trainer_fit(swc_trainer * t, int32_t epochs, float lr, uint64_t seed, float * epoch_loss) {
+    if (!t || epochs < 0 || t->n <= 0) return SWC_BAD_ARG;
+    std::mt19937_64 rng(seed);
+    std::vector<int> perm(t->n);
+    std::vector<float> pred_h, tgt_h(t->n), norm_h(kN);
+    cudaMemcpy(tgt_h.data(), t->tgt, sizeof(float) * t->n, cudaMemcpyDeviceToHost);
+    cudaMemcpy(norm_h.data(), t->norm, sizeof(float) * kN, cudaMemcpyDeviceToHost);
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    for (int e = 0; e < epochs; e++) {
+        std::iota(perm.begin(), perm.end(), 0);
+        std::shuffle(perm.begin(), perm.end(), rng);
+        if (cudaMemcpyAsync(t->idx, perm.data(), sizeof(int) * t->n, cudaMemcpyHostToDevice, t->st) != cudaSuccess)
+            return SWC_CUDA_ERROR;
+        for (long long b0 = 0; b0 < t->n; b0 += t->batch) {
+            const long long nb = std::min<long long>(t->batch, t->n - b0);
+            launch_gather_rows(t->feat, t->tgt, t->idx + b0, nb, t->bfeat, t->btgt, t->st);
+            int rc = forward_batch(t, t->bfeat, nb, t->pred, true);
+            if (rc) return rc;
+            launch_mlp_backward(nb, t->params, t->norm, t->bfeat, t->pred, t->btgt, t->z1, t->h1, t->z2, t->dz1,
+                                t->dz2, t->dy, t->sq, t->grad, t->st);
+            t->adam_t++;
+            const float bc1 = 1.f - std::pow(b1, float(t->adam_t)), bc2 = 1.f - std::pow(b2, float(t->adam_t));
+            launch_adam(t->params, t->grad, t->m, t->v, kP, lr, b1, b2, eps, bc1, bc2, t->st);
+        }
+        if (int rc = check_err(t)) return rc;
+        if (epoch_loss) {
+            // loss of the epoch's parameters over the whole dataset
+            pred_h.resize(t->n);
+            for (long long b0 = 0; b0 < t->n; b0 += t->batch) {
+                const long long nb = std::min<long long>(t->batch, t->n - b0);
+                int rc = forward_batch(t, t->feat + b0 * 6, nb, t->pred, false);
+                if (rc) return rc;
+                cudaMemcpyAsync(pred_h.data() + b0, t->pred, sizeof(float) * nb, cudaMemcpyDeviceToHost, t->st);
+            }
+            if (int rc = check_err(t)) return rc;
+            double s = 0;
+            for (long long i = 0; i < t->n; i++) {
+                const double d = (double(pred_h[i]) - tgt_h[i]) / norm_h[13];
+                s += d * d;
+            }
+            epoch_loss[e] = float(s / double(t->n));
+        }
+    }
+    return cudaGetLastError() == cudaSuccess ? SWC_OK : SWC_CUDA_ERROR;
+}
+
+int swc_mlp_forward(const float * params, const float * norm, const float * f, int64_t n, float * out) {
+    if (!params || !norm || n < 0 || (n > 0 && (!f || !out))) return SWC_BAD_ARG;
+    if (n == 0) return SWC_OK;
+    swc_trainer * t = nullptr;
+    int rc = swc_trainer_create(n, int32_t(std::min<int64_t>(n, 1 << 20)), &t);
+    if (rc) return rc;
+    if ((rc = swc_trainer_set_params(t, params, norm)) || (rc = swc_trainer_add(t, f, f, 0))) {
+        swc_trainer_destroy(t);
+        return rc;
+    }
+    cudaMemcpy(t->feat, f, sizeof(float) * 6 * n, cudaMemcpyHostToDevice);
+    std::vector<float> tmp;
+    for (long long b0 = 0; b0 < n && !rc; b0 += t->batch) {
+        const long long nb = std::min<long long>(t->batch, n - b0);
+        rc = forward_batch(t, t->feat + b0 * 6, nb, t->pred, false);
+        cudaMemcpyAsync(out + b0, t->pred, sizeof(float) * nb, cudaMemcpyDeviceToHost, t->st);
+    }
+    if (!rc) rc = check_err(t);
+    swc_trainer_destroy(t);
+    return rc;
+}
+
+int swc_mlp_gradient(const float * params, const float * norm, const float * f, const float * y, int64_t n,
+                     float * grad, float * loss) {
+    if (!params || !norm || !f || !y || !grad || n <= 0 || n > (1 << 24)) return SWC_BAD_ARG;
+    swc_trainer * t = nullptr;
+    int rc = swc_trainer_create(n, int32_t(n), &t);
+    if (rc) return rc;
+    if ((rc = swc_trainer_set_params(t, params, norm))) {
+        swc_trainer_destroy(t);
+        return rc;
+    }
+    cudaMemcpy(t->bfeat, f, sizeof(float) * 6 * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(t->btgt, y, sizeof(float) * n, cudaMemcpyHostToDevice);
+    rc = forward_batch(t, t->bfeat, n, t->pred, true);
+    if (!rc) {
+        launch_mlp_backward(n, t->params, t->norm, t->bfeat, t->pred, t->btgt, t->z1, t->h1, t->z2, t->dz1, t->dz2,
+                            t->dy, t->sq, t->grad, t->st);
+        rc = check_err(t);
+    }
+    if (!rc) {
+        cudaMemcpy(grad, t->grad, sizeof(float) * kP, cudaMemcpyDeviceToHost);
+        if (loss) {
+            std::vector<float> sq(n);
+            cudaMemcpy(sq.data(), t->sq, sizeof(float) * n, cudaMemcpyDeviceToHost);
+            double s = 0;
+            for (float e : sq) s += e;
+            *loss = float(s / double(n));
+        }
+    }
+    swc_trainer_destroy(t);
+    return rc;
+}
+
+}  // extern "C"

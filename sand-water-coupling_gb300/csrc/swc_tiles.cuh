@@ -103,6 +103,7 @@ __device__ __forceinline__ void load_tile4(const Lattice & L, const unsigned cha
     constexpr int SEGX = G::TX / 4;
     constexpr int NSEG = SEGX * G::TY * G::TZ;
     constexpr int NT   = RowGeom<DIM>::NT;
+#pragma unroll 4
     for (int t = threadIdx.x; t < NSEG; t += NT) {
         const int sx = t % SEGX, ty = (t / SEGX) % G::TY, tz = t / (SEGX * G::TY);
         const int x = bc.x * G::BX - G::HALO + 4 * sx, y = bc.y * G::BY + ty - G::HALO;

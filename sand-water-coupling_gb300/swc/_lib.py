@@ -106,6 +106,18 @@ SIGNATURES = {
     "swc_set_profiling": (C.c_int, [_P, C.c_int]),
     "swc_get_phase_times": (C.c_int, [_P, _D, C.c_int]),
     "swc_time_kernel": (C.c_int, [_P, C.c_int, C.c_int, _D]),
+    "swc_set_mlp": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "swc_get_features": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64, _I64]),
+    "swc_trainer_create": (C.c_int, [C.c_int64, C.c_int32, C.POINTER(_P)]),
+    "swc_trainer_destroy": (None, [_P]),
+    "swc_trainer_add": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64]),
+    "swc_trainer_set_params": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "swc_trainer_get_params": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "swc_trainer_fit": (C.c_int, [_P, C.c_int32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
+    "swc_mlp_forward": (C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64,
+                                  C.POINTER(C.c_float)]),
+    "swc_mlp_gradient": (C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                   C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "swc_host_alloc": (C.c_void_p, [C.c_size_t]),
     "swc_host_free": (None, [C.c_void_p]),
 }

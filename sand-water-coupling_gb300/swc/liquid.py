@@ -249,6 +249,23 @@ class DualParticleSphLiquid:
             ids[offsets[t]:offsets[t + 1]].sort()
         return counts, offsets, ids
 
+    def setMlp(self, params, norm):
+        """Network of the learned warm start (see swc.learn)."""
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        q = np.ascontiguousarray(norm, dtype=np.float32)
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        self._check(self.L.swc_set_mlp(self.h, fp(p), fp(q)), "swc_set_mlp")
+
+    def features(self):
+        """(features[n, 6], targets[n]) logged by the last projection (keep_features=True)."""
+        n = self.numVirtual()
+        f = np.empty((max(n, 1), 6), dtype=np.float32)
+        t = np.empty(max(n, 1), dtype=np.float32)
+        got = C.c_int64()
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        self._check(self.L.swc_get_features(self.h, fp(f), fp(t), max(n, 1), C.byref(got)), "swc_get_features")
+        return f[: got.value], t[: got.value]
+
     def setProfiling(self, on=True):
         self._check(self.L.swc_set_profiling(self.h, 1 if on else 0), "swc_set_profiling")
 

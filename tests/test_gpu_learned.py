@@ -1,0 +1,90 @@
+"""GPU checks of the learned CG warm start: the tensor-core forward pass and the
+training kernels against the FP64 MLP oracle, and what the trained network
+gains (or not) over the plain node-mapped warm start, with the same solution."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as M
+from swc import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _synthetic(n=5000, seed=0):
+    rng = np.random.default_rng(seed)
+    f = rng.normal(size=(n, 6)).astype(np.float32)
+    t = (np.tanh(f[:, 0]) + 0.5 * f[:, 4] - 0.2 * f[:, 1] * f[:, 5]).astype(np.float32)
+    norm = np.concatenate([f.mean(0), f.std(0), [t.mean(), t.std()]]).astype(np.float32)
+    return f, t, norm
+
+
+def test_tensor_core_forward_matches_oracle(swc_mod):
+    from swc import learn
+
+    f, t, norm = _synthetic(1000)
+    p = learn.init_params(4)
+    p[-1] = 0.3
+    gpu = learn.forward(p, norm, f)
+    ref16 = M.forward(p.astype(np.float64), norm, f, bf16=True)
+    ref64 = M.forward(p.astype(np.float64), norm, f, bf16=False)
+    scale = np.abs(ref64).max()
+    # BF16 operands, FP32 accumulation: against the BF16-emulating oracle ~1e-3, against FP64 ~1e-2
+    assert np.abs(gpu - ref16).max() <= 2e-3 * scale, np.abs(gpu - ref16).max() / scale
+    assert np.abs(gpu - ref64).max() <= 3e-2 * scale
+
+
+def test_gradient_matches_oracle(swc_mod):
+    from swc import learn
+
+    f, t, norm = _synthetic(777, seed=1)
+    p = learn.init_params(5)
+    g, loss = learn.gradient(p, norm, f, t)
+    lo, go = M.loss_and_grad(p.astype(np.float64), norm, f, t)
+    assert loss == pytest.approx(lo, rel=2e-2)
+    rel = np.linalg.norm(g - go) / np.linalg.norm(go)
+    assert rel < 3e-2, rel
+
+
+def test_training_reduces_loss(swc_mod):
+    from swc import learn
+
+    f, t, _ = _synthetic(20000, seed=2)
+    p, q, loss = learn.train(f, t, epochs=8, lr=3e-3, batch=2048, seed=3)
+    assert loss[-1] < 0.3 * loss[0], loss
+    pred = learn.forward(p, q, f)
+    assert np.mean((pred - t) ** 2) / np.var(t) < 0.3
+
+
+def test_learned_warm_start_end_to_end(swc_mod):
+    """Train on logged data of one seed, evaluate on a held-out seed: same
+    solution as the plain solver, and the iteration counts of both."""
+    from swc import learn
+
+    train_scene = scenes.projection_block_3d(n=24, seed=11, steps=12)
+    f, t = learn.collect(train_scene, steps=12)
+    assert f.shape[1] == 6 and f.shape[0] == t.shape[0] > 1000
+    assert np.all(np.isfinite(f)) and np.all(np.isfinite(t))
+    p, q, loss = learn.train(f, t, epochs=20, lr=1e-3, batch=4096, seed=0)
+    assert loss[-1] <= loss[0]
+
+    test_scene = scenes.projection_block_3d(n=24, seed=99).rounded_to_float32()
+    out = {}
+    for mode in ("node", "learned"):
+        liq = swc_mod.DualParticleSphLiquid(test_scene, warm_start=mode, compute_true_residual=True)
+        if mode == "learned":
+            liq.setMlp(p, q)
+        liq.initialize()
+        its, used = [], []
+        for _ in range(8):
+            st = liq.advance(test_scene.dt)
+            assert st["status"] == 0 and st["true_rel_residual"] < 5 * test_scene.tolerance
+            its.append(st["cg_iterations"])
+            used.append(st["warm_start_used"])
+        out[mode] = (liq.getParticles()[1], np.array(its), used)
+        liq.close()
+    v_node, it_node, _ = out["node"]
+    v_learn, it_learn, used = out["learned"]
+    assert np.linalg.norm(v_learn - v_node) / np.linalg.norm(v_node) < 1e-4
+    # the residual-based fallback never starts from a worse residual than the plain solver
+    assert it_learn[1:].mean() <= it_node[1:].mean() + 1.0
+    print(f"\nCG iterations  node-mapped: {it_node.tolist()}  learned: {it_learn.tolist()}  used: {used}")
