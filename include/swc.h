@@ -207,6 +207,21 @@ int  swc_trainer_fit(swc_trainer * tr, int32_t epochs, float lr, uint64_t seed, 
 int swc_mlp_forward(const float * params, const float * norm, const float * features, int64_t n, float * out);
 int swc_mlp_gradient(const float * params, const float * norm, const float * features, const float * targets,
                      int64_t n, float * grad, float * loss);
+/* Same loss gradient as swc_mlp_gradient, for callers that cannot allocate
+ * device memory when they need it (frameworks that plan all device memory up
+ * front, callers under a fixed memory budget).  No counterpart in the reference.
+ * It allocates nothing: all pointers are device pointers supplied by the caller
+ * (params[SWC_MLP_PARAMS], norm[SWC_MLP_NORM], features[n][6], targets[n],
+ * grad[SWC_MLP_PARAMS] and loss[1] out), work is queued on `stream` (NULL: the
+ * default stream) and its scratch lives in fixed device arrays for at most
+ * SWC_MLP_NOALLOC_MAX_ROWS rows (about 2.7 MB per device, held until the process
+ * exits).  n above the limit returns SWC_BAD_ARG.  The first call on a device
+ * resolves the arrays' device addresses, so make it before any stream capture.
+ * All calls share the arrays: calls that overlap on the GPU race.  A failure of
+ * the tensor-core pass shows as loss = NaN. */
+#define SWC_MLP_NOALLOC_MAX_ROWS 2048
+int swc_mlp_gradient_noalloc(const float * params, const float * norm, const float * features,
+                             const float * targets, int64_t n, float * grad, float * loss, void * stream);
 
 /* Pinned host memory helpers for callers that stream state every step. */
 void * swc_host_alloc(size_t bytes);

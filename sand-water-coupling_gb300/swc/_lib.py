@@ -118,6 +118,8 @@ SIGNATURES = {
                                   C.POINTER(C.c_float)]),
     "swc_mlp_gradient": (C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                    C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "swc_mlp_gradient_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                           C.c_void_p, C.c_void_p]),
     "swc_host_alloc": (C.c_void_p, [C.c_size_t]),
     "swc_host_free": (None, [C.c_void_p]),
 }
