@@ -235,20 +235,21 @@ def run_gpu_arm(args):
     # dominant kernels timed live (CUDA events on the library stream)
     hbm, peak_kind = peaks()
     kern = {}
-    for which, name in ((0, "cg_spmv"), (1, "cg_update"), (2, "virtual_gather"), (3, "pressure_gradient"),
-                        (4, "density"), (5, "forces")):
+    for which, name in ((6, "cg_direction"), (0, "cg_spmv"), (1, "cg_update"), (2, "virtual_gather"),
+                        (3, "pressure_gradient"), (4, "density"), (5, "forces")):
         kern[name] = liq.timeKernel(which, 20)
     n, nb = scene.n_particles, scene.n_boundary
     # algorithmic bytes per launch (each array touched once per pass)
     alg = {
-        "cg_spmv": 24 * nv,  # reads r, d_prev, V, alpha_hat; writes d, q (FP32)
+        "cg_direction": 20 * nv,  # reads d, r, V; writes d, u = V d
+        "cg_spmv": 16 * nv,  # reads u (halo tiles from L2), d, alpha_hat; writes q (FP32)
         "cg_update": 24 * nv,  # reads x, r, d, q; writes x, r
         "virtual_gather": 32 * (n + nb) + 16 * nv,  # particle pos/vel once; V, D, rho, flag out
         "pressure_gradient": 32 * n + 8 * nv + 48 * nb,  # pos, vel r/w; V, p; boundary pos/vel/nrm
         "density": 16 * n + 4 * n + 4 * n,
         "forces": 32 * n + 16 * n,
     }
-    cg_ms = kern["cg_spmv"] + kern["cg_update"]
+    cg_ms = kern["cg_direction"] + kern["cg_spmv"] + kern["cg_update"]
     dominant = max(("cg_spmv", "virtual_gather", "pressure_gradient"),
                    key=lambda k: kern[k] * (np.mean(iters) if k == "cg_spmv" else 1))
     ach = alg[dominant] / (kern[dominant] / 1e3) / 1e9

@@ -164,7 +164,7 @@ int swc_set_profiling(swc_ctx * ctx, int on);
 int swc_get_phase_times(swc_ctx * ctx, double * ms, int n);
 /* Times `reps` back-to-back launches of one kernel on the live state with CUDA
  * events (0: CG SpMV, 1: CG update, 2: virtual gather, 3: pressure gradient,
- * 4: density, 5: forces); writes the mean ms per launch. */
+ * 4: density, 5: forces, 6: CG direction update); writes the mean ms per launch. */
 int swc_time_kernel(swc_ctx * ctx, int which, int reps, double * mean_ms);
 
 /* ---- Learned CG warm start (no counterpart in the reference) -------------

@@ -11,10 +11,11 @@
 //
 // Kernels: one CTA per brick (row-stencil kernels: one thread per brick x-row,
 // 8 outputs along x in 3D), the V-weighted halo tile staged in shared memory
-// with 16-byte loads.  The search-direction update d_i = r_i + beta d_{i-1} is
-// fused into the SpMV (recomputed for the halo), and x/r are updated in one
-// streaming pass; dot products use exact FP32 products summed in float-float
-// below the warp and FP64 above, reduced deterministically.
+// with 16-byte copies.  A CG iteration is three kernels: the direction update
+// d = r + beta d with u = V d (streaming), the SpMV q = A d reading u tiles by
+// double-buffered cp.async, and the x/r update; dot products use exact FP32
+// products summed in float-float below the warp and FP64 above, reduced
+// deterministically.
 #include "swc_kernels.h"
 #include "swc_tiles.cuh"
 
@@ -174,7 +175,7 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_cg_init(Lattice L, const int * 
                 }
                 const float4 r4 = make_float4(r[0], r[1], r[2], r[3]);
                 st4(N.r, base + 4 * k, r4);
-                st4(N.d0, base + 4 * k, r4);
+                st4(N.d, base + 4 * k, r4);
             }
         }
     }
@@ -204,8 +205,78 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_cg_init(Lattice L, const int * 
     }
 }
 
-// Iteration part 1: d_i = r_i + beta d_{i-1} (i > 0; recomputed for the halo),
-// q = A d_i, pq = d_i . q.
+// Iteration part 0: d_i = r_i + beta d_{i-1} (i > 0) and u = V d_i (16-byte streaming).
+template<int DIM>
+__global__ void __launch_bounds__(kUT) k_cg_direction(const int * __restrict__ blist, const int * __restrict__ bcount,
+                                                      NodeArrays N, const CgState * __restrict__ cg) {
+    using G = BrickGeom<DIM>;
+    constexpr int Q = G::BN / 4;
+    if (cg->done) return;
+    const int it     = cg->iter;
+    const float beta = it == 0 ? 0.f : float(cg->rr / cg->rr_prev);
+    const long long total = (long long) (*bcount) * Q;
+    for (long long i = blockIdx.x * (long long) kUT + threadIdx.x; i < total; i += (long long) gridDim.x * kUT) {
+        const long long s = (long long) blist[i / Q] * G::BN + 4 * (i % Q);
+        float4 d          = ld4(N.d, s);
+        if (it > 0) {
+            d = fma4(beta, d, ld4(N.r, s));
+            st4(N.d, s, d);
+        }
+        st4(N.u, s, mul4(ld4(N.V, s), d));
+    }
+}
+
+__device__ __forceinline__ void cp_async16(float * smem_dst, const float * gsrc, bool valid) {
+    const unsigned sa = unsigned(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(sa), "l"(gsrc), "r"(valid ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Neighbour-brick table of brick b: tab[(k+1)*9 + (j+1)*3 + (i+1)] = id of brick
+// (bx+i, by+j, bz+k) when it exists and is active, else -1.
+template<int DIM>
+__device__ __forceinline__ void neighbour_table(const Lattice & L, const unsigned char * __restrict__ bflag, int b,
+                                                int * tab) {
+    const int t = threadIdx.x;
+    if (t < 27) {
+        const int3 bc = brick_coords(L, b);
+        const int i = t % 3 - 1, j = (t / 3) % 3 - 1, k = t / 9 - 1;
+        const int x = bc.x + i, y = bc.y + j, z = bc.z + k;
+        int id = -1;
+        if (x >= 0 && x < L.bnx && y >= 0 && y < L.bny && z >= 0 && z < L.bnz && (DIM == 3 || k == 0)) {
+            const int nb = x + L.bnx * (y + L.bny * z);
+            if (bflag[nb]) id = nb;
+        }
+        tab[t] = id;
+    }
+}
+
+// Asynchronous copy of the u halo tile of a brick (16-byte segments, zero-filled
+// outside the active set).
+template<int DIM>
+__device__ __forceinline__ void prefetch_u_tile(const int * tab, const float * __restrict__ u, float * tile) {
+    using G            = BrickGeom<DIM>;
+    constexpr int SEGX = G::TX / 4;
+    constexpr int NSEG = SEGX * G::TY * G::TZ;
+    constexpr int NT   = RowGeom<DIM>::NT;
+#pragma unroll 4
+    for (int t = threadIdx.x; t < NSEG; t += NT) {
+        const int sx = t % SEGX, ty = (t / SEGX) % G::TY, tz = t / (SEGX * G::TY);
+        const int tx = 4 * sx;
+        // neighbour offset (-1, 0, 1) and local coordinate along each axis
+        const int oi = (tx - G::HALO + G::BX) / G::BX - 1, oj = (ty - G::HALO + G::BY) / G::BY - 1;
+        const int ok = DIM == 3 ? (tz - G::HALO + G::BZ) / G::BZ - 1 : 0;
+        const int lx = tx - G::HALO - G::BX * oi, ly = ty - G::HALO - G::BY * oj;
+        const int lz = DIM == 3 ? tz - G::HALO - G::BZ * ok : 0;
+        const int nb = tab[(ok + 1) * 9 + (oj + 1) * 3 + (oi + 1)];
+        const long long s = (long long) (nb < 0 ? 0 : nb) * G::BN + lx + G::BX * (ly + G::BY * lz);
+        cp_async16(tile + tx + G::PX * (ty + G::TY * tz), u + s, nb >= 0);
+    }
+}
+
+// Iteration part 1: q = A d_i and pq = d_i . q.  The u = V d tile of the next
+// brick is copied asynchronously while the current one is computed.
 template<int DIM>
 __global__ void __launch_bounds__(KG<DIM>::BT) k_cg_spmv(Lattice L, const int * __restrict__ blist,
                                                          const int * __restrict__ bcount,
@@ -213,51 +284,49 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_cg_spmv(Lattice L, const int * 
                                                          Stencil S, CgState * cg, double * __restrict__ partials) {
     using G = BrickGeom<DIM>;
     constexpr int BT = KG<DIM>::BT;
-    __shared__ __align__(16) float tile[G::TILE];
+    __shared__ __align__(16) float tile[2][G::TILE];
+    __shared__ int tab[2][27];
     __shared__ double red[BT / 32 + 1];
     __shared__ int last;
     if (cg->done) return;
-    const int it      = cg->iter;
-    const float beta  = it == 0 ? 0.f : float(cg->rr / cg->rr_prev);
-    const float * dpv = (it & 1) ? N.d0 : N.d1;  // d_{i-1}
-    float * dcur      = (it & 1) ? N.d1 : N.d0;  // d_i
-    const int nb      = *bcount;
+    const int nb = *bcount;
     const int t = threadIdx.x, ly = t % G::BY, lz = t / G::BY;
     FF pq{0.f, 0.f};
-    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
-        const int b   = blist[bi];
-        const int3 bc = brick_coords(L, b);
+    if (blockIdx.x < nb) neighbour_table<DIM>(L, bflag, blist[blockIdx.x], tab[0]);
+    __syncthreads();
+    if (blockIdx.x < nb) prefetch_u_tile<DIM>(tab[0], N.u, tile[0]);
+    cp_async_commit();
+    int k = 0;
+    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x, k ^= 1) {
+        const int nxt = bi + gridDim.x;
+        if (nxt < nb) neighbour_table<DIM>(L, bflag, blist[nxt], tab[k ^ 1]);
         __syncthreads();
-        if (it == 0)
-            load_tile4<DIM>(L, bflag, bc, tile, [&](long long s) { return mul4(ld4(N.V, s), ld4(dcur, s)); });
-        else
-            load_tile4<DIM>(L, bflag, bc, tile,
-                            [&](long long s) { return mul4(ld4(N.V, s), fma4(beta, ld4(dpv, s), ld4(N.r, s))); });
+        if (nxt < nb) prefetch_u_tile<DIM>(tab[k ^ 1], N.u, tile[k ^ 1]);
+        cp_async_commit();
+        cp_async_wait1();  // the current tile has landed
         __syncthreads();
+        const int b = blist[bi];
         if (t < KG<DIM>::NT) {
             float acc[G::BX];
-            stencil_row<DIM>(tile, ly, lz, S, acc);
+            stencil_row<DIM>(tile[k], ly, lz, S, acc);
             const long long base = row_base<DIM>(b, ly, lz);
 #pragma unroll
-            for (int k = 0; k < G::BX / 4; k++) {
-                float4 dv;
-                if (it == 0) dv = ld4(dcur, base + 4 * k);
-                else {
-                    dv = fma4(beta, ld4(dpv, base + 4 * k), ld4(N.r, base + 4 * k));
-                    st4(dcur, base + 4 * k, dv);
-                }
-                const float4 a = ld4(N.ahat, base + 4 * k);
-                const uchar4 f = *reinterpret_cast<const uchar4 *>(N.flag + base + 4 * k);
+            for (int kk = 0; kk < G::BX / 4; kk++) {
+                const float4 dv = ld4(N.d, base + 4 * kk);
+                const float4 a  = ld4(N.ahat, base + 4 * kk);
+                const uchar4 f  = *reinterpret_cast<const uchar4 *>(N.flag + base + 4 * kk);
                 float q[4];
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    q[j] = compb(f, j) ? fmaf(comp(a, j), comp(dv, j), acc[4 * k + j]) : comp(dv, j);
+                    q[j] = compb(f, j) ? fmaf(comp(a, j), comp(dv, j), acc[4 * kk + j]) : comp(dv, j);
                     ff_add_prod(pq, comp(dv, j), q[j]);
                 }
-                st4(N.q, base + 4 * k, make_float4(q[0], q[1], q[2], q[3]));
+                st4(N.q, base + 4 * kk, make_float4(q[0], q[1], q[2], q[3]));
             }
         }
+        __syncthreads();  // tile[k] and tab[k] are refilled two iterations later
     }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     double part[1] = {block_sum_ff<BT>(pq, red)};
     double tot[1];
     if (grid_reduce<BT, 1>(part, partials, &cg->ticket[1], tot, red, &last) && threadIdx.x == 0) {
@@ -278,12 +347,11 @@ __global__ void __launch_bounds__(kUT) k_cg_update(const int * __restrict__ blis
     if (cg->done) return;
     const int it      = cg->iter;
     const float alpha = float(cg->rr / cg->pq);
-    const float * dc  = (it & 1) ? N.d1 : N.d0;
     const long long total = (long long) (*bcount) * Q;
     FF rr{0.f, 0.f};
     for (long long i = blockIdx.x * (long long) kUT + threadIdx.x; i < total; i += (long long) gridDim.x * kUT) {
         const long long s = (long long) blist[i / Q] * G::BN + 4 * (i % Q);
-        const float4 d = ld4(dc, s), q = ld4(N.q, s);
+        const float4 d = ld4(N.d, s), q = ld4(N.q, s);
         float4 x = ld4(N.x, s), r = ld4(N.r, s);
         x = fma4(alpha, d, x);
         r = fma4(-alpha, q, r);
@@ -381,8 +449,13 @@ void launch_cg_update(const BrickArrays & B, const NodeArrays & N, CgState * cg,
     k_cg_update<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N, cg, partials);
 }
 template<int DIM>
+void launch_cg_direction(const BrickArrays & B, const NodeArrays & N, const CgState * cg, int ugrid, cudaStream_t st) {
+    k_cg_direction<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N, cg);
+}
+template<int DIM>
 void launch_cg_iteration(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
                          CgState * cg, double * partials, int sgrid, int ugrid, cudaStream_t st) {
+    launch_cg_direction<DIM>(B, N, cg, ugrid, st);
     launch_cg_spmv<DIM>(L, B, N, S, cg, partials, sgrid, st);
     launch_cg_update<DIM>(B, N, cg, partials, ugrid, st);
 }
@@ -402,6 +475,7 @@ void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeAr
     template void launch_cg_spmv<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,         \
                                     CgState *, double *, int, cudaStream_t);                                           \
     template void launch_cg_update<D>(const BrickArrays &, const NodeArrays &, CgState *, double *, int, cudaStream_t); \
+    template void launch_cg_direction<D>(const BrickArrays &, const NodeArrays &, const CgState *, int, cudaStream_t); \
     template void launch_cg_iteration<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,    \
                                          CgState *, double *, int, int, cudaStream_t);                                 \
     template void launch_true_residual<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,   \

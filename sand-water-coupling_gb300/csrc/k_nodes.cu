@@ -49,6 +49,43 @@ __global__ void __launch_bounds__(1024) k_brick_list(const unsigned char * __res
     if (threadIdx.x == 0) *count = carry;
 }
 
+// Contributions of one particle / boundary particle at squared distance r2 and
+// offset (dx, dy, dz) = x_I - x_j to the 11 sums of a node.
+struct NodeSums {
+    float wsum, rhoI, VI, ux, uy, uz, bw, dvg, gx, gy, gz;
+    int   cnt;
+};
+
+template<bool REAL>
+__device__ __forceinline__ void add_pair(NodeSums & a, const Phys & P, float r2, float dx, float dy, float dz, float4 p,
+                                         float4 u) {
+    const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
+    const float r    = r2 * rinv;
+    const float q    = r * P.inv_h;
+    const float t    = 1.f - q;
+    const bool inner = q < 0.5f;
+    const float w    = inner ? P.c0h * (6.f * q * q * (q - 1.f) + 1.f) : P.c0h * 2.f * t * t * t;
+    // -W'_h(r)/r: -c1 (3q - 2)/h inside, c1 (1 - q)^2 / r outside (zero offset at r = 0)
+    const float gsc = inner ? -P.c1h * P.inv_h * (3.f * q - 2.f) : P.c1h * t * t * rinv;
+    if (REAL) {
+        a.wsum += w;
+        a.rhoI += kW(r, P.inv_H, P.c0H);
+        a.VI += p.w * p.w * w;
+        a.cnt++;
+    }
+    const float mw = u.w * w;
+    a.ux += mw * u.x;
+    a.uy += mw * u.y;
+    a.uz += mw * u.z;
+    a.bw += p.w * w;
+    const float c  = gsc * p.w;
+    const float cx = c * dx, cy = c * dy, cz = c * dz;
+    a.dvg += u.x * cx + u.y * cy + u.z * cz;
+    a.gx += cx;
+    a.gy += cy;
+    a.gz += cz;
+}
+
 // ---------------------------------------------------------------------------
 // Fused virtual gather.  For every node of an active brick, one pass over the
 // real and boundary particles within h gives (reference VirtualParticle.cpp):
@@ -59,107 +96,118 @@ __global__ void __launch_bounds__(1024) k_brick_list(const unsigned char * __res
 //   D_I     = sum V_j v_j.g_j - vbar_I . sum V_j g_j - kappa max(rho_I - rho0, 0)/rho0   (:172-201)
 // with g_j = -W'_h(r) (x_I - x_j)/r  and sums over real + boundary particles
 // (boundary: m_b, rho_b, V_b) except weight, rho_I and V_I (real only).
+// Each thread handles NX consecutive nodes along x: the candidate particles of a
+// cell row are loaded once for all of them and tested by exact distance, so
+// every node still sums exactly its neighbours within h, in cell-row order.
 // ---------------------------------------------------------------------------
 template<int DIM>
-__global__ void __launch_bounds__(kNT, 3) k_node_gather(Lattice L, Phys P, const int * __restrict__ blist,
-                                                     const int * __restrict__ bcount, NodeArrays N,
-                                                     const float4 * __restrict__ pos, const float4 * __restrict__ vel,
-                                                     const int * __restrict__ cellStart,
-                                                     const float4 * __restrict__ bpos,
-                                                     const float4 * __restrict__ bvel,
-                                                     const int * __restrict__ bcellStart,
-                                                     const unsigned char * __restrict__ bnear) {
-    using G      = BrickGeom<DIM>;
+__global__ void __launch_bounds__(128, 4) k_node_gather(Lattice L, Phys P, const int * __restrict__ blist,
+                                                       const int * __restrict__ bcount, NodeArrays N,
+                                                       const float4 * __restrict__ pos, const float4 * __restrict__ vel,
+                                                       const int * __restrict__ cellStart,
+                                                       const float4 * __restrict__ bpos,
+                                                       const float4 * __restrict__ bvel,
+                                                       const int * __restrict__ bcellStart,
+                                                       const unsigned char * __restrict__ bnear) {
+    using G          = BrickGeom<DIM>;
+    constexpr int NX = 4;
+    constexpr int XS = G::BX / NX;  // thread columns per brick row
+    constexpr int TPB = G::BN / NX;
     const int nb = *bcount;
     for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
-        const int b    = blist[bi];
-        const int3 bc  = brick_coords(L, b);
+        const int b     = blist[bi];
+        const int3 bc   = brick_coords(L, b);
         const int npass = bnear[b] ? 2 : 1;  // boundary particles only near walls
-        for (int l = threadIdx.x; l < G::BN; l += kNT) {
-            const int lx = l % G::BX, ly = (l / G::BX) % G::BY, lz = l / (G::BX * G::BY);
-            const int x = bc.x * G::BX + lx, y = bc.y * G::BY + ly, z = bc.z * G::BZ + lz;
-            const long long s = (long long) b * G::BN + l;
-            if (x >= L.nx || y >= L.ny || (DIM == 3 && z >= L.nz)) {
-                N.flag[s] = 0;
-                N.V[s] = 0.f;
-                N.D[s] = 0.f;
-                N.rho[s] = 0.f;
-                if (N.nreal) N.nreal[s] = 0;
-                if (N.vbar) N.vbar[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-                continue;
-            }
-            const float xn = L.ox + x * L.dx, yn = L.oy + y * L.dx, zn = DIM == 3 ? L.oz + z * L.dx : 0.f;
-            float wsum = 0.f, rhoI = 0.f, VI = 0.f, ux = 0.f, uy = 0.f, uz = 0.f, bw = 0.f, dvg = 0.f, gx = 0.f,
-                  gy = 0.f, gz = 0.f;
-            int cnt = 0;
-            const int cx0 = max(x + P.cell_lo, 0), cx1 = min(x + P.cell_hi, L.nx - 1);
+        for (int l4 = threadIdx.x; l4 < TPB; l4 += blockDim.x) {
+            const int lx0 = (l4 % XS) * NX, ly = (l4 / XS) % G::BY, lz = l4 / (XS * G::BY);
+            const int x0 = bc.x * G::BX + lx0, y = bc.y * G::BY + ly, z = bc.z * G::BZ + lz;
+            const long long s0 = (long long) b * G::BN + lx0 + G::BX * (ly + G::BY * lz);
+            const bool row_in = y < L.ny && (DIM == 2 || z < L.nz);
+            NodeSums a[NX];
+#pragma unroll
+            for (int n = 0; n < NX; n++) a[n] = NodeSums{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0};
+            const float xn0 = L.ox + x0 * L.dx, yn = L.oy + y * L.dx, zn = DIM == 3 ? L.oz + z * L.dx : 0.f;
+            const int cxa = max(x0 + P.cell_lo, 0), cxb = min(x0 + NX - 1 + P.cell_hi, L.nx - 1);
             const int cy0 = max(y + P.cell_lo, 0), cy1 = min(y + P.cell_hi, L.ny - 1);
             const int cz0 = DIM == 3 ? max(z + P.cell_lo, 0) : 0, cz1 = DIM == 3 ? min(z + P.cell_hi, L.nz - 1) : 0;
+            if (row_in) {
 #pragma unroll 1
-            for (int pass = 0; pass < npass; pass++) {
-                const int * cs   = pass == 0 ? cellStart : bcellStart;
-                const float4 * X = pass == 0 ? pos : bpos;
-                const float4 * U = pass == 0 ? vel : bvel;
-                for (int cz = cz0; cz <= cz1; cz++)
-                    for (int cy = cy0; cy <= cy1; cy++) {
-                        const long long row = (long long) L.nx * (cy + (long long) L.ny * cz);
-                        const int jb = cs[row + cx0], je = cs[row + cx1 + 1];
-                        for (int j = jb; j < je; j++) {
-                            const float4 p = X[j];
-                            const float dx = xn - p.x, dy = yn - p.y, dz = zn - p.z;
-                            const float r2 = dx * dx + dy * dy + dz * dz;
-                            if (r2 >= P.h2) continue;
-                            const float4 u = U[j];
-                            float w, gsc;
-                            kernel_and_grad(r2, P.inv_h, P.c0h, P.c1h, w, gsc);
-                            if (pass == 0) {
-                                wsum += w;
-                                rhoI += kW(r2 * rsqrtf(fmaxf(r2, 1e-30f)), P.inv_H, P.c0H);
-                                VI += p.w * p.w * w;
-                                cnt++;
+                for (int pass = 0; pass < npass; pass++) {
+                    const int * cs   = pass == 0 ? cellStart : bcellStart;
+                    const float4 * X = pass == 0 ? pos : bpos;
+                    const float4 * U = pass == 0 ? vel : bvel;
+                    for (int cz = cz0; cz <= cz1; cz++)
+                        for (int cy = cy0; cy <= cy1; cy++) {
+                            const long long row = (long long) L.nx * (cy + (long long) L.ny * cz);
+                            const int jb = cs[row + cxa], je = cs[row + cxb + 1];
+                            for (int j = jb; j < je; j++) {
+                                const float4 p  = X[j];
+                                const float dy  = yn - p.y, dz = zn - p.z;
+                                const float ryz = dy * dy + dz * dz;
+                                if (ryz >= P.h2) continue;
+                                float4 u;
+                                bool have_u = false;
+#pragma unroll
+                                for (int n = 0; n < NX; n++) {
+                                    const float dx = xn0 + n * L.dx - p.x;
+                                    const float r2 = dx * dx + ryz;
+                                    if (r2 >= P.h2) continue;
+                                    if (!have_u) {
+                                        u      = U[j];
+                                        have_u = true;
+                                    }
+                                    if (pass == 0) add_pair<true>(a[n], P, r2, dx, dy, dz, p, u);
+                                    else add_pair<false>(a[n], P, r2, dx, dy, dz, p, u);
+                                }
                             }
-                            const float mw = u.w * w;
-                            ux += mw * u.x;
-                            uy += mw * u.y;
-                            uz += mw * u.z;
-                            bw += p.w * w;
-                            // g_j = -W'_h(r) (x_I - x_j) / r, zero at r = 0 (W'(0) = 0)
-                            const float c  = gsc * p.w;
-                            const float cx = c * dx, cy_ = c * dy, cz_ = c * dz;
-                            dvg += u.x * cx + u.y * cy_ + u.z * cz_;
-                            gx += cx;
-                            gy += cy_;
-                            gz += cz_;
                         }
-                    }
+                }
             }
-            bool active = wsum > 1e-6f;
-            if (fabsf(wsum - 1e-6f) <= 1e-9f) {
-                // borderline: redo the weight in FP64 from the same float positions
-                const double xd = L.ox_d + x * L.dx_d, yd = L.oy_d + y * L.dx_d, zd = DIM == 3 ? L.oz_d + z * L.dx_d : 0.0;
-                double ws = 0;
-                for (int cz = cz0; cz <= cz1; cz++)
-                    for (int cy = cy0; cy <= cy1; cy++) {
-                        const long long row = (long long) L.nx * (cy + (long long) L.ny * cz);
-                        for (int j = cellStart[row + cx0]; j < cellStart[row + cx1 + 1]; j++) {
-                            const float4 p = pos[j];
-                            const double dx = xd - p.x, dy = yd - p.y, dz = DIM == 3 ? zd - p.z : 0.0;
-                            const double r2 = dx * dx + dy * dy + dz * dz;
-                            if (r2 < P.h_d * P.h_d) ws += kW_d(sqrt(r2), P.inv_h_d, P.c0h_d);
+#pragma unroll
+            for (int n = 0; n < NX; n++) {
+                const int x       = x0 + n;
+                const long long s = s0 + n;
+                if (!row_in || x >= L.nx) {
+                    N.flag[s] = 0;
+                    N.V[s]    = 0.f;
+                    N.D[s]    = 0.f;
+                    N.rho[s]  = 0.f;
+                    if (N.nreal) N.nreal[s] = 0;
+                    if (N.vbar) N.vbar[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    continue;
+                }
+                const NodeSums & A = a[n];
+                bool active        = A.wsum > 1e-6f;
+                if (fabsf(A.wsum - 1e-6f) <= 1e-9f) {
+                    // borderline: redo the weight in FP64 from the same float positions
+                    const double xd = L.ox_d + x * L.dx_d, yd = L.oy_d + y * L.dx_d,
+                                 zd = DIM == 3 ? L.oz_d + z * L.dx_d : 0.0;
+                    const int cx0 = max(x + P.cell_lo, 0), cx1 = min(x + P.cell_hi, L.nx - 1);
+                    double ws = 0;
+                    for (int cz = cz0; cz <= cz1; cz++)
+                        for (int cy = cy0; cy <= cy1; cy++) {
+                            const long long row = (long long) L.nx * (cy + (long long) L.ny * cz);
+                            for (int j = cellStart[row + cx0]; j < cellStart[row + cx1 + 1]; j++) {
+                                const float4 p  = pos[j];
+                                const double ex = xd - p.x, ey = yd - p.y, ez = DIM == 3 ? zd - p.z : 0.0;
+                                const double r2 = ex * ex + ey * ey + ez * ez;
+                                if (r2 < P.h_d * P.h_d) ws += kW_d(sqrt(r2), P.inv_h_d, P.c0h_d);
+                            }
                         }
-                    }
-                active = ws > 1e-6;
+                    active = ws > 1e-6;
+                }
+                const float den = A.bw + 1e-6f;
+                const float vbx = A.ux / den, vby = A.uy / den, vbz = A.uz / den;
+                const float rho = A.rhoI * P.mass;
+                const float Dv  = A.dvg - (vbx * A.gx + vby * A.gy + vbz * A.gz) -
+                                 P.kappa * fmaxf(rho - P.rho0, 0.f) / P.rho0;
+                N.flag[s] = active ? 1 : 0;
+                N.V[s]    = active ? A.VI : 0.f;
+                N.D[s]    = active ? Dv : 0.f;
+                N.rho[s]  = active ? rho : 0.f;
+                if (N.nreal) N.nreal[s] = (unsigned short) min(A.cnt, 65535);
+                if (N.vbar) N.vbar[s] = make_float4(vbx, vby, vbz, 0.f);
             }
-            const float den = bw + 1e-6f;
-            const float vbx = ux / den, vby = uy / den, vbz = uz / den;
-            const float rho = rhoI * P.mass;
-            const float Dv  = dvg - (vbx * gx + vby * gy + vbz * gz) - P.kappa * fmaxf(rho - P.rho0, 0.f) / P.rho0;
-            N.flag[s] = active ? 1 : 0;
-            N.V[s]    = active ? VI : 0.f;
-            N.D[s]    = active ? Dv : 0.f;
-            N.rho[s]  = active ? rho : 0.f;
-            if (N.nreal) N.nreal[s] = (unsigned short) min(cnt, 65535);
-            if (N.vbar) N.vbar[s] = make_float4(vbx, vby, vbz, 0.f);
         }
     }
 }
@@ -501,7 +549,7 @@ void launch_node_gather(const Lattice & L, const Phys & P, const BrickArrays & B
                         const float4 * pos, const float4 * vel, const int * cellStart, const float4 * bpos,
                         const float4 * bvel, const int * bcellStart, const unsigned char * bnear, int grid,
                         cudaStream_t st) {
-    k_node_gather<DIM><<<grid, kNT, 0, st>>>(L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel, bcellStart,
+    k_node_gather<DIM><<<grid * 2, 128, 0, st>>>(L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel, bcellStart,
                                              bnear);
 }
 

@@ -611,7 +611,7 @@ int swc_create(const swc_scene * s, const swc_solver_opts * o, swc_ctx ** out) {
     if ((rc = dalloc(c, &c->N.flag, slots)) || (rc = dalloc(c, &c->N.flag_prev, slots)) ||
         (rc = dalloc(c, &c->N.V, slots)) || (rc = dalloc(c, &c->N.D, slots)) || (rc = dalloc(c, &c->N.rho, slots)) ||
         (rc = dalloc(c, &c->N.ahat, slots)) || (rc = dalloc(c, &c->N.x, slots)) || (rc = dalloc(c, &c->N.r, slots)) ||
-        (rc = dalloc(c, &c->N.q, slots)) || (rc = dalloc(c, &c->N.d0, slots)) || (rc = dalloc(c, &c->N.d1, slots)))
+        (rc = dalloc(c, &c->N.q, slots)) || (rc = dalloc(c, &c->N.d, slots)) || (rc = dalloc(c, &c->N.u, slots)))
         return fail(rc);
     if (c->opts.keep_virtual_velocity && (rc = dalloc(c, &c->N.vbar, slots))) return fail(rc);
     if (c->opts.keep_features && (rc = ensure_learn_buffers(c))) return fail(rc);
@@ -676,8 +676,8 @@ void swc_destroy(swc_ctx * c) {
     dfree(c->N.x);
     dfree(c->N.r);
     dfree(c->N.q);
-    dfree(c->N.d0);
-    dfree(c->N.d1);
+    dfree(c->N.d);
+    dfree(c->N.u);
     dfree(c->N.vbar);
     dfree(c->N.nreal);
     dfree(c->N.nvirt);
@@ -1138,6 +1138,7 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
             switch (which) {
             case 0: launch_cg_spmv<3>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->sgrid, c->stream); break;
             case 1: launch_cg_update<3>(c->B, c->N, c->cg, c->partials, c->grid, c->stream); break;
+            case 6: launch_cg_direction<3>(c->B, c->N, c->cg, c->grid, c->stream); break;
             case 2:
                 launch_node_gather<3>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel,
                                       c->bcellStart, c->bnear, c->grid, c->stream);

@@ -33,8 +33,8 @@ struct NodeArrays {
     float *         x         = nullptr;  // pressure (CG solution), kept across steps
     float *         r         = nullptr;
     float *         q         = nullptr;
-    float *         d0        = nullptr;
-    float *         d1        = nullptr;
+    float *         d         = nullptr;  // CG search direction
+    float *         u         = nullptr;  // V * d, the halo source of the SpMV
     float4 *        vbar      = nullptr;  // optional: virtual velocity (debug / export)
     unsigned short * nreal    = nullptr;  // optional: real neighbours within h
     unsigned short * nvirt    = nullptr;  // optional: active virtual neighbours within H (self included)
@@ -129,6 +129,8 @@ void launch_cg_init(const Lattice & L, const BrickArrays & B, const NodeArrays &
 template<int DIM>
 void launch_cg_iteration(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
                          CgState * cg, double * partials, int sgrid, int ugrid, cudaStream_t st);
+template<int DIM>
+void launch_cg_direction(const BrickArrays & B, const NodeArrays & N, const CgState * cg, int ugrid, cudaStream_t st);
 template<int DIM>
 void launch_cg_spmv(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
                     double * partials, int sgrid, cudaStream_t st);
