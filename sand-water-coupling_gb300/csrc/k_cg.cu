@@ -257,21 +257,22 @@ __device__ __forceinline__ void neighbour_table(const Lattice & L, const unsigne
 template<int DIM>
 __device__ __forceinline__ void prefetch_u_tile(const int * tab, const float * __restrict__ u, float * tile) {
     using G            = BrickGeom<DIM>;
-    constexpr int SEGX = G::TX / 4;
-    constexpr int NSEG = SEGX * G::TY * G::TZ;
+    using T            = SpmvTile<DIM>;
+    constexpr int SEGX = T::TX / 4;
+    constexpr int NSEG = SEGX * T::TY * T::TZ;
     constexpr int NT   = RowGeom<DIM>::NT;
 #pragma unroll 4
     for (int t = threadIdx.x; t < NSEG; t += NT) {
-        const int sx = t % SEGX, ty = (t / SEGX) % G::TY, tz = t / (SEGX * G::TY);
+        const int sx = t % SEGX, ty = (t / SEGX) % T::TY, tz = t / (SEGX * T::TY);
         const int tx = 4 * sx;
         // neighbour offset (-1, 0, 1) and local coordinate along each axis
-        const int oi = (tx - G::HALO + G::BX) / G::BX - 1, oj = (ty - G::HALO + G::BY) / G::BY - 1;
-        const int ok = DIM == 3 ? (tz - G::HALO + G::BZ) / G::BZ - 1 : 0;
-        const int lx = tx - G::HALO - G::BX * oi, ly = ty - G::HALO - G::BY * oj;
-        const int lz = DIM == 3 ? tz - G::HALO - G::BZ * ok : 0;
+        const int oi = (tx - T::HX + G::BX) / G::BX - 1, oj = (ty - T::HY + G::BY) / G::BY - 1;
+        const int ok = DIM == 3 ? (tz - T::HZ + G::BZ) / G::BZ - 1 : 0;
+        const int lx = tx - T::HX - G::BX * oi, ly = ty - T::HY - G::BY * oj;
+        const int lz = DIM == 3 ? tz - T::HZ - G::BZ * ok : 0;
         const int nb = tab[(ok + 1) * 9 + (oj + 1) * 3 + (oi + 1)];
         const long long s = (long long) (nb < 0 ? 0 : nb) * G::BN + lx + G::BX * (ly + G::BY * lz);
-        cp_async16(tile + tx + G::PX * (ty + G::TY * tz), u + s, nb >= 0);
+        cp_async16(tile + tx + T::PX * (ty + T::TY * tz), u + s, nb >= 0);
     }
 }
 
@@ -283,8 +284,9 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_cg_spmv(Lattice L, const int * 
                                                          const unsigned char * __restrict__ bflag, NodeArrays N,
                                                          Stencil S, CgState * cg, double * __restrict__ partials) {
     using G = BrickGeom<DIM>;
+    using T = SpmvTile<DIM>;
     constexpr int BT = KG<DIM>::BT;
-    __shared__ __align__(16) float tile[2][G::TILE];
+    __shared__ __align__(16) float tile[2][T::TILE];
     __shared__ int tab[2][27];
     __shared__ double red[BT / 32 + 1];
     __shared__ int last;
@@ -308,7 +310,7 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_cg_spmv(Lattice L, const int * 
         const int b = blist[bi];
         if (t < KG<DIM>::NT) {
             float acc[G::BX];
-            stencil_row<DIM>(tile[k], ly, lz, S, acc);
+            stencil_row_t<DIM, T::PX, T::TY, T::HY, T::HZ>(tile[k], ly, lz, S, acc);
             const long long base = row_base<DIM>(b, ly, lz);
 #pragma unroll
             for (int kk = 0; kk < G::BX / 4; kk++) {
@@ -443,6 +445,11 @@ void launch_cg_spmv(const Lattice & L, const BrickArrays & B, const NodeArrays &
                     double * partials, int sgrid, cudaStream_t st) {
     k_cg_spmv<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, B.list, B.count, B.flag, N, S, cg, partials);
 }
+template<int DIM> int cg_spmv_blocks_per_sm() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cg_spmv<DIM>, KG<DIM>::BT, 0) != cudaSuccess) n = 1;
+    return n > 0 ? n : 1;
+}
 template<int DIM>
 void launch_cg_update(const BrickArrays & B, const NodeArrays & N, CgState * cg, double * partials, int ugrid,
                       cudaStream_t st) {
@@ -479,7 +486,8 @@ void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeAr
     template void launch_cg_iteration<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,    \
                                          CgState *, double *, int, int, cudaStream_t);                                 \
     template void launch_true_residual<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,   \
-                                          CgState *, double *, double *, int, cudaStream_t);
+                                          CgState *, double *, double *, int, cudaStream_t);                           \
+    template int cg_spmv_blocks_per_sm<D>();
 SWC_INST(2)
 SWC_INST(3)
 #undef SWC_INST

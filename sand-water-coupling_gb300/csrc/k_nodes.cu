@@ -49,41 +49,69 @@ __global__ void __launch_bounds__(1024) k_brick_list(const unsigned char * __res
     if (threadIdx.x == 0) *count = carry;
 }
 
-// Contributions of one particle / boundary particle at squared distance r2 and
-// offset (dx, dy, dz) = x_I - x_j to the 11 sums of a node.
-struct NodeSums {
-    float wsum, rhoI, VI, ux, uy, uz, bw, dvg, gx, gy, gz;
-    int   cnt;
+// Sums of two x-adjacent nodes, packed as FP32x2 (.x: node n, .y: node n + 1).
+// The kernel scale factors are applied once at the end:
+//   W_h = 2 c0h w,  -W'_h / r = c1h g,  W_H = c0H wH  (see pair_add).
+struct NodeSums2 {
+    float2 wsum, rhoI, VI, cnt, ux, uy, uz, bw, dvg, gx, gy, gz;
 };
 
-template<bool REAL>
-__device__ __forceinline__ void add_pair(NodeSums & a, const Phys & P, float r2, float dx, float dy, float dz, float4 p,
-                                         float4 u) {
-    const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
-    const float r    = r2 * rinv;
-    const float q    = r * P.inv_h;
-    const float t    = 1.f - q;
-    const bool inner = q < 0.5f;
-    const float w    = inner ? P.c0h * (6.f * q * q * (q - 1.f) + 1.f) : P.c0h * 2.f * t * t * t;
-    // -W'_h(r)/r: -c1 (3q - 2)/h inside, c1 (1 - q)^2 / r outside (zero offset at r = 0)
-    const float gsc = inner ? -P.c1h * P.inv_h * (3.f * q - 2.f) : P.c1h * t * t * rinv;
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 max02(float2 a) { return make_float2(fmaxf(a.x, 0.f), fmaxf(a.y, 0.f)); }
+
+// Contributions of one particle (position / volume p, velocity / m-over-rho u)
+// to two nodes at x offsets dxx = x_I - x_j (dy, dz shared, ryz = dy^2 + dz^2).
+// With q = r / h, a = max(1 - q, 0) and b = max(a - 1/2, 0) the cubic spline is
+//   W_h = c0h (2 a^3 - 8 b^3) = 2 c0h w,   w = a^3 - 4 b^3,
+//   -W'_h(r) / r = (6 c0h / h) (a^2 - 4 b^2) / r = c1h g,
+// (q < 1/2: 2 - 3q over h; 1/2 <= q < 1: (1 - q)^2 / r; 0 beyond), and a node
+// only takes particles with r^2 < h^2 (a is zeroed otherwise).  rho_I uses W_H
+// truncated at h: for H >= 2h (FAST_H) only its inner branch
+// wH = 1 + 6 x^2 (x - 1), x = r / H, is reached; otherwise wH = 2 aH^3 - 8 bH^3.
+template<bool REAL, bool FAST_H>
+__device__ __forceinline__ void pair_add(NodeSums2 & s, const Phys & P, float2 dxx, float dy, float dz, float ryz,
+                                         float4 p, float4 u) {
+    const float2 r2 = fma2(dxx, dxx, f2(ryz));
+    const bool m0 = r2.x < P.h2, m1 = r2.y < P.h2;
+    const float2 ri = make_float2(rsqrt_n(fmaxf(r2.x, 1e-30f)), rsqrt_n(fmaxf(r2.y, 1e-30f)));
+    const float2 q  = mul2(mul2(r2, ri), f2(P.inv_h));
+    float2 a        = max02(fma2(q, f2(-1.f), f2(1.f)));
+    a               = make_float2(m0 ? a.x : 0.f, m1 ? a.y : 0.f);
+    const float2 b  = max02(add2(a, f2(-0.5f)));
+    const float2 a2 = mul2(a, a), b2 = mul2(b, b);
+    const float2 w  = fma2(mul2(b2, b), f2(-4.f), mul2(a2, a));
+    const float2 g  = mul2(fma2(b2, f2(-4.f), a2), ri);
     if (REAL) {
-        a.wsum += w;
-        a.rhoI += kW(r, P.inv_H, P.c0H);
-        a.VI += p.w * p.w * w;
-        a.cnt++;
+        float2 wH;
+        const float2 x = mul2(q, f2(P.h * P.inv_H));
+        if (FAST_H) {
+            wH = fma2(mul2(mul2(x, x), add2(x, f2(-1.f))), f2(6.f), f2(1.f));
+            wH = make_float2(m0 ? wH.x : 0.f, m1 ? wH.y : 0.f);
+        } else {
+            float2 aH = max02(fma2(x, f2(-1.f), f2(1.f)));
+            aH        = make_float2(m0 ? aH.x : 0.f, m1 ? aH.y : 0.f);
+            const float2 bH = max02(add2(aH, f2(-0.5f)));
+            wH = fma2(mul2(mul2(bH, bH), bH), f2(-8.f), mul2(mul2(mul2(aH, aH), aH), f2(2.f)));
+        }
+        s.wsum = add2(s.wsum, w);
+        s.rhoI = add2(s.rhoI, wH);
+        s.VI   = fma2(f2(p.w * p.w), w, s.VI);
+        s.cnt  = add2(s.cnt, make_float2(m0 ? 1.f : 0.f, m1 ? 1.f : 0.f));
     }
-    const float mw = u.w * w;
-    a.ux += mw * u.x;
-    a.uy += mw * u.y;
-    a.uz += mw * u.z;
-    a.bw += p.w * w;
-    const float c  = gsc * p.w;
-    const float cx = c * dx, cy = c * dy, cz = c * dz;
-    a.dvg += u.x * cx + u.y * cy + u.z * cz;
-    a.gx += cx;
-    a.gy += cy;
-    a.gz += cz;
+    const float2 mw = mul2(f2(u.w), w);
+    s.ux  = fma2(f2(u.x), mw, s.ux);
+    s.uy  = fma2(f2(u.y), mw, s.uy);
+    s.uz  = fma2(f2(u.z), mw, s.uz);
+    s.bw  = fma2(f2(p.w), w, s.bw);
+    const float2 c  = mul2(f2(p.w), g);
+    const float2 ud = fma2(f2(u.x), dxx, f2(fmaf(u.y, dy, u.z * dz)));
+    s.dvg = fma2(c, ud, s.dvg);
+    s.gx  = fma2(c, dxx, s.gx);
+    s.gy  = fma2(c, f2(dy), s.gy);
+    s.gz  = fma2(c, f2(dz), s.gz);
 }
 
 // ---------------------------------------------------------------------------
@@ -100,21 +128,22 @@ __device__ __forceinline__ void add_pair(NodeSums & a, const Phys & P, float r2,
 // cell row are loaded once for all of them and tested by exact distance, so
 // every node still sums exactly its neighbours within h, in cell-row order.
 // ---------------------------------------------------------------------------
-template<int DIM>
-__global__ void __launch_bounds__(128, 4) k_node_gather(Lattice L, Phys P, const int * __restrict__ blist,
-                                                       const int * __restrict__ bcount, NodeArrays N,
-                                                       const float4 * __restrict__ pos, const float4 * __restrict__ vel,
-                                                       const int * __restrict__ cellStart,
-                                                       const float4 * __restrict__ bpos,
-                                                       const float4 * __restrict__ bvel,
-                                                       const int * __restrict__ bcellStart,
-                                                       const unsigned char * __restrict__ bnear) {
+template<int DIM, bool FAST_H>
+__global__ void __launch_bounds__(128) k_node_gather(Lattice L, Phys P, const int * __restrict__ blist,
+                                                    const int * __restrict__ bcount, NodeArrays N,
+                                                    const float4 * __restrict__ pos, const float4 * __restrict__ vel,
+                                                    const int * __restrict__ cellStart,
+                                                    const float4 * __restrict__ bpos,
+                                                    const float4 * __restrict__ bvel,
+                                                    const int * __restrict__ bcellStart,
+                                                    const unsigned char * __restrict__ bnear, int * queue) {
     using G          = BrickGeom<DIM>;
-    constexpr int NX = 4;
+    constexpr int NX = 2;
     constexpr int XS = G::BX / NX;  // thread columns per brick row
     constexpr int TPB = G::BN / NX;
+    __shared__ int slot;
     const int nb = *bcount;
-    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
+    for (int bi = queue_take(queue, &slot); bi < nb; bi = queue_take(queue, &slot)) {
         const int b     = blist[bi];
         const int3 bc   = brick_coords(L, b);
         const int npass = bnear[b] ? 2 : 1;  // boundary particles only near walls
@@ -123,10 +152,10 @@ __global__ void __launch_bounds__(128, 4) k_node_gather(Lattice L, Phys P, const
             const int x0 = bc.x * G::BX + lx0, y = bc.y * G::BY + ly, z = bc.z * G::BZ + lz;
             const long long s0 = (long long) b * G::BN + lx0 + G::BX * (ly + G::BY * lz);
             const bool row_in = y < L.ny && (DIM == 2 || z < L.nz);
-            NodeSums a[NX];
-#pragma unroll
-            for (int n = 0; n < NX; n++) a[n] = NodeSums{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0};
+            NodeSums2 a;
+            a.wsum = a.rhoI = a.VI = a.cnt = a.ux = a.uy = a.uz = a.bw = a.dvg = a.gx = a.gy = a.gz = f2(0.f);
             const float xn0 = L.ox + x0 * L.dx, yn = L.oy + y * L.dx, zn = DIM == 3 ? L.oz + z * L.dx : 0.f;
+            const float2 xn = make_float2(xn0, L.ox + (x0 + 1) * L.dx);
             const int cxa = max(x0 + P.cell_lo, 0), cxb = min(x0 + NX - 1 + P.cell_hi, L.nx - 1);
             const int cy0 = max(y + P.cell_lo, 0), cy1 = min(y + P.cell_hi, L.ny - 1);
             const int cz0 = DIM == 3 ? max(z + P.cell_lo, 0) : 0, cz1 = DIM == 3 ? min(z + P.cell_hi, L.nz - 1) : 0;
@@ -145,20 +174,10 @@ __global__ void __launch_bounds__(128, 4) k_node_gather(Lattice L, Phys P, const
                                 const float dy  = yn - p.y, dz = zn - p.z;
                                 const float ryz = dy * dy + dz * dz;
                                 if (ryz >= P.h2) continue;
-                                float4 u;
-                                bool have_u = false;
-#pragma unroll
-                                for (int n = 0; n < NX; n++) {
-                                    const float dx = xn0 + n * L.dx - p.x;
-                                    const float r2 = dx * dx + ryz;
-                                    if (r2 >= P.h2) continue;
-                                    if (!have_u) {
-                                        u      = U[j];
-                                        have_u = true;
-                                    }
-                                    if (pass == 0) add_pair<true>(a[n], P, r2, dx, dy, dz, p, u);
-                                    else add_pair<false>(a[n], P, r2, dx, dy, dz, p, u);
-                                }
+                                const float4 u    = U[j];
+                                const float2 dxx = add2(xn, f2(-p.x));
+                                if (pass == 0) pair_add<true, FAST_H>(a, P, dxx, dy, dz, ryz, p, u);
+                                else pair_add<false, FAST_H>(a, P, dxx, dy, dz, ryz, p, u);
                             }
                         }
                 }
@@ -176,9 +195,12 @@ __global__ void __launch_bounds__(128, 4) k_node_gather(Lattice L, Phys P, const
                     if (N.vbar) N.vbar[s] = make_float4(0.f, 0.f, 0.f, 0.f);
                     continue;
                 }
-                const NodeSums & A = a[n];
-                bool active        = A.wsum > 1e-6f;
-                if (fabsf(A.wsum - 1e-6f) <= 1e-9f) {
+                auto pick = [n](float2 v) { return n == 0 ? v.x : v.y; };
+                const float w2 = 2.f * P.c0h;
+                const float wsum = w2 * pick(a.wsum);
+                const float gx = P.c1h * pick(a.gx), gy = P.c1h * pick(a.gy), gz = P.c1h * pick(a.gz);
+                bool active = wsum > 1e-6f;
+                if (fabsf(wsum - 1e-6f) <= 1e-9f) {
                     // borderline: redo the weight in FP64 from the same float positions
                     const double xd = L.ox_d + x * L.dx_d, yd = L.oy_d + y * L.dx_d,
                                  zd = DIM == 3 ? L.oz_d + z * L.dx_d : 0.0;
@@ -196,20 +218,21 @@ __global__ void __launch_bounds__(128, 4) k_node_gather(Lattice L, Phys P, const
                         }
                     active = ws > 1e-6;
                 }
-                const float den = A.bw + 1e-6f;
-                const float vbx = A.ux / den, vby = A.uy / den, vbz = A.uz / den;
-                const float rho = A.rhoI * P.mass;
-                const float Dv  = A.dvg - (vbx * A.gx + vby * A.gy + vbz * A.gz) -
+                const float den = w2 * pick(a.bw) + 1e-6f;
+                const float vbx = w2 * pick(a.ux) / den, vby = w2 * pick(a.uy) / den, vbz = w2 * pick(a.uz) / den;
+                const float rho = pick(a.rhoI) * (P.mass * P.c0H);
+                const float Dv  = P.c1h * pick(a.dvg) - (vbx * gx + vby * gy + vbz * gz) -
                                  P.kappa * fmaxf(rho - P.rho0, 0.f) / P.rho0;
                 N.flag[s] = active ? 1 : 0;
-                N.V[s]    = active ? A.VI : 0.f;
+                N.V[s]    = active ? w2 * pick(a.VI) : 0.f;
                 N.D[s]    = active ? Dv : 0.f;
                 N.rho[s]  = active ? rho : 0.f;
-                if (N.nreal) N.nreal[s] = (unsigned short) min(A.cnt, 65535);
+                if (N.nreal) N.nreal[s] = (unsigned short) min(int(pick(a.cnt)), 65535);
                 if (N.vbar) N.vbar[s] = make_float4(vbx, vby, vbz, 0.f);
             }
         }
     }
+    queue_finish(queue);
 }
 
 // ---------------------------------------------------------------------------
@@ -400,11 +423,46 @@ __device__ __forceinline__ float grad_scale(float r2, float c1H) {
     // -W'(r) / r_u with W' = c1 q (3q - 2) (q < 1/2) or -c1 (1 - q)^2 (q < 1), q = r_u / 4:
     //   r_u < 2:       c1 (1/2 - 3 r_u / 16)
     //   2 <= r_u < 4:  c1 (1 / r_u - 1/2 + r_u / 16)
-    const float rinv = rsqrtf(fmaxf(r2, 1e-20f));
+    const float rinv = rsqrt_n(fmaxf(r2, 1e-20f));
     const float r    = r2 * rinv;
     const float gin  = fmaf(-0.1875f, r, 0.5f);
     const float gout = rinv + fmaf(0.0625f, r, -0.5f);
     return c1H * (r2 < 4.f ? gin : (r2 < 16.f ? gout : 0.f));
+}
+
+// Two nodes of a row at x offsets dx (packed FP32x2 arithmetic): returns
+// w = u (a^2 - 4 b^2) / r with a = 1 - r/4, b = max(a - 1/2, 0) and r clamped
+// to 4, i.e. the grad_scale factor above without c1H (r < 2: 1/2 - 3r/16;
+// 2 <= r < 4: 1/r - 1/2 + r/16; 0 beyond), and adds w dx to sx.
+// e = dyz2 + 1e-30 keeps r2 > 0 (a node at the particle adds 0).
+__device__ __forceinline__ float2 grad_w2(float2 dx, float e, float2 u, float2 & sx) {
+    float2 r2       = __ffma2_rn(dx, dx, make_float2(e, e));
+    r2              = make_float2(fminf(r2.x, 16.f), fminf(r2.y, 16.f));
+    const float2 ri = make_float2(rsqrt_n(r2.x), rsqrt_n(r2.y));
+    const float2 r  = __fmul2_rn(r2, ri);
+    const float2 a  = __ffma2_rn(r, make_float2(-0.25f, -0.25f), make_float2(1.f, 1.f));
+    float2 b        = __fadd2_rn(a, make_float2(-0.5f, -0.5f));
+    b               = make_float2(fmaxf(b.x, 0.f), fmaxf(b.y, 0.f));
+    float2 g        = __fmul2_rn(a, a);
+    g               = __ffma2_rn(__fmul2_rn(b, b), make_float2(-4.f, -4.f), g);
+    const float2 w  = __fmul2_rn(__fmul2_rn(g, ri), u);
+    sx              = __ffma2_rn(w, dx, sx);
+    return w;
+}
+
+// One row of the 8-node x-window (node k at dx = fx - k, fx in [3, 4); dxp
+// holds the pairs (2,3) (4,5) (1,6) (0,7)): sx += sum w dx, returns the pair
+// sums of w.  Nodes 0 and 7 have |dx| >= 3 and lie outside H when dyz2 >= 7;
+// nodes 1 and 6 have |dx| >= 2 and lie outside when dyz2 >= 12.
+__device__ __forceinline__ float2 gradient_row(const float * trow, const float2 (&dxp)[4], float dyz2, float2 & sx) {
+    const float e = dyz2 + 1e-30f;
+    float2 sg     = grad_w2(dxp[0], e, make_float2(trow[2], trow[3]), sx);
+    sg            = __fadd2_rn(sg, grad_w2(dxp[1], e, make_float2(trow[4], trow[5]), sx));
+    if (dyz2 < 12.f) {
+        sg = __fadd2_rn(sg, grad_w2(dxp[2], e, make_float2(trow[1], trow[6]), sx));
+        if (dyz2 < 7.f) sg = __fadd2_rn(sg, grad_w2(dxp[3], e, make_float2(trow[0], trow[7]), sx));
+    }
+    return sg;
 }
 
 // Global-memory path for particles outside the staged tile (clamped in from
@@ -454,63 +512,99 @@ __global__ void __launch_bounds__(kNT) k_pressure_gradient(Lattice L, Phys P, co
                                                            const float4 * __restrict__ bpos,
                                                            const float4 * __restrict__ bvel,
                                                            const float4 * __restrict__ bnrm,
-                                                           const int * __restrict__ bcellStart) {
+                                                           const int * __restrict__ bcellStart, int * queue) {
     using G = BrickGeom<DIM>;
-    __shared__ float tile[G::TILE];
-    constexpr int ROWS = G::BY * G::BZ;        // cell rows of a brick
-    constexpr int PER_ROW = kNT / ROWS;       // threads per row
+    __shared__ __align__(16) float tile[G::TILE];
+    constexpr int ROWS = G::BY * G::BZ;  // cell rows of a brick
+    __shared__ int rinc[ROWS], rbeg[ROWS];
+    __shared__ int slot;
     const int nb = *pcount;
-    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
+    const int t  = threadIdx.x;
+    for (int bi = queue_take(queue, &slot); bi < nb; bi = queue_take(queue, &slot)) {
         const int b   = plist[bi];
         const int3 bc = brick_coords(L, b);
-        __syncthreads();
-        load_tile<DIM>(L, bflag, bc, tile, [&](long long s) { return N.V[s] * N.x[s]; });
-        __syncthreads();
-        const bool walls = bnear[b] != 0;
-        const int row    = threadIdx.x % ROWS, sub = threadIdx.x / ROWS;
-        const int ly = row % G::BY, lz = row / G::BY;
-        const int y = bc.y * G::BY + ly, z = bc.z * G::BZ + lz;
-        if (y >= L.ny || (DIM == 3 && z >= L.nz)) continue;
         const int x0 = bc.x * G::BX, x1 = min(x0 + G::BX, L.nx);
-        const long long rbase = (long long) L.nx * (y + (long long) L.ny * z);
-        const int jb = cellStart[rbase + x0], je = cellStart[rbase + x1];
+        load_tile4<DIM, kNT>(L, bflag, bc, tile, [&](long long s) {
+            const float4 v = *reinterpret_cast<const float4 *>(N.V + s), x = *reinterpret_cast<const float4 *>(N.x + s);
+            return make_float4(v.x * x.x, v.y * x.y, v.z * x.z, v.w * x.w);
+        });
+        // particles of the brick: the cell rows' sorted ranges, enumerated
+        // row after row (inclusive scan of the row counts in rinc)
+        if (t < 32 * ((ROWS + 31) / 32)) {
+            int cnt = 0, jb = 0;
+            if (t < ROWS) {
+                const int y = bc.y * G::BY + t % G::BY, z = DIM == 3 ? bc.z * G::BZ + t / G::BY : 0;
+                if (y < L.ny && (DIM == 2 || z < L.nz)) {
+                    const long long rbase = (long long) L.nx * (y + (long long) L.ny * z);
+                    jb  = cellStart[rbase + x0];
+                    cnt = cellStart[rbase + x1] - jb;
+                }
+            }
+            int inc = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, inc, o);
+                if ((t & 31) >= o) inc += v;
+            }
+            if (t < ROWS) {
+                rinc[t] = inc;
+                rbeg[t] = jb - (inc - cnt);
+            }
+        }
+        __syncthreads();
+        if (ROWS > 32 && t >= 32 && t < ROWS) {
+            const int w0 = rinc[31];
+            rinc[t] += w0;
+            rbeg[t] -= w0;
+        }
+        __syncthreads();
+        const int total  = rinc[ROWS - 1];
+        const bool walls = bnear[b] != 0;
         // tile origin (node coordinates of tile index 0)
         const float tox = float(x0 - G::HALO), toy = float(bc.y * G::BY - G::HALO);
         const float toz = DIM == 3 ? float(bc.z * G::BZ - G::HALO) : 0.f;
-        for (int j = jb + sub; j < je; j += PER_ROW) {
+        for (int p = t; p < total; p += kNT) {
+            int lo = 0, hi = ROWS - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (rinc[mid] > p) hi = mid;
+                else lo = mid + 1;
+            }
+            const int j     = rbeg[lo] + p;
             const float4 q  = pos[j];
             const float4 vi = vel[j];
             const float ux = (q.x - L.ox) * L.inv_dx - tox, uy = (q.y - L.oy) * L.inv_dx - toy;
             const float uz = DIM == 3 ? (q.z - L.oz) * L.inv_dx - toz : 0.f;
             float3 f = make_float3(0.f, 0.f, 0.f);
-            const bool inside = ux > 3.f && ux < float(G::TX) - 4.f && uy > 3.f && uy < float(G::TY) - 4.f &&
-                                (DIM == 2 || (uz > 3.f && uz < float(G::TZ) - 4.f));
+            const bool inside = ux >= 3.f && ux < float(G::TX) - 4.f && uy >= 3.f && uy < float(G::TY) - 4.f &&
+                                (DIM == 2 || (uz >= 3.f && uz < float(G::TZ) - 4.f));
             if (inside) {
-                // nodes within H lie in the 8-node x-window floor(ux) - 3 .. floor(ux) + 4 of each row
-                const int kz0 = DIM == 3 ? __float2int_ru(uz - 4.f) : 0, kz1 = DIM == 3 ? __float2int_rd(uz + 4.f) : 0;
-                const int ky0 = __float2int_ru(uy - 4.f), ky1 = __float2int_rd(uy + 4.f);
-                const int kxb  = __float2int_rd(ux) - 3;
-                const float dx0 = ux - float(kxb);
-                for (int kz = kz0; kz <= kz1; kz++) {
-                    const float dz = DIM == 3 ? uz - kz : 0.f;
-                    for (int ky = ky0; ky <= ky1; ky++) {
-                        const float dy   = uy - ky;
-                        const float dyz2 = fmaf(dy, dy, dz * dz);
+                // nodes within H of the particle lie in the 8^DIM window
+                // floor(u) - 3 .. floor(u) + 4 (offset -4 is excluded: r2 < 16)
+                const int cx = int(ux), cy = int(uy), cz = DIM == 3 ? int(uz) : 0;
+                const float fx = ux - float(cx - 3);
+                const float2 dxp[4] = {make_float2(fx - 2.f, fx - 3.f), make_float2(fx - 4.f, fx - 5.f),
+                                       make_float2(fx - 1.f, fx - 6.f), make_float2(fx, fx - 7.f)};
+                float2 sx = make_float2(0.f, 0.f);
+                float fy = 0.f, fz = 0.f;
+                for (int oz = 0; oz < (DIM == 3 ? 8 : 1); oz++) {
+                    const int kz    = DIM == 3 ? cz - 3 + oz : 0;
+                    const float dz  = DIM == 3 ? uz - float(kz) : 0.f;
+                    const float dz2 = dz * dz;
+#pragma unroll 2
+                    for (int oy = 0; oy < 8; oy++) {
+                        const int ky     = cy - 3 + oy;
+                        const float dy   = uy - float(ky);
+                        const float dyz2 = fmaf(dy, dy, dz2);
                         if (dyz2 >= 16.f) continue;
-                        const float * trow = tile + G::PX * (ky + G::TY * kz) + kxb;
-                        float sx = 0.f, sg = 0.f;  // sum g dx and sum g over the row
-#pragma unroll
-                        for (int i = 0; i < 8; i++) {
-                            const float dx = dx0 - float(i);
-                            const float g  = grad_scale(fmaf(dx, dx, dyz2), P.c1H) * trow[i];
-                            sx = fmaf(g, dx, sx);
-                            sg += g;
-                        }
-                        f.x += sx;
-                        f.y = fmaf(dy, sg, f.y);
-                        f.z = fmaf(dz, sg, f.z);
+                        const float * trow = tile + G::PX * (ky + G::TY * kz) + (cx - 3);
+                        const float2 sg = gradient_row(trow, dxp, dyz2, sx);
+                        const float s   = sg.x + sg.y;
+                        fy = fmaf(dy, s, fy);
+                        fz = fmaf(dz, s, fz);
                     }
                 }
+                f = make_float3(P.c1H * (sx.x + sx.y), P.c1H * fy, P.c1H * fz);
             } else {
                 f = gradient_virtual_global<DIM>(L, P, bflag, N, q);
             }
@@ -527,6 +621,7 @@ __global__ void __launch_bounds__(kNT) k_pressure_gradient(Lattice L, Phys P, co
             vel[j] = o;
         }
     }
+    queue_finish(queue);
 }
 
 // ---------------------------------------------------------------------------
@@ -536,9 +631,22 @@ template<int DIM>
 void launch_pressure_gradient(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
                               const int * plist, const int * pcount, const unsigned char * bnear, const float4 * pos,
                               float4 * vel, const int * cellStart, const float4 * bpos, const float4 * bvel,
-                              const float4 * bnrm, const int * bcellStart, int grid, cudaStream_t st) {
+                              const float4 * bnrm, const int * bcellStart, int grid, int * queue, cudaStream_t st) {
     k_pressure_gradient<DIM><<<grid, kNT, 0, st>>>(L, P, B.flag, N, plist, pcount, bnear, pos, vel, cellStart, bpos,
-                                                   bvel, bnrm, bcellStart);
+                                                   bvel, bnrm, bcellStart, queue);
+}
+template<int DIM> int pressure_gradient_blocks_per_sm() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pressure_gradient<DIM>, kNT, 0) != cudaSuccess) n = 1;
+    return n > 0 ? n : 1;
+}
+template<int DIM> int node_gather_blocks_per_sm() {
+    int n = 0;
+    int m = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_node_gather<DIM, true>, 128, 0) != cudaSuccess) n = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_node_gather<DIM, false>, 128, 0) != cudaSuccess) m = 1;
+    n = std::min(n, m);
+    return n > 0 ? n : 1;
 }
 void launch_brick_list(const unsigned char * bflag, int nbricks, int * list, int * count, cudaStream_t st) {
     k_brick_list<<<1, 1024, 0, st>>>(bflag, nbricks, list, count);
@@ -548,9 +656,14 @@ template<int DIM>
 void launch_node_gather(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
                         const float4 * pos, const float4 * vel, const int * cellStart, const float4 * bpos,
                         const float4 * bvel, const int * bcellStart, const unsigned char * bnear, int grid,
-                        cudaStream_t st) {
-    k_node_gather<DIM><<<grid * 2, 128, 0, st>>>(L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel, bcellStart,
-                                             bnear);
+                        int * queue, cudaStream_t st) {
+    // H >= 2h: particles within h only reach the inner branch of W_H
+    if (double(P.H) >= 2.0 * double(P.h) * (1.0 - 1e-6))
+        k_node_gather<DIM, true><<<grid, 128, 0, st>>>(L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel,
+                                                       bcellStart, bnear, queue);
+    else
+        k_node_gather<DIM, false><<<grid, 128, 0, st>>>(L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel,
+                                                        bcellStart, bnear, queue);
 }
 
 template<int DIM>
@@ -604,11 +717,13 @@ void launch_zero_active(const Lattice & L, const BrickArrays & B, float * a, int
 #define SWC_INST(D)                                                                                                    \
     template void launch_node_gather<D>(const Lattice &, const Phys &, const BrickArrays &, const NodeArrays &,        \
                                         const float4 *, const float4 *, const int *, const float4 *, const float4 *,   \
-                                        const int *, const unsigned char *, int, cudaStream_t);                        \
+                                        const int *, const unsigned char *, int, int *, cudaStream_t);                 \
     template void launch_pressure_gradient<D>(const Lattice &, const Phys &, const BrickArrays &, const NodeArrays &,  \
                                               const int *, const int *, const unsigned char *, const float4 *,         \
                                               float4 *, const int *, const float4 *, const float4 *, const float4 *,   \
-                                              const int *, int, cudaStream_t);                                         \
+                                              const int *, int, int *, cudaStream_t);                                  \
+    template int pressure_gradient_blocks_per_sm<D>();                                                                 \
+    template int node_gather_blocks_per_sm<D>();                                                                       \
     template void launch_segments<D>(const Lattice &, const BrickArrays &, const NodeArrays &, int *, int,             \
                                      cudaStream_t);                                                                    \
     template void launch_diag_max_f64<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const StencilD &,   \

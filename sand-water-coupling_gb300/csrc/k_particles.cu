@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(256) k_density(const float4 * __restrict__ pos
             const float4 p = pos[j];
             const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < P.h2) s += kW(r2 * rsqrtf(fmaxf(r2, 1e-30f)), P.inv_h, P.c0h);
+            if (r2 < P.h2) s += kW(r2 * rsqrt_n(fmaxf(r2, 1e-30f)), P.inv_h, P.c0h);
         });
         const float rho = mass * s;
         if (rho_out) rho_out[i] = rho;
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(256) k_forces(const float4 * __restrict__ pos,
                     const float4 vj = vel[j];
                     float w, gsc;
                     kernel_and_grad(r2, P.inv_h, P.c0h, P.c1h, w, gsc);
-                    const float rinv = rsqrtf(r2);
+                    const float rinv = rsqrt_n(fmaxf(r2, 1e-30f));
                     const float s = ((vj.x - vi.x) * dx + (vj.y - vi.y) * dy + (vj.z - vi.z) * dz) * (rinv * rinv);
                     // gradientKernel(x_j - x_i) = -W'(r) (x_j - x_i)/r, divided by rho_j = m / vel.w
                     const float g = gsc * s * (vj.w * P.inv_mass);
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(256) k_boundary_density(float4 * __restrict__ 
             const float4 p = bpos[j];
             const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < P.h2) s += kW(r2 * rsqrtf(fmaxf(r2, 1e-30f)), P.inv_h, P.c0h);
+            if (r2 < P.h2) s += kW(r2 * rsqrt_n(fmaxf(r2, 1e-30f)), P.inv_h, P.c0h);
         });
         const float rho = P.bmass * s;
         if (rho_out) rho_out[i] = rho;

@@ -3,6 +3,7 @@
 // one CUDA stream.  The CG loop runs from device-resident scalars; batches of
 // iterations are replayed from captured CUDA graphs between host convergence
 // checks.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -38,8 +39,12 @@ struct swc_ctx {
     Phys            P{};
     Stencil         S{};
     StencilD        SD{};
-    int             grid  = 1;  // persistent grid of the 256-thread brick kernels
-    int             sgrid = 1;  // persistent grid of the row-stencil kernels (one brick per block)
+    int             grid  = 1;  // grid of the 256-thread brick / streaming kernels
+    int             sgrid = 1;  // resident grid of the CG SpMV (static brick striding, deterministic pq)
+    int             rgrid = 1;  // grid of the other row-stencil kernels (one brick per block at a time)
+    int             ggrid = 1;  // resident grid of the virtual gather (brick queue)
+    int             pgrid = 1;  // resident grid of the pressure gradient (brick queue)
+    int *           queues = nullptr;  // brick queues: gather [0, 2), gradient [2, 4)
     std::string     err;
 
     // real particles (sorted by cell)
@@ -253,9 +258,9 @@ template<int DIM> void run_generate(swc_ctx * c, bool with_ahat) {
     launch_brick_list(c->B.flag, c->L.nbricks, c->B.list, c->B.count, c->stream);
     launch_brick_list(c->pflag, c->L.nbricks, c->plist, c->pcount, c->stream);
     launch_node_gather<DIM>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel, c->bcellStart,
-                            c->bnear, c->grid, c->stream);
+                            c->bnear, c->ggrid, c->queues, c->stream);
     launch_segments<DIM>(c->L, c->B, c->N, c->scan_tiles, c->grid, c->stream);
-    if (with_ahat) launch_ahat<DIM>(c->L, c->P, c->B, c->N, c->S, c->N.nvirt, c->sgrid, c->stream);
+    if (with_ahat) launch_ahat<DIM>(c->L, c->P, c->B, c->N, c->S, c->N.nvirt, c->rgrid, c->stream);
 }
 
 int capture_graphs(swc_ctx * c) {
@@ -283,7 +288,7 @@ int capture_graphs(swc_ctx * c) {
 template<int DIM> int cg_init_sync(swc_ctx * c) {
     const int * nv = c->B.seg_off + c->B.nseg;
     launch_cg_init<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->opts.tolerance, c->opts.max_iterations, nv,
-                        c->sgrid, c->stream);
+                        c->rgrid, c->stream);
     CK(cudaMemcpyAsync(&c->hcg->st, c->cg, sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&c->hcg->nv, nv, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&c->hcg->nbricks, c->B.count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -329,7 +334,7 @@ template<int DIM> int run_cg(swc_ctx * c, swc_stats * st, bool initialized) {
         st->status               = status;
     }
     if (c->opts.compute_true_residual && st) {
-        launch_true_residual<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->res2, c->sgrid, c->stream);
+        launch_true_residual<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->res2, c->rgrid, c->stream);
         double r2[2];
         CK(cudaMemcpyAsync(r2, c->res2, sizeof(r2), cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
@@ -404,7 +409,7 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     }
     mark(c, 6);
     launch_pressure_gradient<DIM>(c->L, c->P, c->B, c->N, c->plist, c->pcount, c->bnear, c->pos, c->vel,
-                                  c->cellStart, c->bpos, c->bvel, c->bnrm, c->bcellStart, c->grid, c->stream);
+                                  c->cellStart, c->bpos, c->bvel, c->bnrm, c->bcellStart, c->pgrid, c->queues + 2, c->stream);
     mark(c, 7);
     // p in reference order (next step's prefix warm start) and N_v for it
     launch_compact_export<DIM>(c->L, c->B, c->N, c->pcomp, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
@@ -597,8 +602,17 @@ int swc_create(const swc_scene * s, const swc_solver_opts * o, swc_ctx ** out) {
         return SWC_BAD_ARG;
     }
     c->grid  = std::max(1, std::min(L.nbricks, c->num_sms * 8));
-    c->sgrid = std::max(1, std::min(L.nbricks, c->num_sms * 10));
-    const size_t npart = 2 * size_t(std::max(c->grid, c->sgrid)) + 8;
+    c->rgrid = std::max(1, std::min(L.nbricks, c->num_sms * 10));
+    {
+        const bool d3 = s->dim == 3;
+        const int so  = d3 ? cg_spmv_blocks_per_sm<3>() : cg_spmv_blocks_per_sm<2>();
+        const int go  = d3 ? node_gather_blocks_per_sm<3>() : node_gather_blocks_per_sm<2>();
+        const int po  = d3 ? pressure_gradient_blocks_per_sm<3>() : pressure_gradient_blocks_per_sm<2>();
+        c->sgrid      = std::max(1, std::min(L.nbricks, c->num_sms * so));
+        c->ggrid      = std::max(1, std::min(L.nbricks, c->num_sms * go));
+        c->pgrid      = std::max(1, std::min(L.nbricks, c->num_sms * po));
+    }
+    const size_t npart = 2 * size_t(std::max({c->grid, c->sgrid, c->rgrid})) + 8;
     setup_phys(c);
     int rc = SWC_OK;
     const size_t slots = size_t(L.nbricks) * bx * by * bz;
@@ -624,13 +638,14 @@ int swc_create(const swc_scene * s, const swc_solver_opts * o, swc_ctx ** out) {
         return fail(rc);
     if ((rc = dalloc(c, &c->pcomp, size_t(L.ncells))) || (rc = dalloc(c, &c->nv_prev, 1)) ||
         (rc = dalloc(c, &c->scan_tiles, scan_tile_count(std::max<long long>(c->B.nseg, L.ncells) + 1) + 2)) ||
-        (rc = dalloc(c, &c->cg, 1)) || (rc = dalloc(c, &c->partials, npart)) ||
+        (rc = dalloc(c, &c->cg, 1)) || (rc = dalloc(c, &c->partials, npart)) || (rc = dalloc(c, &c->queues, 4)) ||
         (rc = dalloc(c, &c->diag_bits, 1)) || (rc = dalloc(c, &c->max_bits, 1)) || (rc = dalloc(c, &c->res2, 2)) ||
         (rc = dalloc(c, &c->cellStart, L.ncells + 1)) || (rc = dalloc(c, &c->bcellStart, L.ncells + 1)))
         return fail(rc);
     if (cudaMallocHost(reinterpret_cast<void **>(&c->hcg), sizeof(HostCg)) != cudaSuccess) return fail(SWC_OUT_OF_MEMORY);
     cudaMemsetAsync(c->cg, 0, sizeof(CgState), c->stream);
     cudaMemsetAsync(c->partials, 0, sizeof(double) * npart, c->stream);
+    cudaMemsetAsync(c->queues, 0, sizeof(int) * 4, c->stream);
     cudaMemsetAsync(c->B.flag, 0, L.nbricks, c->stream);
     cudaMemsetAsync(c->B.flag_prev, 0, L.nbricks, c->stream);
     cudaMemsetAsync(c->N.flag, 0, slots, c->stream);
@@ -703,6 +718,7 @@ void swc_destroy(swc_ctx * c) {
     dfree(c->scan_tiles);
     dfree(c->cg);
     dfree(c->partials);
+    dfree(c->queues);
     dfree(c->diag_bits);
     dfree(c->max_bits);
     dfree(c->res2);
@@ -1037,14 +1053,14 @@ int swc_apply_operator(swc_ctx * c, const double * x, double * y, int64_t n) {
     // brick-layout vector: reuse compact export machinery through a temporary NodeArrays view
     if (c->dim == 2) {
         launch_compact_import<2>(c->L, c->B, c->N, d_in, t_in, c->grid, c->stream);
-        launch_apply_operator<2>(c->L, c->B, c->N, c->S, t_in, t_out, c->sgrid, c->stream);
+        launch_apply_operator<2>(c->L, c->B, c->N, c->S, t_in, t_out, c->rgrid, c->stream);
         NodeArrays T = c->N;
         T.x          = t_out;
         launch_compact_export<2>(c->L, c->B, T, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, d_out,
                                  nullptr, c->grid, c->stream);
     } else {
         launch_compact_import<3>(c->L, c->B, c->N, d_in, t_in, c->grid, c->stream);
-        launch_apply_operator<3>(c->L, c->B, c->N, c->S, t_in, t_out, c->sgrid, c->stream);
+        launch_apply_operator<3>(c->L, c->B, c->N, c->S, t_in, t_out, c->rgrid, c->stream);
         NodeArrays T = c->N;
         T.x          = t_out;
         launch_compact_export<3>(c->L, c->B, T, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, d_out,
@@ -1141,11 +1157,11 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
             case 6: launch_cg_direction<3>(c->B, c->N, c->cg, c->grid, c->stream); break;
             case 2:
                 launch_node_gather<3>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel,
-                                      c->bcellStart, c->bnear, c->grid, c->stream);
+                                      c->bcellStart, c->bnear, c->ggrid, c->queues, c->stream);
                 break;
             case 3:
                 launch_pressure_gradient<3>(c->L, c->P, c->B, c->N, c->plist, c->pcount, c->bnear, c->pos, c->vel,
-                                            c->cellStart, c->bpos, c->bvel, c->bnrm, c->bcellStart, c->grid,
+                                            c->cellStart, c->bpos, c->bvel, c->bnrm, c->bcellStart, c->pgrid, c->queues + 2,
                                             c->stream);
                 break;
             case 4: launch_density<3>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->stream); break;
@@ -1155,7 +1171,7 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
             switch (which) {
             case 2:
                 launch_node_gather<2>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel,
-                                      c->bcellStart, c->bnear, c->grid, c->stream);
+                                      c->bcellStart, c->bnear, c->ggrid, c->queues, c->stream);
                 break;
             case 4: launch_density<2>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->stream); break;
             default: break;

@@ -63,6 +63,14 @@ struct Phys {
     int   gravity_on;
 };
 
+// 1/sqrt(x) for normal x (every caller clamps x >= 1e-30): the hardware
+// approximation without the rescaling of denormal inputs that rsqrtf adds.
+__device__ __forceinline__ float rsqrt_n(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // --------------------------------------------------------------------------
 // Cubic spline (reference: Cores/Structures/SmoothedParticles.h:60-72).
 // --------------------------------------------------------------------------
@@ -85,7 +93,7 @@ __device__ __forceinline__ float kdW(float r, float inv_h, float c1) {
 // -W'/r = -c1 (3q - 2)/h for q < 1/2 and c1 (1 - q)^2 / r otherwise; at r = 0 the
 // factor stays finite and multiplies a zero offset (gradientKernel(0) = 0).
 __device__ __forceinline__ void kernel_and_grad(float r2, float inv_h, float c0, float c1, float & w, float & gsc) {
-    const float rinv = rsqrtf(fmaxf(r2, 1e-30f));
+    const float rinv = rsqrt_n(fmaxf(r2, 1e-30f));
     const float q    = r2 * rinv * inv_h;
     const float t    = 1.f - q;
     const bool inner = q < 0.5f;

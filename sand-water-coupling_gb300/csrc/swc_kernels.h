@@ -96,14 +96,20 @@ template<int DIM>
 void launch_node_gather(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
                         const float4 * pos, const float4 * vel, const int * cellStart, const float4 * bpos,
                         const float4 * bvel, const int * bcellStart, const unsigned char * bnear, int grid,
-                        cudaStream_t st);
+                        int * queue, cudaStream_t st);
 // Pressure-gradient update over the bricks that hold particles (plist / pcount),
 // node field staged per brick in shared memory; bnear flags bricks near walls.
 template<int DIM>
 void launch_pressure_gradient(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
                               const int * plist, const int * pcount, const unsigned char * bnear, const float4 * pos,
                               float4 * vel, const int * cellStart, const float4 * bpos, const float4 * bvel,
-                              const float4 * bnrm, const int * bcellStart, int grid, cudaStream_t st);
+                              const float4 * bnrm, const int * bcellStart, int grid, int * queue, cudaStream_t st);
+// Resident blocks per SM of the persistent brick kernels (their grids are
+// SMs x this; gather and gradient take bricks from a zero-initialised queue of
+// two ints).
+template<int DIM> int node_gather_blocks_per_sm();
+template<int DIM> int pressure_gradient_blocks_per_sm();
+template<int DIM> int cg_spmv_blocks_per_sm();
 template<int DIM>
 void launch_segments(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int * tiles, int grid,
                      cudaStream_t st);

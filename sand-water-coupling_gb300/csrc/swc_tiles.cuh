@@ -9,6 +9,27 @@ namespace swc {
 
 constexpr int kNT = 256;  // threads per block of the brick kernels
 
+// Dynamic brick queue of the kernels without cross-block reductions (gather,
+// pressure gradient): blocks take list indices from q[0] until they run out,
+// and the last block to finish resets q[0] and its finish counter q[1] for the
+// next launch, so a queue is zeroed once, at allocation.  Every thread of the
+// block calls queue_take (it synchronises the block).
+__device__ __forceinline__ int queue_take(int * q, int * slot) {
+    __syncthreads();  // the previous *slot has been read by every thread
+    if (threadIdx.x == 0) *slot = atomicAdd(q, 1);
+    __syncthreads();
+    return *slot;
+}
+__device__ __forceinline__ void queue_finish(int * q) {
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(q + 1, 1) == int(gridDim.x) - 1) {
+            atomicExch(q, 0);
+            atomicExch(q + 1, 0);
+        }
+    }
+}
+
 // Brick coordinates of brick id b.
 __device__ __forceinline__ int3 brick_coords(const Lattice & L, int b) {
     return make_int3(b % L.bnx, (b / L.bnx) % L.bny, b / (L.bnx * L.bny));
@@ -96,13 +117,12 @@ template<int DIM> struct RowGeom {
 // which lies inside one brick and is 16-byte aligned in the brick layout.
 // get4(slot) returns the 4 values starting at `slot`; nodes outside the lattice
 // or in inactive bricks read as zero.
-template<int DIM, class Get4>
+template<int DIM, int NT = RowGeom<DIM>::NT, class Get4>
 __device__ __forceinline__ void load_tile4(const Lattice & L, const unsigned char * __restrict__ bflag, int3 bc,
                                            float * tile, Get4 get4) {
     using G            = BrickGeom<DIM>;
     constexpr int SEGX = G::TX / 4;
     constexpr int NSEG = SEGX * G::TY * G::TZ;
-    constexpr int NT   = RowGeom<DIM>::NT;
 #pragma unroll 4
     for (int t = threadIdx.x; t < NSEG; t += NT) {
         const int sx = t % SEGX, ty = (t / SEGX) % G::TY, tz = t / (SEGX * G::TY);
@@ -119,43 +139,92 @@ __device__ __forceinline__ void load_tile4(const Lattice & L, const unsigned cha
     }
 }
 
-// Row stencil: the BX outputs of brick row (ly, lz),
-//   out[i] = sum_{0 < |k|^2 < 16} c(|k|^2) tile[node (i, ly, lz) + k],
-// from one 16-byte-vectorised load of each of the 45 (dy, dz) tile rows.
-template<int DIM>
-__device__ __forceinline__ void stencil_row(const float * tile, int ly, int lz, const Stencil & S,
-                                            float (&out)[BrickGeom<DIM>::BX]) {
-    using G          = BrickGeom<DIM>;
-    constexpr int BX = G::BX;
+// Row stencil over a halo tile with row pitch PX, TY rows per z-plane, y/z
+// halos HY/HZ and an x halo of 4 (rows start 16-byte aligned): the BX outputs
+// of brick row (ly, lz),
+//   out[i] = sum_{0 < |k|^2 < 16} c(|k|^2) tile[node (i, ly, lz) + k].
+// The 45 (dy, dz) rows within reach (7 in 2D) fall into classes of equal
+// m = dy^2 + dz^2 (9 in 3D: 0 1 2 4 5 8 9 10 13; 4 in 2D), and all rows of a
+// class share the x-coefficients c(dx^2 + m).  The rows of a class are summed
+// first (T_m) and the 1D x-convolution is applied once per class, so in 3D a
+// row of 8 outputs costs 45 row loads, 450 adds and 416 FMAs instead of 2000
+// FMAs.
+template<int DIM, int PX, int TY, int M>
+__device__ __forceinline__ void stencil_class(const float * centre, const Stencil & S,
+                                              float (&out)[BrickGeom<DIM>::BX]) {
+    constexpr int BX = BrickGeom<DIM>::BX, TX = BX + 8;
     constexpr int ZR = DIM == 3 ? 3 : 0;
-#pragma unroll
-    for (int i = 0; i < BX; i++) out[i] = 0.f;
+    constexpr int R  = M <= 6 ? 3 : (M <= 11 ? 2 : 1);  // x reach: dx^2 + M <= 15
+    float T[TX];
+    bool have = false;
 #pragma unroll
     for (int dz = -ZR; dz <= ZR; dz++)
 #pragma unroll
         for (int dy = -3; dy <= 3; dy++) {
-            const int ryz = dy * dy + dz * dz;
-            if (ryz >= 16) continue;
-            const float * row = tile + G::PX * ((ly + G::HALO + dy) + G::TY * (DIM == 3 ? lz + G::HALO + dz : 0));
-            float v[G::TX];
+            if (dy * dy + dz * dz != M) continue;
+            const float * row = centre + PX * (dy + TY * dz);
 #pragma unroll
-            for (int s = 0; s < G::TX / 4; s++) {
+            for (int s = 0; s < TX / 4; s++) {
                 const float4 t = reinterpret_cast<const float4 *>(row)[s];
-                v[4 * s] = t.x;
-                v[4 * s + 1] = t.y;
-                v[4 * s + 2] = t.z;
-                v[4 * s + 3] = t.w;
-            }
 #pragma unroll
-            for (int dx = -3; dx <= 3; dx++) {
-                const int r2 = dx * dx + ryz;
-                if (r2 >= 16 || r2 == 0) continue;
-                const float c = S.c[r2];
-#pragma unroll
-                for (int i = 0; i < BX; i++) out[i] = fmaf(c, v[i + G::HALO + dx], out[i]);
+                for (int j = 0; j < 4; j++) {
+                    const int k = 4 * s + j;
+                    if (k < 4 - R || k > BX + 3 + R) continue;
+                    const float v = j == 0 ? t.x : (j == 1 ? t.y : (j == 2 ? t.z : t.w));
+                    T[k]          = have ? T[k] + v : v;
+                }
             }
+            have = true;
         }
+#pragma unroll
+    for (int dx = -R; dx <= R; dx++) {
+        if (dx == 0 && M == 0) continue;
+        const float c = S.c[dx * dx + M];
+#pragma unroll
+        for (int i = 0; i < BX; i++) out[i] = fmaf(c, T[i + 4 + dx], out[i]);
+    }
 }
+
+template<int DIM, int PX, int TY, int HY, int HZ>
+__device__ __forceinline__ void stencil_row_t(const float * tile, int ly, int lz, const Stencil & S,
+                                              float (&out)[BrickGeom<DIM>::BX]) {
+    constexpr int BX     = BrickGeom<DIM>::BX;
+    const float * centre = tile + PX * ((ly + HY) + TY * (DIM == 3 ? lz + HZ : 0));
+#pragma unroll
+    for (int i = 0; i < BX; i++) out[i] = 0.f;
+    stencil_class<DIM, PX, TY, 0>(centre, S, out);
+    stencil_class<DIM, PX, TY, 1>(centre, S, out);
+    if constexpr (DIM == 3) stencil_class<DIM, PX, TY, 2>(centre, S, out);
+    stencil_class<DIM, PX, TY, 4>(centre, S, out);
+    if constexpr (DIM == 3) {
+        stencil_class<DIM, PX, TY, 5>(centre, S, out);
+        stencil_class<DIM, PX, TY, 8>(centre, S, out);
+    }
+    stencil_class<DIM, PX, TY, 9>(centre, S, out);
+    if constexpr (DIM == 3) {
+        stencil_class<DIM, PX, TY, 10>(centre, S, out);
+        stencil_class<DIM, PX, TY, 13>(centre, S, out);
+    }
+}
+
+// Row stencil over a brick-geometry tile (halo 4 on every side).
+template<int DIM>
+__device__ __forceinline__ void stencil_row(const float * tile, int ly, int lz, const Stencil & S,
+                                            float (&out)[BrickGeom<DIM>::BX]) {
+    using G = BrickGeom<DIM>;
+    stencil_row_t<DIM, G::PX, G::TY, G::HALO, G::HALO>(tile, ly, lz, S, out);
+}
+
+// Halo tile of the CG SpMV: x halo 4 (16-byte aligned rows), y/z halo 3 (the
+// stencil reach), pitch chosen so the 8 rows read by a quarter-warp's LDS.128
+// hit distinct banks.
+template<int DIM> struct SpmvTile {
+    using G = BrickGeom<DIM>;
+    static constexpr int HX = 4, HY = 3, HZ = DIM == 3 ? 3 : 0;
+    static constexpr int TX = G::BX + 2 * HX, TY = G::BY + 2 * HY, TZ = DIM == 3 ? G::BZ + 2 * HZ : 1;
+    static constexpr int PX   = DIM == 3 ? 20 : 28;
+    static constexpr int TILE = PX * TY * TZ;
+};
 
 
 }  // namespace swc
