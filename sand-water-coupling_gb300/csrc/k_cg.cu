@@ -15,7 +15,11 @@
 // d = r + beta d with u = V d (streaming), the SpMV q = A d reading u tiles by
 // double-buffered cp.async, and the x/r update; dot products use exact FP32
 // products summed in float-float below the warp and FP64 above, reduced
-// deterministically.
+// deterministically.  A is not symmetric (alpha_IJ carries V_J) and the
+// reference runs Hestenes-Stiefel CG on the full matrix, so single-reduction
+// rearrangements that rely on symmetry (Chronopoulos-Gear, pipelined CG) are
+// not equivalent here: on a 2D dam break the Chronopoulos-Gear form stalls
+// after ~10 iterations where this form converges.
 #include "swc_kernels.h"
 #include "swc_tiles.cuh"
 

@@ -56,12 +56,6 @@ struct NodeSums2 {
     float2 wsum, rhoI, VI, cnt, ux, uy, uz, bw, dvg, gx, gy, gz;
 };
 
-__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 max02(float2 a) { return make_float2(fmaxf(a.x, 0.f), fmaxf(a.y, 0.f)); }
-
 // Contributions of one particle (position / volume p, velocity / m-over-rho u)
 // to two nodes at x offsets dxx = x_I - x_j (dy, dz shared, ryz = dy^2 + dz^2).
 // With q = r / h, a = max(1 - q, 0) and b = max(a - 1/2, 0) the cubic spline is

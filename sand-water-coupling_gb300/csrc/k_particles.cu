@@ -118,25 +118,85 @@ __global__ void k_permute(const int * __restrict__ perm, long long n, const floa
     }
 }
 
+// Sum of w (W_h = 2 c0h w) over the neighbours within h of two particles a, b,
+// visited once for both (packed FP32x2 arithmetic).
+template<int DIM>
+__device__ __forceinline__ float2 density_sum2(const Lattice & L, const Phys & P, const int * __restrict__ cellStart,
+                                               const float4 * __restrict__ pos, float4 qa, float4 qb) {
+    const float2 qx = make_float2(qa.x, qb.x), qy = make_float2(qa.y, qb.y), qz = make_float2(qa.z, qb.z);
+    float2 s = f2(0.f);
+    for_each_in_radius2<DIM>(L, cellStart, make_float3(qa.x, qa.y, qa.z), make_float3(qb.x, qb.y, qb.z), P.h, P.h2,
+                             [&](int j) {
+                                 const float4 p  = pos[j];
+                                 const float2 dx = add2(qx, f2(-p.x)), dy = add2(qy, f2(-p.y));
+                                 float2 r2       = fma2(dy, dy, mul2(dx, dx));
+                                 if (DIM == 3) {
+                                     const float2 dz = add2(qz, f2(-p.z));
+                                     r2              = fma2(dz, dz, r2);
+                                 }
+                                 const bool m0 = r2.x < P.h2, m1 = r2.y < P.h2;
+                                 if (m0 || m1) s = add2(s, spline2(r2, m0, m1, P.inv_h).w);
+                             });
+    return s;
+}
+
 // rho_i = m sum_j W_h(x_i - x_j)  (SmoothedParticles::computeDensities,
-// Cores/Structures/SmoothedParticles.cpp:25-31).  Writes vel.w = m / rho_i and rho_i.
+// Cores/Structures/SmoothedParticles.cpp:25-31); writes vel.w = m / rho_i and rho_i.
+// One thread per pair of consecutive sorted particles.  A pair that is not in
+// one cell row is appended to left (left[0] = count, ids from left[2]) and
+// visited particle by particle by k_density_left, so no warp runs both paths.
 template<int DIM>
 __global__ void __launch_bounds__(256) k_density(const float4 * __restrict__ pos, float4 * __restrict__ vel,
                                                  float * __restrict__ rho_out, long long n, Lattice L, Phys P,
-                                                 const int * __restrict__ cellStart, float mass) {
-    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+                                                 const int * __restrict__ cellStart, float mass, int * __restrict__ left) {
+    const long long npair = (n + 1) / 2;
+    const float c         = 2.f * P.c0h * mass;
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < npair;
+         t += (long long) gridDim.x * blockDim.x) {
+        const long long ia = 2 * t, ib = ia + 1 < n ? ia + 1 : ia;
+        const float4 qa = pos[ia], qb = pos[ib];
+        if (!near_pair<DIM>(L, qa, qb)) {
+            left[2 + atomicAdd(left, 1)] = int(t);
+            continue;
+        }
+        const float2 s  = density_sum2<DIM>(L, P, cellStart, pos, qa, qb);
+        const float ra = c * s.x, rb = c * s.y;
+        if (rho_out) rho_out[ia] = ra;
+        vel[ia].w = mass / ra;
+        if (ib != ia) {
+            if (rho_out) rho_out[ib] = rb;
+            vel[ib].w = mass / rb;
+        }
+    }
+}
+template<int DIM>
+__global__ void __launch_bounds__(256) k_density_left(const float4 * __restrict__ pos, float4 * __restrict__ vel,
+                                                      float * __restrict__ rho_out, long long n, Lattice L, Phys P,
+                                                      const int * __restrict__ cellStart, float mass, int * left) {
+    // one warp per left-over particle, its neighbour rows spread over the lanes
+    const long long cnt = 2LL * left[0];
+    const float c       = 2.f * P.c0h * mass;
+    const int lane      = threadIdx.x & 31;
+    const long long nw  = (long long) gridDim.x * (blockDim.x >> 5);
+    for (long long k = (blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5; k < cnt; k += nw) {
+        const long long i = 2LL * left[2 + k / 2] + (k & 1);
+        if (i >= n) continue;
         const float4 q = pos[i];
         float s        = 0.f;
-        for_each_in_radius<DIM>(L, cellStart, q.x, q.y, q.z, P.h, P.h2, [&](int j) {
+        for_rows_in_radius<DIM>(L, cellStart, q.x, q.y, q.z, P.h, P.h2, lane, 32, [&](int j) {
             const float4 p = pos[j];
-            const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < P.h2) s += kW(r2 * rsqrt_n(fmaxf(r2, 1e-30f)), P.inv_h, P.c0h);
+            const float dx = q.x - p.x, dy = q.y - p.y, dz = DIM == 3 ? q.z - p.z : 0.f;
+            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            s += spline2(f2(r2), r2 < P.h2, false, P.inv_h).w.x;
         });
-        const float rho = mass * s;
-        if (rho_out) rho_out[i] = rho;
-        vel[i].w = mass / rho;
+        s = warp_sum(s);
+        if (lane == 0) {
+            const float r = c * s;
+            if (rho_out) rho_out[i] = r;
+            vel[i].w = mass / r;
+        }
     }
+    grid_done_reset(left);
 }
 
 // V_i = m / rho_i, stored in pos.w (initialize only; DualParticleSphLiquid.cpp:88-89).
@@ -145,50 +205,115 @@ __global__ void k_set_volume(float4 * __restrict__ pos, const float * __restrict
         pos[i].w = mass / rho[i];
 }
 
-// Gravity (applyExternalForces, SmthParticleHydrodLiquid.cpp:84-88) followed by
-// the div-free Laplacian viscosity (applyViscosityForce :90-98 with
+// Viscous sums of two particles a, b over their neighbours within h (packed;
 // ParticlesBasedVectorField::divFreeLaplacianAtDataPoint,
-// Cores/Structures/ParticlesBasedVectorField.cpp:56-69).  Velocity differences
-// are invariant under the uniform gravity increment, so both run in one pass.
+// Cores/Structures/ParticlesBasedVectorField.cpp:56-69):
+// l += g s (m/rho_j) / m (x_j - x_i) with s = (v_j - v_i).(x_j - x_i) / r^2 and
+// gradientKernel(x_j - x_i) = -W'(r) (x_j - x_i) / r = c1h g (x_j - x_i)
+// (c1h applied by the caller); the particle itself (r = 0) adds nothing.
+template<int DIM>
+__device__ __forceinline__ void viscous_sum2(const Lattice & L, const Phys & P, const int * __restrict__ cellStart,
+                                             const float4 * __restrict__ pos, const float4 * __restrict__ vel,
+                                             float4 qa, float4 va, float4 qb, float4 vb, float2 & lx, float2 & ly,
+                                             float2 & lz) {
+    const float2 qx = make_float2(qa.x, qb.x), qy = make_float2(qa.y, qb.y), qz = make_float2(qa.z, qb.z);
+    const float2 vx = make_float2(va.x, vb.x), vy = make_float2(va.y, vb.y), vz = make_float2(va.z, vb.z);
+    for_each_in_radius2<DIM>(
+        L, cellStart, make_float3(qa.x, qa.y, qa.z), make_float3(qb.x, qb.y, qb.z), P.h, P.h2, [&](int j) {
+            const float4 p = pos[j];
+            // x_j - x_i and v_j - v_i
+            const float2 dx = fma2(qx, f2(-1.f), f2(p.x)), dy = fma2(qy, f2(-1.f), f2(p.y));
+            const float2 dz = DIM == 3 ? fma2(qz, f2(-1.f), f2(p.z)) : f2(0.f);
+            float2 r2       = fma2(dy, dy, mul2(dx, dx));
+            if (DIM == 3) r2 = fma2(dz, dz, r2);
+            const bool m0 = r2.x < P.h2 && r2.x > 0.f, m1 = r2.y < P.h2 && r2.y > 0.f;
+            if (!(m0 || m1)) return;
+            const float4 vj = vel[j];
+            float2 dot = fma2(fma2(vy, f2(-1.f), f2(vj.y)), dy, mul2(fma2(vx, f2(-1.f), f2(vj.x)), dx));
+            if (DIM == 3) dot = fma2(fma2(vz, f2(-1.f), f2(vj.z)), dz, dot);
+            const Spline2 k = spline2(r2, m0, m1, P.inv_h);
+            const float2 gs = mul2(mul2(k.g, mul2(dot, mul2(k.ri, k.ri))), f2(vj.w * P.inv_mass));
+            lx              = fma2(gs, dx, lx);
+            ly              = fma2(gs, dy, ly);
+            if (DIM == 3) lz = fma2(gs, dz, lz);
+        });
+}
+
+// Gravity (applyExternalForces, SmthParticleHydrodLiquid.cpp:84-88) followed by
+// the div-free Laplacian viscosity (applyViscosityForce :90-98).  Velocity
+// differences are invariant under the uniform gravity increment, so both run
+// in one pass; one thread per pair of consecutive sorted particles as in
+// k_density.
+__device__ __forceinline__ float4 forces_out(float4 v, float gx, float gy, float gz, float visc, float lx, float ly,
+                                             float lz, bool d3) {
+    v.x += gx;
+    v.y += gy;
+    v.z += gz;
+    v.x += visc * lx;
+    v.y += visc * ly;
+    if (d3) v.z += visc * lz;
+    return v;
+}
+
 template<int DIM>
 __global__ void __launch_bounds__(256) k_forces(const float4 * __restrict__ pos, const float4 * __restrict__ vel,
                                                 float4 * __restrict__ vel_out, long long n, Lattice L, Phys P,
-                                                const int * __restrict__ cellStart, float dt) {
-    const float visc = P.viscosity * 2.f * (DIM + 2.f) * P.mass * dt;
-    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
-        const float4 q = pos[i];
-        const float4 vi = vel[i];
+                                                const int * __restrict__ cellStart, float dt, int * __restrict__ left) {
+    const float visc      = P.viscosity * 2.f * (DIM + 2.f) * P.mass * dt * P.c1h;
+    const float gx = P.gravity_on ? P.gx * dt : 0.f, gy = P.gravity_on ? P.gy * dt : 0.f;
+    const float gz = P.gravity_on && DIM == 3 ? P.gz * dt : 0.f;
+    const long long npair = (n + 1) / 2;
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < npair;
+         t += (long long) gridDim.x * blockDim.x) {
+        const long long ia = 2 * t, ib = ia + 1 < n ? ia + 1 : ia;
+        const float4 qa = pos[ia], qb = pos[ib], va = vel[ia], vb = vel[ib];
+        float2 lx = f2(0.f), ly = f2(0.f), lz = f2(0.f);
+        if (P.viscosity != 0.f) {
+            if (!near_pair<DIM>(L, qa, qb)) {
+                left[2 + atomicAdd(left, 1)] = int(t);
+                continue;
+            }
+            viscous_sum2<DIM>(L, P, cellStart, pos, vel, qa, va, qb, vb, lx, ly, lz);
+        }
+        vel_out[ia] = forces_out(va, gx, gy, gz, visc, lx.x, ly.x, lz.x, DIM == 3);
+        if (ib != ia) vel_out[ib] = forces_out(vb, gx, gy, gz, visc, lx.y, ly.y, lz.y, DIM == 3);
+    }
+}
+template<int DIM>
+__global__ void __launch_bounds__(256) k_forces_left(const float4 * __restrict__ pos, const float4 * __restrict__ vel,
+                                                     float4 * __restrict__ vel_out, long long n, Lattice L, Phys P,
+                                                     const int * __restrict__ cellStart, float dt, int * left) {
+    const float visc = P.viscosity * 2.f * (DIM + 2.f) * P.mass * dt * P.c1h;
+    const float gx = P.gravity_on ? P.gx * dt : 0.f, gy = P.gravity_on ? P.gy * dt : 0.f;
+    const float gz = P.gravity_on && DIM == 3 ? P.gz * dt : 0.f;
+    // one warp per left-over particle, its neighbour rows spread over the lanes
+    const long long cnt = 2LL * left[0];
+    const int lane      = threadIdx.x & 31;
+    const long long nw  = (long long) gridDim.x * (blockDim.x >> 5);
+    for (long long k = (blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5; k < cnt; k += nw) {
+        const long long i = 2LL * left[2 + k / 2] + (k & 1);
+        if (i >= n) continue;
+        const float4 q = pos[i], v = vel[i];
         float lx = 0.f, ly = 0.f, lz = 0.f;
         if (P.viscosity != 0.f) {
-            for_each_in_radius<DIM>(L, cellStart, q.x, q.y, q.z, P.h, P.h2, [&](int j) {
-                const float4 p = pos[j];
-                const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;  // x_j - x_i
-                const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 < P.h2 && r2 > 0.f) {
-                    const float4 vj = vel[j];
-                    float w, gsc;
-                    kernel_and_grad(r2, P.inv_h, P.c0h, P.c1h, w, gsc);
-                    const float rinv = rsqrt_n(fmaxf(r2, 1e-30f));
-                    const float s = ((vj.x - vi.x) * dx + (vj.y - vi.y) * dy + (vj.z - vi.z) * dz) * (rinv * rinv);
-                    // gradientKernel(x_j - x_i) = -W'(r) (x_j - x_i)/r, divided by rho_j = m / vel.w
-                    const float g = gsc * s * (vj.w * P.inv_mass);
-                    lx += g * dx;
-                    ly += g * dy;
-                    lz += g * dz;
-                }
+            for_rows_in_radius<DIM>(L, cellStart, q.x, q.y, q.z, P.h, P.h2, lane, 32, [&](int j) {
+                const float4 p = pos[j], vj = vel[j];
+                const float dx = p.x - q.x, dy = p.y - q.y, dz = DIM == 3 ? p.z - q.z : 0.f;  // x_j - x_i
+                const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                const float dot = fmaf(vj.z - v.z, dz, fmaf(vj.y - v.y, dy, (vj.x - v.x) * dx));
+                const Spline2 k2 = spline2(f2(r2), r2 < P.h2 && r2 > 0.f, false, P.inv_h);
+                const float gs   = k2.g.x * (dot * (k2.ri.x * k2.ri.x)) * (vj.w * P.inv_mass);
+                lx = fmaf(gs, dx, lx);
+                ly = fmaf(gs, dy, ly);
+                lz = fmaf(gs, dz, lz);
             });
+            lx = warp_sum(lx);
+            ly = warp_sum(ly);
+            lz = warp_sum(lz);
         }
-        float4 o = vi;
-        if (P.gravity_on) {
-            o.x += P.gx * dt;
-            o.y += P.gy * dt;
-            if (DIM == 3) o.z += P.gz * dt;
-        }
-        o.x += visc * lx;
-        o.y += visc * ly;
-        if (DIM == 3) o.z += visc * lz;
-        vel_out[i] = o;
+        if (lane == 0) vel_out[i] = forces_out(v, gx, gy, gz, visc, lx, ly, lz, DIM == 3);
     }
+    grid_done_reset(left);
 }
 
 // Boundary densities from boundary-boundary neighbours (initialize,
@@ -477,6 +602,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int * __restr
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
+constexpr int kLeftBlocks = 256;  // grid of the single-particle passes over left-over pairs (grid-stride)
 static inline int grid_for(long long n, int threads, int cap = 152 * 16) {
     long long g = (n + threads - 1) / threads;
     if (g < 1) g = 1;
@@ -530,17 +656,22 @@ void launch_bin(const Lattice & L, long long n, float4 * pos, float4 * vel, floa
 
 template<int DIM>
 void launch_density(const float4 * pos, float4 * vel, float * rho, long long n, const Lattice & L, const Phys & P,
-                    const int * cellStart, cudaStream_t st) {
-    if (n > 0) k_density<DIM><<<grid_for(n, 256, 1 << 20), 256, 0, st>>>(pos, vel, rho, n, L, P, cellStart, P.mass);
+                    const int * cellStart, int * left, cudaStream_t st) {
+    if (n <= 0) return;
+    k_density<DIM><<<grid_for((n + 1) / 2, 256, 1 << 20), 256, 0, st>>>(pos, vel, rho, n, L, P, cellStart, P.mass,
+                                                                         left);
+    k_density_left<DIM><<<kLeftBlocks, 256, 0, st>>>(pos, vel, rho, n, L, P, cellStart, P.mass, left);
 }
 void launch_set_volume(float4 * pos, const float * rho, long long n, float mass, cudaStream_t st) {
     if (n > 0) k_set_volume<<<grid_for(n, 256), 256, 0, st>>>(pos, rho, n, mass);
 }
 template<int DIM>
 void launch_forces(const float4 * pos, const float4 * vel, float4 * vel_out, long long n, const Lattice & L,
-                   const Phys & P, const int * cellStart, float dt, cudaStream_t st) {
-    if (n > 0)
-        k_forces<DIM><<<grid_for(n, 256, 1 << 20), 256, 0, st>>>(pos, vel, vel_out, n, L, P, cellStart, dt);
+                   const Phys & P, const int * cellStart, float dt, int * left, cudaStream_t st) {
+    if (n <= 0) return;
+    k_forces<DIM><<<grid_for((n + 1) / 2, 256, 1 << 20), 256, 0, st>>>(pos, vel, vel_out, n, L, P, cellStart, dt,
+                                                                       left);
+    k_forces_left<DIM><<<kLeftBlocks, 256, 0, st>>>(pos, vel, vel_out, n, L, P, cellStart, dt, left);
 }
 template<int DIM>
 void launch_boundary_density(float4 * bpos, float4 * bvel, float * rho, long long nb, const Lattice & L,
@@ -592,9 +723,9 @@ void launch_debug_neighbors(int which, long long nq, const double * q, const Lat
     template void launch_bin<D>(const Lattice &, long long, float4 *, float4 *, float4 *, int *, SortScratch &, int *, \
                                 cudaStream_t);                                                                         \
     template void launch_density<D>(const float4 *, float4 *, float *, long long, const Lattice &, const Phys &,       \
-                                    const int *, cudaStream_t);                                                        \
+                                    const int *, int *, cudaStream_t);                                                 \
     template void launch_forces<D>(const float4 *, const float4 *, float4 *, long long, const Lattice &, const Phys &,  \
-                                   const int *, float, cudaStream_t);                                                  \
+                                   const int *, float, int *, cudaStream_t);                                           \
     template void launch_boundary_density<D>(float4 *, float4 *, float *, long long, const Lattice &, const Phys &,    \
                                              const int *, cudaStream_t);                                               \
     template void launch_mark_bricks<D>(const float4 *, long long, const Lattice &, const Phys &, unsigned char *,     \

@@ -54,6 +54,7 @@ struct swc_ctx {
     float *    rho = nullptr;
     float *    vol_by_id = nullptr;
     double *   stage = nullptr;  // FP64 host-format staging (2 * n * dim)
+    int *      pleft = nullptr;  // particle pairs left to the single-particle pass: [count, done, pair ids]
     int *      cellStart = nullptr;
     SortScratch sortR{};
 
@@ -447,10 +448,10 @@ template<int DIM> int do_advance(swc_ctx * c, double dt, swc_stats * st, bool mo
     }
     run_bin_real<DIM>(c);
     mark(c, 1);
-    launch_density<DIM>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->stream);
+    launch_density<DIM>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->pleft, c->stream);
     mark(c, 2);
     if (move) {
-        launch_forces<DIM>(c->pos, c->vel, c->vel2, c->n, c->L, c->P, c->cellStart, float(dt), c->stream);
+        launch_forces<DIM>(c->pos, c->vel, c->vel2, c->n, c->L, c->P, c->cellStart, float(dt), c->pleft, c->stream);
         std::swap(c->vel, c->vel2);
     }
     int rc = run_projection<DIM>(c, st);
@@ -478,7 +479,7 @@ template<int DIM> int do_initialize(swc_ctx * c) {
         return SWC_BAD_ARG;
     }
     run_bin_real<DIM>(c);
-    launch_density<DIM>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->stream);
+    launch_density<DIM>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->pleft, c->stream);
     launch_set_volume(c->pos, c->rho, c->n, float(c->scene.mass), c->stream);
     // V_i per particle id (travels with the particle)
     launch_scatter_w_to_id(c->pos, c->id, c->n, c->vol_by_id, c->stream);
@@ -671,6 +672,7 @@ void swc_destroy(swc_ctx * c) {
     dfree(c->id);
     dfree(c->rho);
     dfree(c->vol_by_id);
+    dfree(c->pleft);
     dfree(c->stage);
     dfree(c->cellStart);
     free_sort(c->sortR);
@@ -778,9 +780,11 @@ int swc_set_particles(swc_ctx * c, const double * x, const double * v, int64_t n
         CK(cudaStreamSynchronize(c->stream));
         if ((rc = dalloc(c, &c->pos, n)) || (rc = dalloc(c, &c->vel, n)) || (rc = dalloc(c, &c->vel2, n)) ||
             (rc = dalloc(c, &c->id, n)) || (rc = dalloc(c, &c->rho, n)) || (rc = dalloc(c, &c->vol_by_id, n)) ||
-            (rc = dalloc(c, &c->stage, size_t(2) * std::max<int64_t>(n, 1) * c->dim)))
+            (rc = dalloc(c, &c->stage, size_t(2) * std::max<int64_t>(n, 1) * c->dim)) ||
+            (rc = dalloc(c, &c->pleft, size_t(n) / 2 + 3)))
             return rc;
         if ((rc = alloc_sort(c, c->sortR, n, false))) return rc;
+        CK(cudaMemsetAsync(c->pleft, 0, sizeof(int) * 2, c->stream));
         c->n = n;
     }
     const size_t bytes = sizeof(double) * size_t(n) * c->dim;
@@ -1124,7 +1128,7 @@ int swc_get_phase_times(swc_ctx * c, double * ms, int n) {
 }
 
 int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
-    if (!valid_ctx(c) || !mean_ms || reps <= 0 || !c->initialized) return SWC_BAD_ARG;
+    if (!valid_ctx(c) || !mean_ms || reps <= 0 || !c->initialized || which < 0 || which > 6) return SWC_BAD_ARG;
     CK(cudaStreamSynchronize(c->stream));
     // keep the solver state: run the CG kernels against a scratch copy of the scalars
     CgState saved{};
@@ -1164,8 +1168,8 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
                                             c->cellStart, c->bpos, c->bvel, c->bnrm, c->bcellStart, c->pgrid, c->queues + 2,
                                             c->stream);
                 break;
-            case 4: launch_density<3>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->stream); break;
-            case 5: launch_forces<3>(c->pos, c->vel, c->vel2, c->n, c->L, c->P, c->cellStart, 0.f, c->stream); break;
+            case 4: launch_density<3>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->pleft, c->stream); break;
+            case 5: launch_forces<3>(c->pos, c->vel, c->vel2, c->n, c->L, c->P, c->cellStart, 0.f, c->pleft, c->stream); break;
             }
         } else {
             switch (which) {
@@ -1173,7 +1177,7 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
                 launch_node_gather<2>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel,
                                       c->bcellStart, c->bnear, c->ggrid, c->queues, c->stream);
                 break;
-            case 4: launch_density<2>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->stream); break;
+            case 4: launch_density<2>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->pleft, c->stream); break;
             default: break;
             }
         }

@@ -100,6 +100,36 @@ __device__ __forceinline__ void kernel_and_grad(float r2, float inv_h, float c0,
     w   = inner ? c0 * (6.f * q * q * (q - 1.f) + 1.f) : (q < 1.f ? c0 * 2.f * t * t * t : 0.f);
     gsc = inner ? -c1 * inv_h * (3.f * q - 2.f) : (q < 1.f ? c1 * t * t * rinv : 0.f);
 }
+// Packed FP32x2 helpers (two particles or two nodes per thread).
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 max02(float2 a) { return make_float2(fmaxf(a.x, 0.f), fmaxf(a.y, 0.f)); }
+
+// Cubic spline of two squared distances in the clamped form used by the packed
+// kernels: with q = r / h, a = max(1 - q, 0) (0 where the mask is off) and
+// b = max(a - 1/2, 0),
+//   W_h = 2 c0h w,          w = a^3 - 4 b^3,
+//   -W'_h(r) / r = c1h g,   g = (a^2 - 4 b^2) / r,
+// which equals the piecewise form (q < 1/2: 1 - 6q^2 + 6q^3 and (2 - 3q)/h;
+// 1/2 <= q < 1: 2 (1 - q)^3 and (1 - q)^2 / r; 0 beyond).  ri = 1/r (r2 >= 1e-30).
+struct Spline2 {
+    float2 w, g, ri;
+};
+__device__ __forceinline__ Spline2 spline2(float2 r2, bool m0, bool m1, float inv_h) {
+    Spline2 o;
+    o.ri            = make_float2(rsqrt_n(fmaxf(r2.x, 1e-30f)), rsqrt_n(fmaxf(r2.y, 1e-30f)));
+    const float2 q  = mul2(mul2(r2, o.ri), f2(inv_h));
+    float2 a        = max02(fma2(q, f2(-1.f), f2(1.f)));
+    a               = make_float2(m0 ? a.x : 0.f, m1 ? a.y : 0.f);
+    const float2 b  = max02(add2(a, f2(-0.5f)));
+    const float2 a2 = mul2(a, a), b2 = mul2(b, b);
+    o.w             = fma2(mul2(b2, b), f2(-4.f), mul2(a2, a));
+    o.g             = mul2(fma2(b2, f2(-4.f), a2), o.ri);
+    return o;
+}
+
 __device__ __forceinline__ double kW_d(double r, double inv_h, double c0) {
     const double x = r * inv_h;
     if (x < .5) return c0 * (6 * x * x * (x - 1) + 1);
@@ -260,6 +290,113 @@ __device__ __forceinline__ void for_each_in_radius(const Lattice & L, const int 
             for (int j = b; j < e; j++) f(j);
         }
     }
+}
+
+// The same visit for two query points a and b at once (neighbours in the
+// sorted order, normally in one cell row): rows within R of either point and,
+// per row, the union of the two x-ranges, so f(j) sees every particle that
+// either single-point visit would (and a few more, which the caller's exact
+// distance tests reject).  The x reach comes from the hardware rsqrt with a
+// relative margin of 1e-5 (its error is below 3e-7).
+template<int DIM, class F>
+__device__ __forceinline__ void for_each_in_radius2(const Lattice & L, const int * __restrict__ cellStart, float3 a,
+                                                    float3 b, float R, float R2, F && f) {
+    const int cy0 = clampi(__float2int_rd((fminf(a.y, b.y) - R - L.oy) * L.inv_dx), 0, L.ny - 1);
+    const int cy1 = clampi(__float2int_rd((fmaxf(a.y, b.y) + R - L.oy) * L.inv_dx), 0, L.ny - 1);
+    int cz0 = 0, cz1 = 0;
+    if (DIM == 3) {
+        cz0 = clampi(__float2int_rd((fminf(a.z, b.z) - R - L.oz) * L.inv_dx), 0, L.nz - 1);
+        cz1 = clampi(__float2int_rd((fmaxf(a.z, b.z) + R - L.oz) * L.inv_dx), 0, L.nz - 1);
+    }
+    for (int cz = cz0; cz <= cz1; cz++) {
+        float rza = R2, rzb = R2;
+        if (DIM == 3) {
+            const float da = slab_dist(a.z, cz, L.nz, L.oz, L.dx), db = slab_dist(b.z, cz, L.nz, L.oz, L.dx);
+            rza -= da * da;
+            rzb -= db * db;
+        }
+        if (rza <= 0.f && rzb <= 0.f) continue;
+        for (int cy = cy0; cy <= cy1; cy++) {
+            const float ya = slab_dist(a.y, cy, L.ny, L.oy, L.dx), yb = slab_dist(b.y, cy, L.ny, L.oy, L.dx);
+            const float ra = rza - ya * ya, rb = rzb - yb * yb;
+            if (ra <= 0.f && rb <= 0.f) continue;
+            float lo = 3.0e38f, hi = -3.0e38f;
+            if (ra > 0.f) {
+                const float rx = ra * rsqrt_n(fmaxf(ra, 1e-30f)) * 1.00001f + 1e-6f * L.dx;
+                lo = a.x - rx;
+                hi = a.x + rx;
+            }
+            if (rb > 0.f) {
+                const float rx = rb * rsqrt_n(fmaxf(rb, 1e-30f)) * 1.00001f + 1e-6f * L.dx;
+                lo = fminf(lo, b.x - rx);
+                hi = fmaxf(hi, b.x + rx);
+            }
+            const int cx0 = clampi(__float2int_rd((lo - L.ox) * L.inv_dx), 0, L.nx - 1);
+            const int cx1 = clampi(__float2int_rd((hi - L.ox) * L.inv_dx), 0, L.nx - 1);
+            const long long row = (long long) L.nx * (cy + (long long) L.ny * cz);
+            const int jb = cellStart[row + cx0], je = cellStart[row + cx1 + 1];
+            for (int j = jb; j < je; j++) f(j);
+        }
+    }
+}
+
+// Row-parallel form of for_each_in_radius for one query point: the caller's
+// lane `lane` of `nl` visits the rows lane, lane + nl, ... of the (z, y) row
+// window (same pruning and x-ranges), so a warp walks one point's neighbours
+// about 25 times faster than a single thread (used for the few particles left
+// over by the paired kernels).
+template<int DIM, class F>
+__device__ __forceinline__ void for_rows_in_radius(const Lattice & L, const int * __restrict__ cellStart, float qx,
+                                                   float qy, float qz, float R, float R2, int lane, int nl, F && f) {
+    const int cy0 = clampi(__float2int_rd((qy - R - L.oy) * L.inv_dx), 0, L.ny - 1);
+    const int cy1 = clampi(__float2int_rd((qy + R - L.oy) * L.inv_dx), 0, L.ny - 1);
+    int cz0 = 0, cz1 = 0;
+    if (DIM == 3) {
+        cz0 = clampi(__float2int_rd((qz - R - L.oz) * L.inv_dx), 0, L.nz - 1);
+        cz1 = clampi(__float2int_rd((qz + R - L.oz) * L.inv_dx), 0, L.nz - 1);
+    }
+    const int nyr = cy1 - cy0 + 1, nrows = nyr * (cz1 - cz0 + 1);
+    for (int r = lane; r < nrows; r += nl) {
+        const int cy = cy0 + r % nyr, cz = cz0 + r / nyr;
+        const float dz = DIM == 3 ? slab_dist(qz, cz, L.nz, L.oz, L.dx) : 0.f;
+        const float dy = slab_dist(qy, cy, L.ny, L.oy, L.dx);
+        const float rem = R2 - dz * dz - dy * dy;
+        if (rem <= 0.f) continue;
+        const float rx = rem * rsqrt_n(fmaxf(rem, 1e-30f)) * 1.00001f + 1e-6f * L.dx;
+        const int cx0  = clampi(__float2int_rd((qx - rx - L.ox) * L.inv_dx), 0, L.nx - 1);
+        const int cx1  = clampi(__float2int_rd((qx + rx - L.ox) * L.inv_dx), 0, L.nx - 1);
+        const long long row = (long long) L.nx * (cy + (long long) L.ny * cz);
+        const int jb = cellStart[row + cx0], je = cellStart[row + cx1 + 1];
+        for (int j = jb; j < je; j++) f(j);
+    }
+}
+
+// Deterministic warp sum (xor butterfly; every lane gets the total).
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// End of a kernel that consumed the counter q[0]: the last block to get here
+// zeroes q[0] and the finish counter q[1], so the pair is zeroed once, at
+// allocation.  Every thread of every block calls it after its last read of q[0].
+__device__ __forceinline__ void grid_done_reset(int * q) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(q + 1, 1) == int(gridDim.x) - 1) {
+            atomicExch(q, 0);
+            atomicExch(q + 1, 0);
+        }
+    }
+}
+
+// Two consecutive sorted particles share one neighbour visit when they lie in
+// the same cell row at most one cell apart.
+template<int DIM> __device__ __forceinline__ bool near_pair(const Lattice & L, float4 a, float4 b) {
+    const int3 ca = cell_of<DIM>(L, a.x, a.y, a.z), cb = cell_of<DIM>(L, b.x, b.y, b.z);
+    return ca.y == cb.y && ca.z == cb.z && abs(ca.x - cb.x) <= 1;
 }
 
 // Friction-free wall term of the pressure-gradient update for particle

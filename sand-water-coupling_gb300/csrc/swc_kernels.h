@@ -72,12 +72,15 @@ void launch_max_positive(const float * a, long long n, int * out_bits, cudaStrea
 template<int DIM>
 void launch_bin(const Lattice & L, long long n, float4 * pos, float4 * vel, float4 * aux, int * id, SortScratch & S,
                 int * cellStart, cudaStream_t st);
+// Density and forces run one thread per pair of consecutive sorted particles;
+// `left` (n/2 + 3 ints, zeroed once at allocation) collects the pairs that are
+// not in one cell row for a second, single-particle pass.
 template<int DIM>
 void launch_density(const float4 * pos, float4 * vel, float * rho, long long n, const Lattice & L, const Phys & P,
-                    const int * cellStart, cudaStream_t st);
+                    const int * cellStart, int * left, cudaStream_t st);
 template<int DIM>
 void launch_forces(const float4 * pos, const float4 * vel, float4 * vel_out, long long n, const Lattice & L,
-                   const Phys & P, const int * cellStart, float dt, cudaStream_t st);
+                   const Phys & P, const int * cellStart, float dt, int * left, cudaStream_t st);
 template<int DIM>
 void launch_boundary_density(float4 * bpos, float4 * bvel, float * rho, long long nb, const Lattice & L,
                              const Phys & P, const int * bcellStart, cudaStream_t st);
