@@ -57,7 +57,8 @@ struct NodeSums2 {
 };
 
 // Contributions of one particle (position / volume p, velocity / m-over-rho u)
-// to two nodes at x offsets dxx = x_I - x_j (dy, dz shared, ryz = dy^2 + dz^2).
+// to two nodes at x offsets dxx = x_I - x_j (dy, dz shared), squared distances
+// r2 and masks m0 / m1 = (r2 < h^2).
 // With q = r / h, a = max(1 - q, 0) and b = max(a - 1/2, 0) the cubic spline is
 //   W_h = c0h (2 a^3 - 8 b^3) = 2 c0h w,   w = a^3 - 4 b^3,
 //   -W'_h(r) / r = (6 c0h / h) (a^2 - 4 b^2) / r = c1h g,
@@ -66,10 +67,8 @@ struct NodeSums2 {
 // truncated at h: for H >= 2h (FAST_H) only its inner branch
 // wH = 1 + 6 x^2 (x - 1), x = r / H, is reached; otherwise wH = 2 aH^3 - 8 bH^3.
 template<bool REAL, bool FAST_H>
-__device__ __forceinline__ void pair_add(NodeSums2 & s, const Phys & P, float2 dxx, float dy, float dz, float ryz,
-                                         float4 p, float4 u) {
-    const float2 r2 = fma2(dxx, dxx, f2(ryz));
-    const bool m0 = r2.x < P.h2, m1 = r2.y < P.h2;
+__device__ __forceinline__ void pair_add(NodeSums2 & s, const Phys & P, float2 dxx, float dy, float dz, float2 r2,
+                                         bool m0, bool m1, float4 p, float4 u) {
     const float2 ri = make_float2(rsqrt_n(fmaxf(r2.x, 1e-30f)), rsqrt_n(fmaxf(r2.y, 1e-30f)));
     const float2 q  = mul2(mul2(r2, ri), f2(P.inv_h));
     float2 a        = max02(fma2(q, f2(-1.f), f2(1.f)));
@@ -168,10 +167,13 @@ __global__ void __launch_bounds__(128) k_node_gather(Lattice L, Phys P, const in
                                 const float dy  = yn - p.y, dz = zn - p.z;
                                 const float ryz = dy * dy + dz * dz;
                                 if (ryz >= P.h2) continue;
-                                const float4 u    = U[j];
                                 const float2 dxx = add2(xn, f2(-p.x));
-                                if (pass == 0) pair_add<true, FAST_H>(a, P, dxx, dy, dz, ryz, p, u);
-                                else pair_add<false, FAST_H>(a, P, dxx, dy, dz, ryz, p, u);
+                                const float2 r2  = fma2(dxx, dxx, f2(ryz));
+                                const bool m0 = r2.x < P.h2, m1 = r2.y < P.h2;
+                                if (!(m0 || m1)) continue;
+                                const float4 u = U[j];
+                                if (pass == 0) pair_add<true, FAST_H>(a, P, dxx, dy, dz, r2, m0, m1, p, u);
+                                else pair_add<false, FAST_H>(a, P, dxx, dy, dz, r2, m0, m1, p, u);
                             }
                         }
                 }
