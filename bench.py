@@ -50,6 +50,12 @@ def peaks():
         return 6800.0, "fallback"
 
 
+SM_MAX_MHZ = 2070.0
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_cg_spmv launch on the
+# 128^3 block (32,769,792 B at 2,246,535 active nodes), per active node
+DRAM_BYTES_PER_NODE = {"cg_spmv": 32769792 / 2246535}
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -253,10 +259,20 @@ def run_gpu_arm(args):
     dominant = max(("cg_spmv", "virtual_gather", "pressure_gradient"),
                    key=lambda k: kern[k] * (np.mean(iters) if k == "cg_spmv" else 1))
     ach = alg[dominant] / (kern[dominant] / 1e3) / 1e9
+    # DRAM bytes (read + write) per active node of one launch, from the ncu capture of
+    # the same workload summarised in profiles/k_cg_spmv_block128.md
+    traffic = DRAM_BYTES_PER_NODE[dominant] * nv if dominant in DRAM_BYTES_PER_NODE else None
     roofline = {"kernel": dominant, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
-                "frac": ach / hbm, "peak_source": peak_kind, "traffic": None,
+                "frac": ach / hbm, "peak_source": peak_kind, "traffic": traffic,
                 "per_kernel_ms": kern, "per_kernel_GBps": {k: alg[k] / (kern[k] / 1e3) / 1e9 for k in kern},
                 "cg_iteration_ms": cg_ms}
+    if dominant == "cg_spmv":
+        # the stencil's arithmetic against the FP32 FMA roof (nominal: SMs x 128 lanes x 2 x max clock)
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        fp32_peak = sms * 128 * 2 * SM_MAX_MHZ * 1e6 / 1e12
+        flops = 2 * 250 * nv  # 250 off-diagonal taps per active row (the reference's per-row work)
+        roofline["fp32"] = {"achieved": flops / (kern["cg_spmv"] / 1e3) / 1e12, "peak": fp32_peak,
+                            "unit": "TFLOP/s", "peak_source": "nominal"}
 
     # end-to-end through the public API with pinned host buffers
     L = _lib.load()

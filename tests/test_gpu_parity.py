@@ -97,6 +97,9 @@ def test_projection_step_parity(swc_mod, oracle_mod, name):
         # the GPU pressure solves the oracle's FP64 system to the CG tolerance
         res = np.linalg.norm(ov["div"] - ref.apply_operator(gv["p"])) / np.linalg.norm(ov["div"])
         assert res < 20 * s.tolerance + 1e-5, res
+        # same Hestenes-Stiefel iteration on both sides: iteration counts agree
+        # (FP32 SpMV vs FP64 can move the crossing of the tolerance by one)
+        assert abs(st["cg_iterations"] - ref.stats()["iterations"]) <= 1, (st["cg_iterations"], ref.stats())
 
 
 @pytest.mark.parametrize("name", ["dam_break_2d", "block_3d_n16"])
