@@ -10,7 +10,11 @@ Metric: projection steps/s at 2M particles.  ``value`` is device time (CUDA
 events on the library's stream) with the state resident in HBM; ``e2e`` runs the
 same steps through the public API with host FP64 buffers (pinned), the
 host->device copy of each step's particle state and the device->host read of
-its result inside the timed region.
+its result inside the timed region.  The headline form is the learned warm
+start (the trained model in swc/models/, prediction kept without the residual
+fallback); ``forms`` reports plain CG from the node-mapped previous pressure,
+from the reference's stale prefix and from zero, and the learned start with
+the fallback, all on the same scene and steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl swc|reference]
 
@@ -39,6 +43,9 @@ import numpy as np  # noqa: E402
 
 METRIC = "projection steps/s at 2M particles (CG to 1e-5 relative residual)"
 UNIT = "steps/s"
+# learned warm start trained by swc/train_warm_start.py (dam-break variants + blocks, seeds
+# disjoint from the benchmark block's)
+MODEL = os.path.join(ROOT, "sand-water-coupling_gb300", "swc", "models", "warm_start.npz")
 
 
 def peaks():
@@ -185,7 +192,7 @@ def run_gpu_arm(args):
     import torch
 
     import swc
-    from swc import _lib, scenes
+    from swc import _lib, learn, scenes
 
     dist, rank, ws = dist_setup()
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -194,7 +201,11 @@ def run_gpu_arm(args):
     stream = torch.cuda.Stream()
 
     def make(warm):
-        liq = swc.DualParticleSphLiquid(scene, warm_start=warm, tolerance=1e-5)
+        no_fallback = warm == "learned_no_fallback"
+        mode = "learned" if no_fallback else warm
+        liq = swc.DualParticleSphLiquid(scene, warm_start=mode, tolerance=1e-5, learned_no_fallback=no_fallback)
+        if mode == "learned":
+            liq.setMlp(*learn.load_model(MODEL))
         liq.setStream(stream.cuda_stream)
         liq.initialize()
         return liq
@@ -313,7 +324,8 @@ def run_gpu_arm(args):
     # plain-CG comparison forms (same scene, same steps)
     forms = {}
     if args.compare_forms:
-        for warm in ("prefix", "node", "zero"):
+        cands = ["prefix", "node", "zero"] + (["learned", "learned_no_fallback"] if os.path.exists(MODEL) else [])
+        for warm in cands:
             if warm == args.warm_start:
                 continue
             l2 = make(warm)
@@ -363,7 +375,10 @@ def main():
     ap.add_argument("--impl", default="swc", choices=["swc", "reference"])
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--warm-start", dest="warm_start", default="node", choices=["prefix", "node", "zero", "learned"])
+    ap.add_argument("--warm-start", dest="warm_start", default="auto",
+                    choices=["auto", "prefix", "node", "zero", "learned", "learned_no_fallback"],
+                    help="auto: the learned start (prediction always kept) when the trained model is "
+                         "present, else the node-mapped previous pressure")
     ap.add_argument("--cpu-sample", dest="cpu_sample", type=int, default=48)
     ap.add_argument("--cpu-steps", dest="cpu_steps", type=int, default=3)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
@@ -371,6 +386,8 @@ def main():
     ap.add_argument("--profile-run", dest="profile_run", action="store_true",
                     help="only the timed steps (for profiler captures); prints a reduced line")
     args = ap.parse_args()
+    if args.warm_start == "auto":
+        args.warm_start = "learned_no_fallback" if os.path.exists(MODEL) else "node"
     if args.impl == "reference":
         if args.steps > 10:
             args.steps = 10  # each reference step is seconds of CPU work

@@ -75,7 +75,9 @@ typedef struct swc_solver_opts {
     int32_t keep_virtual_velocity; /* store vbar_I for swc_get_virtual */
     int32_t compute_true_residual; /* evaluate |b - A x| / |b| after each solve */
     int32_t keep_features;         /* keep per-node neighbour counts (learned warm start) */
-    int32_t reserved[2];
+    int32_t learned_no_fallback;   /* learned start: keep the prediction even when its initial
+                                      residual exceeds the node-mapped start's (evaluation) */
+    int32_t reserved[1];
 } swc_solver_opts;
 
 typedef struct swc_stats {

@@ -382,6 +382,29 @@ __global__ void __launch_bounds__(kUT) k_cg_update(const int * __restrict__ blis
 }
 
 // True residual |b - A x|^2 and |b|^2 (FP64, out2[0], out2[1]).
+// |b|^2 = sum_I D_I^2 into cg->bb (the learned start's scale sD before the
+// solve, when no fallback residual of the node-mapped start is needed).
+template<int DIM>
+__global__ void __launch_bounds__(kUT) k_rhs_norm(const int * __restrict__ blist, const int * __restrict__ bcount,
+                                                  NodeArrays N, CgState * cg, double * __restrict__ partials) {
+    using G = BrickGeom<DIM>;
+    constexpr int Q = G::BN / 4;
+    __shared__ double red[kUT / 32 + 1];
+    __shared__ int last;
+    const long long total = (long long) (*bcount) * Q;
+    FF bb{0.f, 0.f};
+    for (long long i = blockIdx.x * (long long) kUT + threadIdx.x; i < total; i += (long long) gridDim.x * kUT) {
+        const float4 d = ld4(N.D, (long long) blist[i / Q] * G::BN + 4 * (i % Q));
+        ff_add_prod(bb, d.x, d.x);
+        ff_add_prod(bb, d.y, d.y);
+        ff_add_prod(bb, d.z, d.z);
+        ff_add_prod(bb, d.w, d.w);
+    }
+    double part[1] = {block_sum_ff<kUT>(bb, red)};
+    double tot[1];
+    if (grid_reduce<kUT, 1>(part, partials, &cg->ticket[3], tot, red, &last) && threadIdx.x == 0) cg->bb = tot[0];
+}
+
 template<int DIM>
 __global__ void __launch_bounds__(KG<DIM>::BT) k_true_residual(Lattice L, const int * __restrict__ blist,
                                                                const int * __restrict__ bcount,
@@ -475,6 +498,11 @@ void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeAr
                           CgState * cg, double * partials, double * out2, int sgrid, cudaStream_t st) {
     k_true_residual<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, B.list, B.count, B.flag, N, S, cg, partials, out2);
 }
+template<int DIM>
+void launch_rhs_norm(const BrickArrays & B, const NodeArrays & N, CgState * cg, double * partials, int ugrid,
+                     cudaStream_t st) {
+    k_rhs_norm<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N, cg, partials);
+}
 
 #define SWC_INST(D)                                                                                                    \
     template void launch_ahat<D>(const Lattice &, const Phys &, const BrickArrays &, const NodeArrays &,               \
@@ -491,7 +519,8 @@ void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeAr
                                          CgState *, double *, int, int, cudaStream_t);                                 \
     template void launch_true_residual<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,   \
                                           CgState *, double *, double *, int, cudaStream_t);                           \
-    template int cg_spmv_blocks_per_sm<D>();
+    template int cg_spmv_blocks_per_sm<D>();                                                                           \
+    template void launch_rhs_norm<D>(const BrickArrays &, const NodeArrays &, CgState *, double *, int, cudaStream_t);
 SWC_INST(2)
 SWC_INST(3)
 #undef SWC_INST

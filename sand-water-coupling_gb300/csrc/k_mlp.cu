@@ -99,9 +99,17 @@ __device__ __forceinline__ uint32_t canon_off(int r, int k, int kdim) {
     return uint32_t((r >> 3) * (kdim / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+// sigma(z) = (1 + tanh(z/2)) / 2 with the hardware tanh approximation (relative
+// error about 2^-11, below the bf16 rounding the activations go through);
+// silu(z) = z sigma(z), silu'(z) = sigma(z) (1 + z (1 - sigma(z))).
+__device__ __forceinline__ float sigmoid_fast(float z) {
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
+    return fmaf(0.5f, t, 0.5f);
+}
+__device__ __forceinline__ float silu(float z) { return z * sigmoid_fast(z); }
 __device__ __forceinline__ float dsilu(float z) {
-    const float s = 1.f / (1.f + __expf(-z));
+    const float s = sigmoid_fast(z);
     return s * (1.f + z * (1.f - s));
 }
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
@@ -201,23 +209,34 @@ __global__ void __launch_bounds__(kMlpNT) k_mlp_forward(int mode, long long n, c
     }
     uint32_t phase = 0;
     const long long ntiles = (rows + kMlpNT - 1) / kMlpNT;
+    // features of a tile row (raw; gathered through slot_of in node mode)
+    auto gather = [&](long long r, float (&g)[6], long long & gs) {
+#pragma unroll
+        for (int k = 0; k < 6; k++) g[k] = 0.f;
+        gs = 0;
+        if (r >= rows) return;
+        if (mode == kMlpFromArray) {
+#pragma unroll
+            for (int k = 0; k < 6; k++) g[k] = feat[r * 6 + k];
+        } else {
+            gs = slot_of[r];
+            node_features(N, gs, F, g);
+        }
+    };
+    // the next tile's gathers are issued before this tile's MMAs are waited on
+    float fn[6];
+    long long sn = 0;
+    gather(blockIdx.x * (long long) kMlpNT + tid, fn, sn);
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const long long row = tile * kMlpNT + tid;
         const bool valid    = row < rows;
-        float f[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        long long s = 0;
-        if (valid) {
-            if (mode == kMlpFromArray) {
+        float f[6];
 #pragma unroll
-                for (int k = 0; k < 6; k++) f[k] = feat[row * 6 + k];
-            } else {
-                s = slot_of[row];
-                node_features(N, s, F, f);
-                if (feat_out) {
+        for (int k = 0; k < 6; k++) f[k] = fn[k];
+        const long long s = sn;
+        if (valid && mode != kMlpFromArray && feat_out) {
 #pragma unroll
-                    for (int k = 0; k < 6; k++) feat_out[row * 6 + k] = f[k];
-                }
-            }
+            for (int k = 0; k < 6; k++) feat_out[row * 6 + k] = f[k];
         }
         // X row: normalised features in bf16, K padded to 16
         float xn[6];
@@ -234,6 +253,7 @@ __global__ void __launch_bounds__(kMlpNT) k_mlp_forward(int mode, long long n, c
             mma_bf16(tbase, dX, dW1, kIdescM128N64, 0u);
             mma_commit(&mbar);
         }
+        gather((tile + gridDim.x) * kMlpNT + tid, fn, sn);
         if (!mbar_wait(&mbar, phase)) s_fail = 1;
         phase ^= 1u;
         tc_fence_after();

@@ -24,6 +24,8 @@ struct HostCg {
     CgState st;
     int     nv;
     int     nbricks;
+    double  rr_node;  // initial |r|^2 of the node-mapped start (learned-start fallback test)
+    int     mlp_err;
 };
 
 }  // namespace
@@ -361,9 +363,16 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
         launch_warm_start<DIM>(c->L, c->B, c->N, kWarmNode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
         CK(cudaMemcpyAsync(c->xprev, c->N.x, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
         launch_slot_of<DIM>(c->L, c->B, c->N, c->slot_of, c->grid, c->stream);
-        int rc = cg_init_sync<DIM>(c);  // |b|^2 for sD, initial residual of the node-mapped start
-        if (rc) return rc;
-        const double rr_node = c->hcg->st.rr0;
+        // |b|^2 for sD and (for the fallback test) the initial residual of the
+        // node-mapped start, read back with the learned start's (one host synchronisation)
+        const bool no_fallback = learned && c->opts.learned_no_fallback && !logging;
+        if (no_fallback) launch_rhs_norm<DIM>(c->B, c->N, c->cg, c->partials, c->grid, c->stream);
+        else {
+            launch_cg_init<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->opts.tolerance, c->opts.max_iterations,
+                                nv, c->rgrid, c->stream);
+            CK(cudaMemcpyAsync(&c->hcg->rr_node, &c->cg->rr0, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        }
+        int rc = SWC_OK;
         const float inv_a0 = float(1.0 / c->alpha0), inv_r0 = float(1.0 / c->rho0), inv_nr = 1.f / 32.f,
                     inv_nv = DIM == 3 ? 1.f / 251.f : 1.f / 45.f;
         if (logging)
@@ -371,12 +380,12 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
                                  c->feat_buf, c->stream);
         if (learned) {
             launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->slot_of, nv, c->cg, inv_a0, inv_r0, inv_nr,
-                                     inv_nv, nullptr, c->mlp_err, c->num_sms * 2, c->stream);
+                                     inv_nv, nullptr, c->mlp_err, c->num_sms * 4, c->stream);  // 4 x 128 TMEM columns per SM
+            CK(cudaMemcpyAsync(&c->hcg->mlp_err, c->mlp_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
             if ((rc = cg_init_sync<DIM>(c))) return rc;
-            int err = 0;
-            CK(cudaMemcpy(&err, c->mlp_err, sizeof(int), cudaMemcpyDeviceToHost));
-            const double rr_mlp = c->hcg->st.rr0;
-            if (err || !(rr_mlp <= rr_node)) {
+            const int err        = c->hcg->mlp_err;
+            const double rr_node = c->hcg->rr_node, rr_mlp = c->hcg->st.rr0;
+            if (err || !(rr_mlp == rr_mlp) || (!c->opts.learned_no_fallback && !(rr_mlp <= rr_node))) {
                 // the prediction starts from a larger residual (or failed): keep the node-mapped start
                 CK(cudaMemcpyAsync(c->N.x, c->xprev, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
                 if ((rc = cg_init_sync<DIM>(c))) return rc;
@@ -384,6 +393,7 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
             } else used = SWC_WARM_LEARNED;
             initialized = true;
         } else if (mode == SWC_WARM_NODE || mode == SWC_WARM_LEARNED) {
+            if ((rc = cg_init_sync<DIM>(c))) return rc;  // host copy of the node-mapped start's state
             initialized = true;
         } else {
             launch_warm_start<DIM>(c->L, c->B, c->N, mode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);

@@ -155,6 +155,9 @@ template<int DIM>
 void launch_compact_import(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const double * in,
                            float * out, int grid, cudaStream_t st);
 template<int DIM>
+void launch_rhs_norm(const BrickArrays & B, const NodeArrays & N, CgState * cg, double * partials, int ugrid,
+                     cudaStream_t st);
+template<int DIM>
 void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
                           CgState * cg, double * partials, double * out2, int sgrid, cudaStream_t st);
 

@@ -50,7 +50,8 @@ class SolverOpts(C.Structure):
         ("keep_virtual_velocity", C.c_int32),
         ("compute_true_residual", C.c_int32),
         ("keep_features", C.c_int32),
-        ("reserved", C.c_int32 * 2),
+        ("learned_no_fallback", C.c_int32),
+        ("reserved", C.c_int32 * 1),
     ]
 
 

@@ -41,7 +41,8 @@ def _f64(a, shape=None):
 
 class DualParticleSphLiquid:
     def __init__(self, scene, tolerance=None, max_iterations=-1, warm_start="prefix", keep_virtual_velocity=False,
-                 compute_true_residual=False, keep_features=False, check_interval=0, raise_on_nonconvergence=False):
+                 compute_true_residual=False, keep_features=False, check_interval=0, raise_on_nonconvergence=False,
+                 learned_no_fallback=False):
         self.L = _lib.load()
         self.scene = scene
         self.dim = scene.dim
@@ -68,6 +69,7 @@ class DualParticleSphLiquid:
         o.keep_virtual_velocity = 1 if keep_virtual_velocity else 0
         o.compute_true_residual = 1 if compute_true_residual else 0
         o.keep_features = 1 if keep_features else 0
+        o.learned_no_fallback = 1 if learned_no_fallback else 0
         self._opts = o
         self._scene_c = s
         h = C.c_void_p()
