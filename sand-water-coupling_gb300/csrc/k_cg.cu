@@ -215,6 +215,7 @@ __global__ void __launch_bounds__(kUT) k_cg_direction(const int * __restrict__ b
                                                       NodeArrays N, const CgState * __restrict__ cg) {
     using G = BrickGeom<DIM>;
     constexpr int Q = G::BN / 4;
+    pdl_wait_and_release();
     if (cg->done) return;
     const int it     = cg->iter;
     const float beta = it == 0 ? 0.f : float(cg->rr / cg->rr_prev);
@@ -281,7 +282,10 @@ __device__ __forceinline__ void prefetch_u_tile(const int * tab, const float * _
 }
 
 // Iteration part 1: q = A d_i and pq = d_i . q.  The u = V d tile of the next
-// brick is copied asynchronously while the current one is computed.
+// brick is copied asynchronously while the current one is computed.  The grid
+// is the resident capacity and bricks are strided statically over it (a
+// dynamic brick queue with per-brick partials measured slower: its atomics and
+// per-brick block reductions cost more than the tail it removes).
 template<int DIM>
 __global__ void __launch_bounds__(KG<DIM>::BT) k_cg_spmv(Lattice L, const int * __restrict__ blist,
                                                          const int * __restrict__ bcount,
@@ -294,6 +298,7 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_cg_spmv(Lattice L, const int * 
     __shared__ int tab[2][27];
     __shared__ double red[BT / 32 + 1];
     __shared__ int last;
+    pdl_wait_and_release();
     if (cg->done) return;
     const int nb = *bcount;
     const int t = threadIdx.x, ly = t % G::BY, lz = t / G::BY;
@@ -350,6 +355,7 @@ __global__ void __launch_bounds__(kUT) k_cg_update(const int * __restrict__ blis
     constexpr int Q = G::BN / 4;
     __shared__ double red[kUT / 32 + 1];
     __shared__ int last;
+    pdl_wait_and_release();
     if (cg->done) return;
     const int it      = cg->iter;
     const float alpha = float(cg->rr / cg->pq);
@@ -467,12 +473,34 @@ void launch_cg_init(const Lattice & L, const BrickArrays & B, const NodeArrays &
     k_cg_init<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, B.list, B.count, B.flag, N, S, cg, partials, tol, max_iterations,
                                                   nv);
 }
+// Launch with programmatic stream serialization: the kernel's blocks may be
+// dispatched while the previous kernel on the stream drains; the kernel itself
+// waits (pdl_wait_and_release) before touching its inputs.
+template<class Kern, class... Args>
+static void launch_pdl(Kern kernel, int grid, int block, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim          = dim3(unsigned(grid));
+    cfg.blockDim         = dim3(unsigned(block));
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream           = st;
+    cudaLaunchAttribute at[1];
+    at[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs    = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template<int DIM>
 void launch_cg_spmv(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
                     double * partials, int sgrid, cudaStream_t st) {
-    k_cg_spmv<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, B.list, B.count, B.flag, N, S, cg, partials);
+    launch_pdl(k_cg_spmv<DIM>, sgrid, KG<DIM>::BT, st, L, (const int *) B.list, (const int *) B.count,
+               (const unsigned char *) B.flag, N, S, cg, partials);
 }
 template<int DIM> int cg_spmv_blocks_per_sm() {
+    // all of the unified L1 / shared memory as shared memory: the SpMV keeps no
+    // data in L1 worth more than a seventh resident block
+    cudaFuncSetAttribute(k_cg_spmv<DIM>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cg_spmv<DIM>, KG<DIM>::BT, 0) != cudaSuccess) n = 1;
     return n > 0 ? n : 1;
@@ -480,11 +508,11 @@ template<int DIM> int cg_spmv_blocks_per_sm() {
 template<int DIM>
 void launch_cg_update(const BrickArrays & B, const NodeArrays & N, CgState * cg, double * partials, int ugrid,
                       cudaStream_t st) {
-    k_cg_update<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N, cg, partials);
+    launch_pdl(k_cg_update<DIM>, ugrid, kUT, st, (const int *) B.list, (const int *) B.count, N, cg, partials);
 }
 template<int DIM>
 void launch_cg_direction(const BrickArrays & B, const NodeArrays & N, const CgState * cg, int ugrid, cudaStream_t st) {
-    k_cg_direction<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N, cg);
+    launch_pdl(k_cg_direction<DIM>, ugrid, kUT, st, (const int *) B.list, (const int *) B.count, N, cg);
 }
 template<int DIM>
 void launch_cg_iteration(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,

@@ -63,6 +63,15 @@ struct Phys {
     int   gravity_on;
 };
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization waits here until the preceding kernel's memory is visible
+// (a no-op for an ordinary launch), then lets the next kernel's blocks be
+// dispatched while it runs, which hides the launch gap between short kernels.
+__device__ __forceinline__ void pdl_wait_and_release() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // 1/sqrt(x) for normal x (every caller clamps x >= 1e-30): the hardware
 // approximation without the rescaling of denormal inputs that rsqrtf adds.
 __device__ __forceinline__ float rsqrt_n(float x) {

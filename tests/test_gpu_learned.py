@@ -88,3 +88,35 @@ def test_learned_warm_start_end_to_end(swc_mod):
     # the residual-based fallback never starts from a worse residual than the plain solver
     assert it_learn[1:].mean() <= it_node[1:].mean() + 1.0
     print(f"\nCG iterations  node-mapped: {it_node.tolist()}  learned: {it_learn.tolist()}  used: {used}")
+
+
+def test_committed_model_without_fallback(swc_mod):
+    """The shipped model (swc/models/warm_start.npz) drives CG on a held-out block
+    with the prediction always kept: same solution as the node-mapped start, and
+    the learned start is the one used on every step."""
+    import os
+
+    from swc import learn
+
+    path = os.path.join(os.path.dirname(learn.__file__), "models", "warm_start.npz")
+    p, q = learn.load_model(path)
+    sc = scenes.projection_block_3d(n=32, seed=77).rounded_to_float32()
+    out = {}
+    for mode in ("node", "learned"):
+        liq = swc_mod.DualParticleSphLiquid(sc, warm_start=mode, compute_true_residual=True,
+                                            learned_no_fallback=True)
+        if mode == "learned":
+            liq.setMlp(p, q)
+        liq.initialize()
+        its, used = [], []
+        for _ in range(6):
+            st = liq.advance(sc.dt)
+            assert st["status"] == 0 and st["true_rel_residual"] < 5 * sc.tolerance
+            its.append(st["cg_iterations"])
+            used.append(st["warm_start_used"])
+        out[mode] = (liq.getParticles()[1], its, used)
+        liq.close()
+    assert all(u == 3 for u in out["learned"][2])  # SWC_WARM_LEARNED
+    v_node, v_learn = out["node"][0], out["learned"][0]
+    assert np.linalg.norm(v_learn - v_node) / np.linalg.norm(v_node) < 1e-4
+    print(f"\nCG iterations  node-mapped: {out['node'][1]}  learned (kept): {out['learned'][1]}")
