@@ -158,24 +158,39 @@ __global__ void __launch_bounds__(128) k_node_gather(Lattice L, Phys P, const in
                     const int * cs   = pass == 0 ? cellStart : bcellStart;
                     const float4 * X = pass == 0 ? pos : bpos;
                     const float4 * U = pass == 0 ? vel : bvel;
-                    for (int cz = cz0; cz <= cz1; cz++)
-                        for (int cy = cy0; cy <= cy1; cy++) {
-                            const long long row = (long long) L.nx * (cy + (long long) L.ny * cz);
-                            const int jb = cs[row + cxa], je = cs[row + cxb + 1];
-                            for (int j = jb; j < je; j++) {
-                                const float4 p  = X[j];
-                                const float dy  = yn - p.y, dz = zn - p.z;
-                                const float ryz = dy * dy + dz * dz;
-                                if (ryz >= P.h2) continue;
-                                const float2 dxx = add2(xn, f2(-p.x));
-                                const float2 r2  = fma2(dxx, dxx, f2(ryz));
-                                const bool m0 = r2.x < P.h2, m1 = r2.y < P.h2;
-                                if (!(m0 || m1)) continue;
-                                const float4 u = U[j];
-                                if (pass == 0) pair_add<true, FAST_H>(a, P, dxx, dy, dz, r2, m0, m1, p, u);
-                                else pair_add<false, FAST_H>(a, P, dxx, dy, dz, r2, m0, m1, p, u);
-                            }
+                    // cell rows (cy, cz) in order; the next row's range and the next
+                    // candidate's position / velocity are loaded one step ahead
+                    int cy = cy0, cz = cz0;
+                    long long row = (long long) L.nx * (cy + (long long) L.ny * cz);
+                    int jb = cs[row + cxa], je = cs[row + cxb + 1];
+                    for (;;) {
+                        int ny = cy + 1, nz = cz;
+                        if (ny > cy1) ny = cy0, nz++;
+                        const bool more = nz <= cz1;
+                        int nb_ = 0, ne_ = 0;
+                        if (more) {
+                            const long long nrow = (long long) L.nx * (ny + (long long) L.ny * nz);
+                            nb_ = cs[nrow + cxa];
+                            ne_ = cs[nrow + cxb + 1];
                         }
+                        float4 pn = make_float4(0.f, 0.f, 0.f, 0.f), un = pn;
+                        if (jb < je) pn = X[jb], un = U[jb];
+                        for (int j = jb; j < je; j++) {
+                            const float4 p = pn, u = un;
+                            if (j + 1 < je) pn = X[j + 1], un = U[j + 1];
+                            const float dy  = yn - p.y, dz = zn - p.z;
+                            const float ryz = dy * dy + dz * dz;
+                            if (ryz >= P.h2) continue;
+                            const float2 dxx = add2(xn, f2(-p.x));
+                            const float2 r2  = fma2(dxx, dxx, f2(ryz));
+                            const bool m0 = r2.x < P.h2, m1 = r2.y < P.h2;
+                            if (!(m0 || m1)) continue;
+                            if (pass == 0) pair_add<true, FAST_H>(a, P, dxx, dy, dz, r2, m0, m1, p, u);
+                            else pair_add<false, FAST_H>(a, P, dxx, dy, dz, r2, m0, m1, p, u);
+                        }
+                        if (!more) break;
+                        cy = ny, cz = nz, jb = nb_, je = ne_;
+                    }
                 }
             }
 #pragma unroll
