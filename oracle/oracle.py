@@ -61,6 +61,7 @@ def lib():
         L.orc_set_particles.argtypes = [P, C.c_int64, D, D]
         L.orc_get_particles.argtypes = [P, D, D]
         L.orc_set_boundary.argtypes = [P, C.c_int64, D, D, D]
+        L.orc_set_boundary_motion.argtypes = [P, C.POINTER(C.c_uint8), D, C.c_double]
         for n in ("orc_initialize", "orc_project", "orc_compute_densities"):
             getattr(L, n).argtypes = [P]
         L.orc_advance.argtypes = [P, C.c_double]
@@ -156,6 +157,14 @@ class Oracle:
         v = np.ascontiguousarray(v, dtype=np.float64)
         self.nb = x.shape[0]
         lib().orc_set_boundary(self.h, self.nb, _dp(x), _dp(nrm), _dp(v))
+
+    def set_boundary_motion(self, moving, center, omega):
+        """Rigid rotation of the flagged boundary particles about the vertical axis
+        through `center` at `omega` rad/s, applied at the start of every advance."""
+        m = np.ascontiguousarray(moving, dtype=np.uint8)
+        assert m.shape[0] == self.nb
+        c = np.ascontiguousarray(np.asarray(center, dtype=np.float64).reshape(-1)[:3])
+        lib().orc_set_boundary_motion(self.h, m.ctypes.data_as(C.POINTER(C.c_uint8)), _dp(c), float(omega))
 
     def particles(self):
         x = np.zeros((self.n, self.dim))

@@ -529,8 +529,36 @@ template<int D> struct Oracle {
         pres.clear();
     }
 
+    // Moving solids (the paddle-tank extension; the reference's boundary is static
+    // after initialize): flagged boundary particles turn rigidly by -omega dt about
+    // the vertical (y) axis through c, their normals with them, v_b = omega x
+    // (x_b - c) in the scene's convention (v_x = omega r_z, v_z = -omega r_x);
+    // the boundary grid is rebuilt and V_b keeps its initial value.
+    std::vector<unsigned char> moving;
+    double motionC[3] = {0, 0, 0}, omega = 0;
+    bool hasMotion = false;
+    void moveBoundary(double dt) {
+        if constexpr (D == 3) {
+            const double ca = std::cos(omega * dt), sa = std::sin(omega * dt);
+            for (size_t i = 0; i < xb.size(); i++) {
+                if (!moving[i]) continue;
+                const double rx = xb[i][0] - motionC[0], rz = xb[i][2] - motionC[2];
+                const double nx = rx * ca + rz * sa, nz = -rx * sa + rz * ca;
+                xb[i][0]        = motionC[0] + nx;
+                xb[i][2]        = motionC[2] + nz;
+                const double mx = nb[i][0] * ca + nb[i][2] * sa, mz = -nb[i][0] * sa + nb[i][2] * ca;
+                nb[i][0]        = mx;
+                nb[i][2]        = mz;
+                vb[i][0]        = omega * nz;
+                vb[i][2]        = -omega * nx;
+            }
+            sBnd.reset(xb);
+        }
+    }
+
     // DualParticleSphLiquid::advance (DualParticleSphLiquid.cpp:112-126).
     void advance(double dt) {
+        if (hasMotion) moveBoundary(dt);
         moveParticles(dt);
         applyExternalForces(dt);
         applyViscosityForce(dt);
@@ -610,6 +638,14 @@ void orc_set_boundary(Handle * h, int64_t n, const double * x, const double * nr
         orc::loadVecs<D>(O.xb, x, n);
         orc::loadVecs<D>(O.nb, nrm, n);
         orc::loadVecs<D>(O.vb, v, n);
+    });
+}
+void orc_set_boundary_motion(Handle * h, const unsigned char * moving, const double * center, double omega) {
+    DISPATCH(h, {
+        O.moving.assign(moving, moving + O.xb.size());
+        for (int a = 0; a < 3; a++) O.motionC[a] = center[a];
+        O.omega     = omega;
+        O.hasMotion = true;
     });
 }
 void orc_initialize(Handle * h) { DISPATCH(h, O.initialize()); }

@@ -53,6 +53,14 @@ __global__ void k_export_scalar(const float * __restrict__ a, int stride, int co
         out[id[s]] = a[s * stride + comp];
 }
 
+// out[id] = num / a[slot * stride + comp] (a density from a stored m / rho that
+// travels with the particle through every re-sort).
+__global__ void k_export_ratio(const float * __restrict__ a, int stride, int comp, float num,
+                               const int * __restrict__ id, long long n, double * __restrict__ out) {
+    for (long long s = blockIdx.x * (long long) blockDim.x + threadIdx.x; s < n; s += (long long) gridDim.x * blockDim.x)
+        out[id[s]] = double(num) / double(a[s * stride + comp]);
+}
+
 // x += v dt  (SmthParticleHydrodLiquid::moveParticles, Cores/Physics/SmthParticleHydrodLiquid.cpp:72-76).
 __global__ void k_advect(float4 * __restrict__ pos, const float4 * __restrict__ vel, long long n, float dt) {
     for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
@@ -621,6 +629,10 @@ void launch_export(const float4 * pos, const float4 * vel, const int * id, int d
 void launch_export_scalar(const float * a, int stride, int comp, const int * id, long long n, double * out,
                           cudaStream_t st) {
     if (n > 0) k_export_scalar<<<grid_for(n, 256), 256, 0, st>>>(a, stride, comp, id, n, out);
+}
+void launch_export_ratio(const float * a, int stride, int comp, float num, const int * id, long long n, double * out,
+                         cudaStream_t st) {
+    if (n > 0) k_export_ratio<<<grid_for(n, 256), 256, 0, st>>>(a, stride, comp, num, id, n, out);
 }
 void launch_advect(float4 * pos, const float4 * vel, long long n, float dt, cudaStream_t st) {
     if (n > 0) k_advect<<<grid_for(n, 256), 256, 0, st>>>(pos, vel, n, dt);

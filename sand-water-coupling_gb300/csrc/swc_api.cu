@@ -923,7 +923,10 @@ int swc_get_boundary_info(swc_ctx * c, double * rho, double * vol, int64_t nb) {
     if (nb == 0) return SWC_OK;
     double * s0 = c->bstage;
     double * s1 = c->bstage + size_t(nb) * c->dim;
-    if (rho) launch_export_scalar(c->brho, 1, 0, c->bid, nb, s0, c->stream);
+    // rho_b = m_b / (m_b / rho_b): bvel.w travels through the boundary re-sorts of
+    // moving solids, a separate per-slot rho array would not
+    if (rho)
+        launch_export_ratio(reinterpret_cast<const float *>(c->bvel), 4, 3, c->P.bmass, c->bid, nb, s0, c->stream);
     if (vol) launch_export_scalar(reinterpret_cast<const float *>(c->bpos), 4, 3, c->bid, nb, s1, c->stream);
     if (rho) CK(cudaMemcpyAsync(rho, s0, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
     if (vol) CK(cudaMemcpyAsync(vol, s1, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));

@@ -57,6 +57,8 @@ void launch_export(const float4 * pos, const float4 * vel, const int * id, int d
                    double * v, cudaStream_t st);
 void launch_export_scalar(const float * a, int stride, int comp, const int * id, long long n, double * out,
                           cudaStream_t st);
+void launch_export_ratio(const float * a, int stride, int comp, float num, const int * id, long long n, double * out,
+                         cudaStream_t st);
 void launch_advect(float4 * pos, const float4 * vel, long long n, float dt, cudaStream_t st);
 void launch_scan(const int * in, long long n, int * out, int * tile_buf, cudaStream_t st);
 long long scan_tile_count(long long n);
