@@ -73,27 +73,37 @@ class ClockSampler:
         self._t = None
 
     def _run(self):
+        # one nvidia-smi in loop mode (50 ms period), read line by line until stopped
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
-                                     timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([x.strip() for x in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                           "--format=csv,noheader,nounits", "-lms", "50"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            return
+        for line in self._proc.stdout:
+            if self._stop.is_set():
+                break
+            line = line.strip()
+            if line:
+                self.samples.append([x.strip() for x in line.split(",")])
 
     def __enter__(self):
+        self._proc = None
         self._t = threading.Thread(target=self._run, daemon=True)
         self._t.start()
         return self
 
     def __exit__(self, *a):
         self._stop.set()
+        if self._proc is not None:
+            self._proc.terminate()  # our own child process, by handle
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
         self._t.join(timeout=10)
 
     def summary(self):
@@ -285,7 +295,9 @@ def run_gpu_arm(args):
         roofline["fp32"] = {"achieved": flops / (kern["cg_spmv"] / 1e3) / 1e12, "peak": fp32_peak,
                             "unit": "TFLOP/s", "peak_source": "nominal"}
 
-    # end-to-end through the public API with pinned host buffers
+    # end-to-end through the public API with pinned host buffers, on a fresh
+    # context over the same steps as the device-resident measurement (the state
+    # evolves, so later steps are a different workload)
     L = _lib.load()
     dim = 3
     nbytes = n * dim * 8
@@ -293,31 +305,35 @@ def run_gpu_arm(args):
     hv_p = L.swc_host_alloc(nbytes)
     hx = np.frombuffer((C.c_double * (n * dim)).from_address(hx_p), dtype=np.float64).reshape(n, dim)
     hv = np.frombuffer((C.c_double * (n * dim)).from_address(hv_p), dtype=np.float64).reshape(n, dim)
-    x0, v0 = liq.getParticles()
+    le = make(args.warm_start)
+    x0, v0 = le.getParticles()
     hx[:] = x0
     hv[:] = v0
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
     stt = _lib.Stats()
-    for _ in range(2):
-        L.swc_set_particles(liq.h, dp(hx), dp(hv), n)
-        L.swc_advance(liq.h, scene.dt, C.byref(stt))
-        L.swc_get_particles(liq.h, dp(hx), dp(hv), n)
+
+    def e2e_step():
+        rc = L.swc_set_particles(le.h, dp(hx), dp(hv), n)
+        rc |= L.swc_advance(le.h, scene.dt, C.byref(stt))
+        rc |= L.swc_get_particles(le.h, dp(hx), dp(hv), n)
+        if rc:
+            raise RuntimeError("e2e step failed")
+
+    for _ in range(args.warmup):
+        e2e_step()
     torch.cuda.synchronize()
     barrier(dist)
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     for _ in range(args.steps):
-        rc = L.swc_set_particles(liq.h, dp(hx), dp(hv), n)
-        rc |= L.swc_advance(liq.h, scene.dt, C.byref(stt))
-        rc |= L.swc_get_particles(liq.h, dp(hx), dp(hv), n)
-        if rc:
-            raise RuntimeError("e2e step failed")
+        e2e_step()
     f1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = reduce_max(dist, f0.elapsed_time(f1))
     e2e = {"value": ws * args.steps / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
            "d2h_bytes_per_step": 2 * nbytes}
+    le.close()
     L.swc_host_free(hx_p)
     L.swc_host_free(hv_p)
 
@@ -370,6 +386,8 @@ def run_gpu_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
+    # the benchmark configuration: 50 repetitions of advect + projection (the
+    # state evolves, so the step count is part of the workload)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="swc", choices=["swc", "reference"])
