@@ -265,6 +265,8 @@ def run_gpu_arm(args):
     for which, name in ((6, "cg_direction"), (0, "cg_spmv"), (1, "cg_update"), (2, "virtual_gather"),
                         (3, "pressure_gradient"), (4, "density"), (5, "forces")):
         kern[name] = liq.timeKernel(which, 20)
+    if args.warm_start.startswith("learned"):
+        kern["mlp_forward"] = liq.timeKernel(7, 20)
     n, nb = scene.n_particles, scene.n_boundary
     # algorithmic bytes per launch (each array touched once per pass)
     alg = {
@@ -275,6 +277,7 @@ def run_gpu_arm(args):
         "pressure_gradient": 32 * n + 8 * nv + 48 * nb,  # pos, vel r/w; V, p; boundary pos/vel/nrm
         "density": 16 * n + 4 * n + 4 * n,
         "forces": 32 * n + 16 * n,
+        "mlp_forward": 28 * nv,  # slot_of, D, alpha_hat, n_real, n_virt, p_prev, rho read; p0 written
     }
     cg_ms = kern["cg_direction"] + kern["cg_spmv"] + kern["cg_update"]
     dominant = max(("cg_spmv", "virtual_gather", "pressure_gradient"),
@@ -340,7 +343,8 @@ def run_gpu_arm(args):
     # plain-CG comparison forms (same scene, same steps)
     forms = {}
     if args.compare_forms:
-        cands = ["prefix", "node", "zero"] + (["learned", "learned_no_fallback"] if os.path.exists(MODEL) else [])
+        cands = ["prefix", "node", "zero", "extrapolate"] + (["learned", "learned_no_fallback"]
+                                                             if os.path.exists(MODEL) else [])
         for warm in cands:
             if warm == args.warm_start:
                 continue
@@ -394,7 +398,7 @@ def main():
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--warm-start", dest="warm_start", default="auto",
-                    choices=["auto", "prefix", "node", "zero", "learned", "learned_no_fallback"],
+                    choices=["auto", "prefix", "node", "zero", "extrapolate", "learned", "learned_no_fallback"],
                     help="auto: the learned start (prediction always kept) when the trained model is "
                          "present, else the node-mapped previous pressure")
     ap.add_argument("--cpu-sample", dest="cpu_sample", type=int, default=48)

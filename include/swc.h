@@ -44,7 +44,9 @@ typedef enum swc_warm_start {
     SWC_WARM_PREFIX  = 0, /* reference: previous pressure vector by position in the active list */
     SWC_WARM_NODE    = 1, /* previous pressure of the same lattice node (0 for new nodes) */
     SWC_WARM_ZERO    = 2,
-    SWC_WARM_LEARNED = 3  /* MLP prediction; falls back to NODE when its initial residual is larger */
+    SWC_WARM_LEARNED = 3, /* MLP prediction; falls back to NODE when its initial residual is larger */
+    SWC_WARM_EXTRAPOLATE = 4 /* 2 p_{n-1} - p_{n-2} of the same lattice node (NODE where the node or the
+                                history is new; the history spans consecutive swc_advance calls) */
 } swc_warm_start;
 
 typedef struct swc_ctx swc_ctx;
@@ -166,7 +168,8 @@ int swc_set_profiling(swc_ctx * ctx, int on);
 int swc_get_phase_times(swc_ctx * ctx, double * ms, int n);
 /* Times `reps` back-to-back launches of one kernel on the live state with CUDA
  * events (0: CG SpMV, 1: CG update, 2: virtual gather, 3: pressure gradient,
- * 4: density, 5: forces, 6: CG direction update); writes the mean ms per launch. */
+ * 4: density, 5: forces, 6: CG direction update, 7: learned warm-start forward
+ * pass, after a projection that used it); writes the mean ms per launch. */
 int swc_time_kernel(swc_ctx * ctx, int which, int reps, double * mean_ms);
 
 /* ---- Learned CG warm start (no counterpart in the reference) -------------

@@ -7,7 +7,7 @@
 // Forward pass on the 5th-generation tensor cores: M = 128 rows (nodes) per tile,
 // BF16 operands staged in shared memory in the K-major no-swizzle canonical
 // layout (8-row x 16-byte core matrices), tcgen05.mma kind::f16 issued by one
-// thread with FP32 accumulators in TMEM (64 + 64 columns), completion tracked by
+// thread with FP32 accumulators in TMEM (64 columns, reused by both layers), completion tracked by
 // an mbarrier, accumulators read back with tcgen05.ld for the FP32 epilogues
 // (bias, SiLU, final 64-wide dot).  Every wait is bounded: on timeout the kernel
 // records an error, frees its TMEM and returns.
@@ -15,6 +15,9 @@
 // Training: the same forward kernel (saving pre-activations), an FP32 backward
 // pass and Adam (FP32 master weights), all deterministic.
 #include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstdio>
 
 #include "swc_kernels.h"
 
@@ -141,51 +144,79 @@ __device__ __forceinline__ void node_features(const NodeArrays & N, long long s,
 // Modes of the forward kernel.
 enum { kMlpFromArray = 0, kMlpFromNodes = 1 };
 
+// TMEM columns per CTA: the layer-1 and layer-2 accumulators (N = 64 each) share
+// the same 64 columns (layer 2 is issued after every thread has read layer 1
+// back), so up to 512 / 64 = 8 CTAs fit the SM's TMEM.
+constexpr uint32_t kMlpTmemCols = 64;
+constexpr int kMlpMaxCtasPerSm  = 512 / int(kMlpTmemCols);
+
+// tanh with the hardware approximation (relative error about 2^-11).
+__device__ __forceinline__ float tanh_fast(float h) {
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
+    return t;
+}
+
 // params: FP32 vector (layout above); norm: f_mean[6], f_std[6], t_mean, t_std.
-// kMlpFromArray: rows of feat[n][6] -> out[n] (prediction t); optional saves of
-//   z1, z2 (pre-activations) and h1 (bf16-rounded) for training.
+// kMlpFromArray: rows of feat[n][6] -> out[n] (prediction t); with SAVE, the
+//   pre-activations z1, z2 and h1 (bf16-rounded) for training.
 // kMlpFromNodes: rows = active nodes (slot_of[I]); writes the warm start
 //   x[s] = p_prev + t * sD / alpha_hat into N.x (and feat_out when non-null).
-__global__ void __launch_bounds__(kMlpNT) k_mlp_forward(int mode, long long n, const float * __restrict__ params,
-                                                        const float * __restrict__ norm,
-                                                        const float * __restrict__ feat, float * __restrict__ out,
-                                                        float * __restrict__ z1s, float * __restrict__ h1s,
-                                                        float * __restrict__ z2s, NodeArrays N,
-                                                        const int * __restrict__ slot_of, const int * __restrict__ nv,
-                                                        const CgState * __restrict__ cg, FeatScale F0,
-                                                        float * __restrict__ feat_out, int * __restrict__ err) {
-    __shared__ __align__(1024) uint8_t sw1[kMlpH * 16 * 2];   // W1 [64 x 16] bf16 (K padded 6 -> 16)
-    __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpH * 2];  // W2 [64 x 64]
-    __shared__ __align__(1024) uint8_t sx[kMlpNT * 16 * 2];    // X  [128 x 16]
-    __shared__ __align__(1024) uint8_t sh[kMlpNT * kMlpH * 2];  // H1 [128 x 64]
-    __shared__ float sb1[kMlpH], sb2[kMlpH], sw3[kMlpH], snorm[14];
+//
+// Arithmetic: W1, b1, W2, b2 are scaled by 1/2 when staged (exact in bf16 and
+// FP32), so the accumulators hold h = z/2 and silu(z) = h + h tanh(h) is one
+// tanh and one FMA; bias, SiLU and the final dot run as packed FP32x2 pairs.
+// The X tile aliases the first 4 KB of the H1 tile: X is dead once layer 1
+// completes, H1 once layer 2 completes.
+template<int MODE, bool SAVE>
+__global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
+    k_mlp_forward(long long n, const float * __restrict__ params, const float * __restrict__ norm,
+                  const float * __restrict__ feat, float * __restrict__ out, float * __restrict__ z1s,
+                  float * __restrict__ h1s, float * __restrict__ z2s, NodeArrays N, const int * __restrict__ slot_of,
+                  const int * __restrict__ nv, const CgState * __restrict__ cg, FeatScale F0,
+                  float * __restrict__ feat_out, int * __restrict__ err) {
+    __shared__ __align__(1024) uint8_t sw1[kMlpH * 16 * 2];   // W1/2 [64 x 16] bf16 (K padded 6 -> 16)
+    __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpH * 2];  // W2/2 [64 x 64]
+    __shared__ __align__(1024) uint8_t sh[kMlpNT * kMlpH * 2];  // H1 [128 x 64]; X [128 x 16] in its first 4 KB
+    __shared__ float2 sb1[kMlpH / 2], sb2[kMlpH / 2], sw3[kMlpH / 2];  // b1/2, b2/2, w3 as pairs
+    __shared__ float snorm[14];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
     __shared__ int s_fail;
+    uint8_t * const sx = sh;
     const int tid = threadIdx.x, warp = tid >> 5;
 
     if (warp == 0) {
-        tmem_alloc(&tmem_base, 128);
+        tmem_alloc(&tmem_base, kMlpTmemCols);
         tmem_relinquish();
     }
     if (tid == 0) {
         mbar_init(&mbar, 1);
         s_fail = 0;
     }
-    // weights -> bf16 canonical layouts
-    for (int e = tid; e < kMlpH * 16; e += kMlpNT) {
-        const int r = e / 16, k = e % 16;
-        const float w = k < kMlpIn ? params[kOffW1 + r * kMlpIn + k] : 0.f;
-        *reinterpret_cast<__nv_bfloat16 *>(sw1 + canon_off(r, k, 16)) = __float2bfloat16_rn(w);
+    // weights -> bf16 canonical layouts, one 16-byte core-matrix row (8 k) per item
+    {
+        const int r = tid >> 1, k0 = (tid & 1) * 8;  // W1: 64 rows x 2 chunks = 128 items
+        uint32_t pk[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int ka = k0 + 2 * j, kb = ka + 1;
+            pk[j] = pack_bf16(ka < kMlpIn ? 0.5f * params[kOffW1 + r * kMlpIn + ka] : 0.f,
+                              kb < kMlpIn ? 0.5f * params[kOffW1 + r * kMlpIn + kb] : 0.f);
+        }
+        *reinterpret_cast<uint4 *>(sw1 + canon_off(r, k0, 16)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
     }
-    for (int e = tid; e < kMlpH * kMlpH; e += kMlpNT) {
-        const int r = e / kMlpH, k = e % kMlpH;
-        *reinterpret_cast<__nv_bfloat16 *>(sw2 + canon_off(r, k, kMlpH)) = __float2bfloat16_rn(params[kOffW2 + e]);
+    for (int e = tid; e < kMlpH * (kMlpH / 8); e += kMlpNT) {  // W2: 64 rows x 8 chunks
+        const int r = e >> 3, k0 = (e & 7) * 8;
+        const float * w = params + kOffW2 + r * kMlpH + k0;
+        *reinterpret_cast<uint4 *>(sw2 + canon_off(r, k0, kMlpH)) =
+            make_uint4(pack_bf16(0.5f * w[0], 0.5f * w[1]), pack_bf16(0.5f * w[2], 0.5f * w[3]),
+                       pack_bf16(0.5f * w[4], 0.5f * w[5]), pack_bf16(0.5f * w[6], 0.5f * w[7]));
     }
-    if (tid < kMlpH) {
-        sb1[tid] = params[kOffB1 + tid];
-        sb2[tid] = params[kOffB2 + tid];
-        sw3[tid] = params[kOffW3 + tid];
+    if (tid < kMlpH / 2) {
+        sb1[tid] = make_float2(0.5f * params[kOffB1 + 2 * tid], 0.5f * params[kOffB1 + 2 * tid + 1]);
+        sb2[tid] = make_float2(0.5f * params[kOffB2 + 2 * tid], 0.5f * params[kOffB2 + 2 * tid + 1]);
+        sw3[tid] = make_float2(params[kOffW3 + 2 * tid], params[kOffW3 + 2 * tid + 1]);
     }
     if (tid < 14) snorm[tid] = norm[tid];
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -194,14 +225,19 @@ __global__ void __launch_bounds__(kMlpNT) k_mlp_forward(int mode, long long n, c
     __syncthreads();
     tc_fence_after();
     const float b3 = params[kOffB3];
-    const uint32_t tbase = tmem_base;
-    const uint32_t lane_off = uint32_t(warp * 32) << 16;
+    const uint32_t tacc = tmem_base + (uint32_t(warp * 32) << 16);  // this warp's 32 lanes
     const uint64_t dW1 = smem_desc(smem_u32(sw1), 128, 256), dW2 = smem_desc(smem_u32(sw2), 128, 1024);
     const uint64_t dX = smem_desc(smem_u32(sx), 128, 256), dH = smem_desc(smem_u32(sh), 128, 1024);
+    float mean[6], inv_std[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        mean[k]    = snorm[k];
+        inv_std[k] = 1.f / snorm[6 + k];
+    }
 
     long long rows = n;
     FeatScale F = F0;
-    if (mode == kMlpFromNodes) {
+    if (MODE == kMlpFromNodes) {
         rows = *nv;
         // sD = RMS of the right-hand side over active nodes
         const double sD = rows > 0 ? sqrt(cg->bb / double(rows)) : 1.0;
@@ -209,21 +245,26 @@ __global__ void __launch_bounds__(kMlpNT) k_mlp_forward(int mode, long long n, c
     }
     uint32_t phase = 0;
     const long long ntiles = (rows + kMlpNT - 1) / kMlpNT;
-    // features of a tile row (raw; gathered through slot_of in node mode)
+    // Raw inputs of a tile row, gathered one tile ahead: the six features in
+    // array mode; D, alpha_hat, n_real, n_virt, p_prev, rho at slot_of[r] in node mode.
     auto gather = [&](long long r, float (&g)[6], long long & gs) {
 #pragma unroll
         for (int k = 0; k < 6; k++) g[k] = 0.f;
         gs = 0;
         if (r >= rows) return;
-        if (mode == kMlpFromArray) {
+        if (MODE == kMlpFromArray) {
 #pragma unroll
             for (int k = 0; k < 6; k++) g[k] = feat[r * 6 + k];
         } else {
-            gs = slot_of[r];
-            node_features(N, gs, F, g);
+            gs   = slot_of[r];
+            g[0] = N.D[gs];
+            g[1] = N.ahat[gs];
+            g[2] = N.nreal ? float(N.nreal[gs]) : 0.f;
+            g[3] = N.nvirt ? float(N.nvirt[gs]) : 0.f;
+            g[4] = N.x[gs];  // node-mapped previous pressure
+            g[5] = N.rho[gs];
         }
     };
-    // the next tile's gathers are issued before this tile's MMAs are waited on
     float fn[6];
     long long sn = 0;
     gather(blockIdx.x * (long long) kMlpNT + tid, fn, sn);
@@ -233,57 +274,65 @@ __global__ void __launch_bounds__(kMlpNT) k_mlp_forward(int mode, long long n, c
         float f[6];
 #pragma unroll
         for (int k = 0; k < 6; k++) f[k] = fn[k];
+        const float ah = fn[1], pp = fn[4];
         const long long s = sn;
-        if (valid && mode != kMlpFromArray && feat_out) {
+        if (MODE == kMlpFromNodes) {  // raw inputs -> features (as node_features)
+            f[0] = f[0] * F.inv_sD;
+            f[1] = ah * F.inv_alpha0;
+            f[2] = f[2] * F.inv_nreal;
+            f[3] = f[3] * F.inv_nvirt;
+            f[4] = pp * ah * F.inv_sD;
+            f[5] = f[5] * F.inv_rho0;
+            if (valid && feat_out) {
 #pragma unroll
-            for (int k = 0; k < 6; k++) feat_out[row * 6 + k] = f[k];
+                for (int k = 0; k < 6; k++) feat_out[row * 6 + k] = f[k];
+            }
         }
         // X row: normalised features in bf16, K padded to 16
         float xn[6];
 #pragma unroll
-        for (int k = 0; k < 6; k++) xn[k] = valid ? (f[k] - snorm[k]) / snorm[6 + k] : 0.f;
-        uint4 c0 = make_uint4(pack_bf16(xn[0], xn[1]), pack_bf16(xn[2], xn[3]), pack_bf16(xn[4], xn[5]), 0u);
-        *reinterpret_cast<uint4 *>(sx + canon_off(tid, 0, 16)) = c0;
+        for (int k = 0; k < 6; k++) xn[k] = valid ? (f[k] - mean[k]) * inv_std[k] : 0.f;
+        *reinterpret_cast<uint4 *>(sx + canon_off(tid, 0, 16)) =
+            make_uint4(pack_bf16(xn[0], xn[1]), pack_bf16(xn[2], xn[3]), pack_bf16(xn[4], xn[5]), 0u);
         *reinterpret_cast<uint4 *>(sx + canon_off(tid, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
         if (tid == 0) {
-            mma_bf16(tbase, dX, dW1, kIdescM128N64, 0u);
+            mma_bf16(tmem_base, dX, dW1, kIdescM128N64, 0u);
             mma_commit(&mbar);
         }
+        // the next tile's gathers are in flight while this tile's MMAs run
         gather((tile + gridDim.x) * kMlpNT + tid, fn, sn);
         if (!mbar_wait(&mbar, phase)) s_fail = 1;
         phase ^= 1u;
         tc_fence_after();
-        // layer-1 epilogue: bias + SiLU -> H1 (bf16)
+        // layer-1 epilogue: h = z/2 + b1/2, silu = h + h tanh(h) -> H1 (bf16)
 #pragma unroll
         for (int cblk = 0; cblk < 4; cblk++) {
             float z[16];
-            tmem_ld16(tbase + lane_off + uint32_t(cblk * 16), z);
+            tmem_ld16(tacc + uint32_t(cblk * 16), z);
             tmem_ld_wait();
             uint32_t pk[8];
 #pragma unroll
-            for (int i = 0; i < 16; i += 2) {
-                const int c = cblk * 16 + i;
-                const float za = z[i] + sb1[c], zb = z[i + 1] + sb1[c + 1];
-                float ha = silu(za), hb = silu(zb);
-                if (z1s && valid) {
-                    z1s[row * kMlpH + c]     = za;
-                    z1s[row * kMlpH + c + 1] = zb;
-                }
-                pk[i / 2] = pack_bf16(ha, hb);
-                if (h1s && valid) {
-                    const __nv_bfloat162 hv = *reinterpret_cast<const __nv_bfloat162 *>(&pk[i / 2]);
-                    h1s[row * kMlpH + c]     = __bfloat162float(hv.x);
-                    h1s[row * kMlpH + c + 1] = __bfloat162float(hv.y);
+            for (int i = 0; i < 8; i++) {
+                const int c    = cblk * 8 + i;  // column pair
+                const float2 h = add2(make_float2(z[2 * i], z[2 * i + 1]), sb1[c]);
+                const float2 a = fma2(h, make_float2(tanh_fast(h.x), tanh_fast(h.y)), h);
+                pk[i]          = pack_bf16(a.x, a.y);
+                if (SAVE && valid) {
+                    const __nv_bfloat162 hv = *reinterpret_cast<const __nv_bfloat162 *>(&pk[i]);
+                    *reinterpret_cast<float2 *>(z1s + row * kMlpH + 2 * c) = make_float2(2.f * h.x, 2.f * h.y);
+                    *reinterpret_cast<float2 *>(h1s + row * kMlpH + 2 * c) =
+                        make_float2(__bfloat162float(hv.x), __bfloat162float(hv.y));
                 }
             }
             *reinterpret_cast<uint4 *>(sh + canon_off(tid, cblk * 16, kMlpH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
             *reinterpret_cast<uint4 *>(sh + canon_off(tid, cblk * 16 + 8, kMlpH)) =
                 make_uint4(pk[4], pk[5], pk[6], pk[7]);
         }
+        // every thread's tcgen05.ld of layer 1 is complete before layer 2 reuses the columns
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
@@ -291,36 +340,34 @@ __global__ void __launch_bounds__(kMlpNT) k_mlp_forward(int mode, long long n, c
         if (tid == 0) {
 #pragma unroll
             for (int j = 0; j < 4; j++)  // K = 64 in four K = 16 steps (2 core matrices = 256 B each)
-                mma_bf16(tbase + 64u, dH + uint64_t((j * 256) >> 4), dW2 + uint64_t((j * 256) >> 4), kIdescM128N64,
+                mma_bf16(tmem_base, dH + uint64_t((j * 256) >> 4), dW2 + uint64_t((j * 256) >> 4), kIdescM128N64,
                          j > 0 ? 1u : 0u);
             mma_commit(&mbar);
         }
         if (!mbar_wait(&mbar, phase)) s_fail = 1;
         phase ^= 1u;
         tc_fence_after();
-        // layer-2 epilogue: bias + SiLU, final dot
-        float y = b3;
+        // layer-2 epilogue: h = z/2 + b2/2, silu, final dot as two packed partial sums
+        float2 y2 = make_float2(0.f, 0.f);
 #pragma unroll
         for (int cblk = 0; cblk < 4; cblk++) {
             float z[16];
-            tmem_ld16(tbase + lane_off + 64u + uint32_t(cblk * 16), z);
+            tmem_ld16(tacc + uint32_t(cblk * 16), z);
             tmem_ld_wait();
 #pragma unroll
-            for (int i = 0; i < 16; i++) {
-                const int c    = cblk * 16 + i;
-                const float zz = z[i] + sb2[c];
-                if (z2s && valid) z2s[row * kMlpH + c] = zz;
-                y = fmaf(sw3[c], silu(zz), y);
+            for (int i = 0; i < 8; i++) {
+                const int c    = cblk * 8 + i;
+                const float2 h = add2(make_float2(z[2 * i], z[2 * i + 1]), sb2[c]);
+                if (SAVE && valid)
+                    *reinterpret_cast<float2 *>(z2s + row * kMlpH + 2 * c) = make_float2(2.f * h.x, 2.f * h.y);
+                const float2 a = fma2(h, make_float2(tanh_fast(h.x), tanh_fast(h.y)), h);
+                y2             = fma2(sw3[c], a, y2);
             }
         }
-        const float t = snorm[12] + snorm[13] * y;
+        const float t = snorm[12] + snorm[13] * (b3 + (y2.x + y2.y));
         if (valid) {
-            if (mode == kMlpFromArray) out[row] = t;
-            else {
-                const float ah = N.ahat[s];
-                const float pp = N.x[s];
-                N.x[s]         = pp + t / (F.inv_sD * ah);
-            }
+            if (MODE == kMlpFromArray) out[row] = t;
+            else N.x[s] = pp + t / (F.inv_sD * ah);
         }
         tc_fence_before();
         __syncthreads();
@@ -331,7 +378,7 @@ __global__ void __launch_bounds__(kMlpNT) k_mlp_forward(int mode, long long n, c
     if (s_fail && tid == 0) atomicExch(err, 1);
     if (warp == 0) {
         tc_fence_after();
-        tmem_dealloc(tbase, 128);
+        tmem_dealloc(tmem_base, kMlpTmemCols);
     }
 }
 
@@ -515,18 +562,88 @@ void launch_gather_rows(const float * src, const float * src_t, const int * idx,
     if (n <= 0) return;
     k_gather_rows<<<int(std::min<long long>((n + 255) / 256, 152 * 8)), 256, 0, st>>>(src, src_t, idx, n, dst, dst_t);
 }
+// Resident CTAs per SM of a forward instantiation, capped by TMEM (a CTA that
+// found its columns taken would wait in tcgen05.alloc).  When shared memory and
+// registers alone would allow more, the launch asks for padding dynamic shared
+// memory (`dyn`) until the occupancy is within the TMEM cap.
+struct MlpLaunch {
+    int per_sm = 0;
+    size_t dyn = 0;
+};
+// Residency is computed from the kernel's registers and shared memory and the
+// SM's limits (the occupancy calculator is only consulted as a cross-check and
+// reported on stderr when it disagrees).
+template<int MODE, bool SAVE>
+static MlpLaunch mlp_launch_shape() {
+    static MlpLaunch shape;
+    if (shape.per_sm) return shape;
+    auto kern = k_mlp_forward<MODE, SAVE>;
+    MlpLaunch s;
+    s.per_sm = 1;
+    int dev = 0, regs_sm = 65536, smem_sm = 233472, reserved = 1024, threads_sm = 2048;
+    cudaFuncAttributes fa{};
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaFuncGetAttributes(&fa, kern) == cudaSuccess) {
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+        cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        const int regs_cta = ((fa.numRegs + 7) / 8) * 8 * kMlpNT;
+        auto fit           = [&](size_t dyn) {
+            const size_t smem_cta = fa.sharedSizeBytes + dyn + size_t(reserved);
+            return std::min({regs_sm / std::max(regs_cta, 1), int(size_t(smem_sm) / smem_cta), threads_sm / kMlpNT});
+        };
+        while (fit(s.dyn) > kMlpMaxCtasPerSm) s.dyn += 1024;  // pad until TMEM cannot be oversubscribed
+        s.per_sm = std::max(1, fit(s.dyn));
+        if (s.dyn) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(s.dyn));
+        int occ          = 0;
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kMlpNT, s.dyn);
+        if (e != cudaSuccess || occ != s.per_sm)
+            fprintf(stderr, "swc: k_mlp_forward residency %d CTAs/SM (occupancy calculator: %d, %s)\n", s.per_sm, occ,
+                    cudaGetErrorString(e));
+    }
+    cudaGetLastError();
+    shape = s;
+    return shape;
+}
+static int num_sms_cached() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 152;
+    }
+    return sms;
+}
+// Persistent grid: every resident CTA slot once, never more CTAs than tiles.
+template<int MODE, bool SAVE>
+static void launch_forward(long long rows_max, const float * params, const float * norm, const float * feat,
+                           float * out, float * z1s, float * h1s, float * z2s, const NodeArrays & N,
+                           const int * slot_of, const int * nv, const CgState * cg, const FeatScale & F,
+                           float * feat_out, int * err, cudaStream_t st) {
+    const MlpLaunch s     = mlp_launch_shape<MODE, SAVE>();
+    const long long tiles = std::max<long long>(1, (rows_max + kMlpNT - 1) / kMlpNT);
+    const int grid        = int(std::min<long long>(tiles, (long long) s.per_sm * num_sms_cached()));
+    k_mlp_forward<MODE, SAVE><<<grid, kMlpNT, s.dyn, st>>>(rows_max, params, norm, feat, out, z1s, h1s, z2s, N,
+                                                           slot_of, nv, cg, F, feat_out, err);
+}
 void launch_mlp_forward_array(long long n, const float * params, const float * norm, const float * feat, float * out,
-                              float * z1s, float * h1s, float * z2s, int * err, int grid, cudaStream_t st) {
+                              float * z1s, float * h1s, float * z2s, int * err, cudaStream_t st) {
     if (n <= 0) return;
-    k_mlp_forward<<<grid, kMlpNT, 0, st>>>(kMlpFromArray, n, params, norm, feat, out, z1s, h1s, z2s, NodeArrays{},
-                                           nullptr, nullptr, nullptr, FeatScale{}, nullptr, err);
+    if (z1s || h1s || z2s)
+        launch_forward<kMlpFromArray, true>(n, params, norm, feat, out, z1s, h1s, z2s, NodeArrays{}, nullptr, nullptr,
+                                            nullptr, FeatScale{}, nullptr, err, st);
+    else
+        launch_forward<kMlpFromArray, false>(n, params, norm, feat, out, nullptr, nullptr, nullptr, NodeArrays{},
+                                             nullptr, nullptr, nullptr, FeatScale{}, nullptr, err, st);
 }
 void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const int * slot_of,
-                              const int * nv, const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal,
-                              float inv_nvirt, float * feat_out, int * err, int grid, cudaStream_t st) {
+                              const int * nv, long long rows_max, const CgState * cg, float inv_alpha0,
+                              float inv_rho0, float inv_nreal, float inv_nvirt, float * feat_out, int * err,
+                              cudaStream_t st) {
     FeatScale F{0.f, inv_alpha0, inv_rho0, inv_nreal, inv_nvirt};
-    k_mlp_forward<<<grid, kMlpNT, 0, st>>>(kMlpFromNodes, 0, params, norm, nullptr, nullptr, nullptr, nullptr, nullptr,
-                                           N, slot_of, nv, cg, F, feat_out, err);
+    launch_forward<kMlpFromNodes, false>(rows_max, params, norm, nullptr, nullptr, nullptr, nullptr, nullptr, N,
+                                         slot_of, nv, cg, F, feat_out, err, st);
 }
 void launch_mlp_backward(long long n, const float * params, const float * norm, const float * feat,
                          const float * pred, const float * target, const float * z1s, const float * h1s,

@@ -308,11 +308,18 @@ __global__ void __launch_bounds__(kNT) k_diag_max_f64(Lattice L, const int * __r
 //   node:   previous pressure of the same node, 0 if it was inactive
 //   zero:   0
 //   given:  caller-supplied values in brick layout
+//   extrap: linear extrapolation in time of the same node's pressure,
+//           2 p_{n-1} - p_{n-2} where the node was active in both previous
+//           steps (bflag_m2 non-null: the history is valid), else p_{n-1}, else
+//           0; p_{n-1} is kept in xm1 for the next step.  xm1 is written for
+//           every slot of an active brick; slots whose value is stale there are
+//           masked by the activity flags of the next step.
 // ---------------------------------------------------------------------------
 template<int DIM>
 __global__ void __launch_bounds__(kNT) k_warm_start(Lattice L, const int * __restrict__ blist,
                                                     const int * __restrict__ bcount, const int * __restrict__ seg_off,
-                                                    const unsigned char * __restrict__ bflag_prev, NodeArrays N,
+                                                    const unsigned char * __restrict__ bflag_prev,
+                                                    const unsigned char * __restrict__ bflag_m2, NodeArrays N,
                                                     int mode, const float * __restrict__ pcomp,
                                                     const int * __restrict__ nv_prev, const float * __restrict__ given) {
     using G      = BrickGeom<DIM>;
@@ -334,8 +341,14 @@ __global__ void __launch_bounds__(kNT) k_warm_start(Lattice L, const int * __res
                     v = (bflag_prev[b] && N.flag_prev[s]) ? N.x[s] : 0.f;
                 } else if (mode == kWarmGiven) {
                     v = given[s];
+                } else if (mode == kWarmExtrap) {
+                    if (bflag_prev[b] && N.flag_prev[s]) {
+                        const float p1 = N.x[s];
+                        v = (bflag_m2 && bflag_m2[b] && N.flag_m2[s]) ? fmaf(2.f, p1, -N.xm1[s]) : p1;
+                    }
                 }
             }
+            if (mode == kWarmExtrap) N.xm1[s] = N.x[s];
             N.x[s] = v;
         }
     }
@@ -525,7 +538,11 @@ __global__ void __launch_bounds__(kNT) k_pressure_gradient(Lattice L, Phys P, co
                                                            const float4 * __restrict__ bnrm,
                                                            const int * __restrict__ bcellStart, int * queue) {
     using G = BrickGeom<DIM>;
-    __shared__ __align__(16) float tile[G::TILE];
+    // Row pitch 24 in 3D: a warp's particles span about four consecutive cell
+    // rows of one z-plane, whose 8-node windows then fall in disjoint banks
+    // (24 dy mod 32 = 0, 24, 16, 8).
+    constexpr int PX = DIM == 3 ? 24 : G::PX;
+    __shared__ __align__(16) float tile[PX * G::TY * G::TZ];
     constexpr int ROWS = G::BY * G::BZ;  // cell rows of a brick
     __shared__ int rinc[ROWS], rbeg[ROWS];
     __shared__ int slot;
@@ -535,7 +552,7 @@ __global__ void __launch_bounds__(kNT) k_pressure_gradient(Lattice L, Phys P, co
         const int b   = plist[bi];
         const int3 bc = brick_coords(L, b);
         const int x0 = bc.x * G::BX, x1 = min(x0 + G::BX, L.nx);
-        load_tile4<DIM, kNT>(L, bflag, bc, tile, [&](long long s) {
+        load_tile4<DIM, kNT, PX>(L, bflag, bc, tile, [&](long long s) {
             const float4 v = *reinterpret_cast<const float4 *>(N.V + s), x = *reinterpret_cast<const float4 *>(N.x + s);
             return make_float4(v.x * x.x, v.y * x.y, v.z * x.z, v.w * x.w);
         });
@@ -608,7 +625,7 @@ __global__ void __launch_bounds__(kNT) k_pressure_gradient(Lattice L, Phys P, co
                         const float dy   = uy - float(ky);
                         const float dyz2 = fmaf(dy, dy, dz2);
                         if (dyz2 >= 16.f) continue;
-                        const float * trow = tile + G::PX * (ky + G::TY * kz) + (cx - 3);
+                        const float * trow = tile + PX * (ky + G::TY * kz) + (cx - 3);
                         const float2 sg = gradient_row(trow, dxp, dyz2, sx);
                         const float s   = sg.x + sg.y;
                         fy = fmaf(dy, s, fy);
@@ -695,9 +712,9 @@ void launch_diag_max_f64(const Lattice & L, const BrickArrays & B, const NodeArr
 
 template<int DIM>
 void launch_warm_start(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int mode, const float * pcomp,
-                       const int * nv_prev, const float * given, int grid, cudaStream_t st) {
-    k_warm_start<DIM><<<grid, kNT, 0, st>>>(L, B.list, B.count, B.seg_off, B.flag_prev, N, mode, pcomp, nv_prev,
-                                            given);
+                       const int * nv_prev, const float * given, int grid, cudaStream_t st, bool history) {
+    k_warm_start<DIM><<<grid, kNT, 0, st>>>(L, B.list, B.count, B.seg_off, B.flag_prev,
+                                            history ? B.flag_m2 : nullptr, N, mode, pcomp, nv_prev, given);
 }
 
 template<int DIM>
@@ -740,7 +757,7 @@ void launch_zero_active(const Lattice & L, const BrickArrays & B, float * a, int
     template void launch_diag_max_f64<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const StencilD &,   \
                                          unsigned long long *, int, cudaStream_t);                                     \
     template void launch_warm_start<D>(const Lattice &, const BrickArrays &, const NodeArrays &, int, const float *,   \
-                                       const int *, const float *, int, cudaStream_t);                                 \
+                                       const int *, const float *, int, cudaStream_t, bool);                           \
     template void launch_compact_export<D>(const Lattice &, const BrickArrays &, const NodeArrays &, float *,          \
                                            long long *, double *, double *, double *, double *, double *, double *,    \
                                            unsigned short *, int, cudaStream_t);                                       \

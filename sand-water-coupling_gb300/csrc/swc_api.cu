@@ -89,6 +89,11 @@ struct swc_ctx {
     float * feat_buf   = nullptr;  // logged features (reference order, 6 per node)
     float * tgt_buf    = nullptr;  // logged targets
     bool    features_valid = false;
+    bool    slot_of_valid  = false;  // slot_of / node count are those of the last projection
+    // extrapolated warm start: consecutive advance steps whose solution history
+    // (N.xm1, flags two steps back) is valid, and whether this step shifted the flags
+    int     extrap_steps   = 0;
+    bool    extrap_shifted = false;
     float *     pcomp = nullptr;
     int *       nv_prev = nullptr;
     int *       scan_tiles = nullptr;
@@ -173,6 +178,25 @@ void free_sort(SortScratch & S) {
     dfree(S.vel2);
     dfree(S.aux2);
     dfree(S.id2);
+}
+
+// History of the extrapolated warm start (allocated on demand, zero history).
+int ensure_extrap_buffers(swc_ctx * c) {
+    if (c->N.xm1) return SWC_OK;
+    const size_t slots = size_t(c->L.nbricks) * (c->dim == 3 ? 512 : 256);
+    int rc;
+    if ((rc = dalloc(c, &c->N.flag_m2, slots)) || (rc = dalloc(c, &c->B.flag_m2, size_t(c->L.nbricks))) ||
+        (rc = dalloc(c, &c->N.xm1, slots)))
+        return rc;
+    CK(cudaMemset(c->N.flag_m2, 0, slots));
+    CK(cudaMemset(c->B.flag_m2, 0, size_t(c->L.nbricks)));
+    CK(cudaMemset(c->N.xm1, 0, sizeof(float) * slots));
+    c->extrap_steps = 0;
+    // the CG graphs captured the old NodeArrays: recapture
+    if (c->g1) cudaGraphExecDestroy(c->g1);
+    if (c->g8) cudaGraphExecDestroy(c->g8);
+    c->g1 = c->g8 = nullptr;
+    return SWC_OK;
 }
 
 // Buffers of the learned warm start and of training-data logging (allocated on demand).
@@ -349,6 +373,7 @@ template<int DIM> int run_cg(swc_ctx * c, swc_stats * st, bool initialized) {
 // The shared tail of advance / project: virtual generation, projection, G_i.
 template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     mark(c, 3);
+    c->slot_of_valid = false;
     run_generate<DIM>(c, true);
     mark(c, 4);
     const int mode     = c->opts.warm_start;
@@ -358,11 +383,17 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     const size_t slots = size_t(c->L.nbricks) * BrickGeom<DIM>::BN;
     int used           = mode == SWC_WARM_LEARNED ? SWC_WARM_NODE : mode;
     bool initialized   = false;
+    // extrapolation in time needs the previous advance's history; without it the node-mapped start
+    const bool extrap  = mode == SWC_WARM_EXTRAPOLATE && c->N.xm1;
+    const bool history = extrap && c->extrap_shifted && c->extrap_steps >= 1;
+    const int wmode    = (mode == SWC_WARM_LEARNED || (mode == SWC_WARM_EXTRAPOLATE && !extrap)) ? kWarmNode : mode;
+    if (mode == SWC_WARM_EXTRAPOLATE && !history) used = SWC_WARM_NODE;
     if (learned || logging) {
         // node-mapped previous pressure: the fallback, feature f4 and the target reference
         launch_warm_start<DIM>(c->L, c->B, c->N, kWarmNode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
         CK(cudaMemcpyAsync(c->xprev, c->N.x, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
         launch_slot_of<DIM>(c->L, c->B, c->N, c->slot_of, c->grid, c->stream);
+        c->slot_of_valid = true;
         // |b|^2 for sD and (for the fallback test) the initial residual of the
         // node-mapped start, read back with the learned start's (one host synchronisation)
         const bool no_fallback = learned && c->opts.learned_no_fallback && !logging;
@@ -379,8 +410,8 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
             launch_node_features(c->N, c->slot_of, nv, c->L.ncells, c->cg, inv_a0, inv_r0, inv_nr, inv_nv,
                                  c->feat_buf, c->stream);
         if (learned) {
-            launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->slot_of, nv, c->cg, inv_a0, inv_r0, inv_nr,
-                                     inv_nv, nullptr, c->mlp_err, c->num_sms * 4, c->stream);  // 4 x 128 TMEM columns per SM
+            launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->slot_of, nv, (long long) slots, c->cg, inv_a0,
+                                     inv_r0, inv_nr, inv_nv, nullptr, c->mlp_err, c->stream);
             CK(cudaMemcpyAsync(&c->hcg->mlp_err, c->mlp_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
             if ((rc = cg_init_sync<DIM>(c))) return rc;
             const int err        = c->hcg->mlp_err;
@@ -396,14 +427,16 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
             if ((rc = cg_init_sync<DIM>(c))) return rc;  // host copy of the node-mapped start's state
             initialized = true;
         } else {
-            launch_warm_start<DIM>(c->L, c->B, c->N, mode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
+            launch_warm_start<DIM>(c->L, c->B, c->N, wmode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream,
+                                   history);
         }
     } else {
-        launch_warm_start<DIM>(c->L, c->B, c->N, mode == SWC_WARM_LEARNED ? kWarmNode : mode, c->pcomp, c->nv_prev,
-                               nullptr, c->grid, c->stream);
+        launch_warm_start<DIM>(c->L, c->B, c->N, wmode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream, history);
     }
     mark(c, 5);
     int rc = run_cg<DIM>(c, st, initialized);
+    c->extrap_steps   = (extrap && c->extrap_shifted && (rc == SWC_OK || rc == SWC_CG_NOT_CONVERGED)) ? c->extrap_steps + 1 : 0;
+    c->extrap_shifted = false;
     if (st) st->warm_start_used = used;
     if (logging && (rc == SWC_OK || rc == SWC_CG_NOT_CONVERGED)) {
         launch_mlp_targets(c->L.ncells, nv, c->slot_of, c->N.x, c->xprev, c->N.ahat, c->cg, c->tgt_buf, c->stream);
@@ -434,9 +467,18 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     return cg_status;
 }
 
-void save_prev_flags(swc_ctx * c) {
+// Activity flags of the previous step (and, for the extrapolated warm start on
+// an advance, of the step before).  A projection without motion (swc_project)
+// ends the extrapolation history.
+void save_prev_flags(swc_ctx * c, bool move) {
     using namespace swc;
     const size_t bn = c->dim == 3 ? BrickGeom<3>::BN : BrickGeom<2>::BN;
+    c->extrap_shifted = false;
+    if (move && c->opts.warm_start == SWC_WARM_EXTRAPOLATE && c->N.xm1) {
+        cudaMemcpyAsync(c->N.flag_m2, c->N.flag_prev, size_t(c->L.nbricks) * bn, cudaMemcpyDeviceToDevice, c->stream);
+        cudaMemcpyAsync(c->B.flag_m2, c->B.flag_prev, size_t(c->L.nbricks), cudaMemcpyDeviceToDevice, c->stream);
+        c->extrap_shifted = true;
+    }
     cudaMemcpyAsync(c->N.flag_prev, c->N.flag, size_t(c->L.nbricks) * bn, cudaMemcpyDeviceToDevice, c->stream);
     cudaMemcpyAsync(c->B.flag_prev, c->B.flag, size_t(c->L.nbricks), cudaMemcpyDeviceToDevice, c->stream);
 }
@@ -444,7 +486,7 @@ void save_prev_flags(swc_ctx * c) {
 template<int DIM> int do_advance(swc_ctx * c, double dt, swc_stats * st, bool move) {
     CK(cudaEventRecord(c->evA, c->stream));
     mark(c, 0);
-    save_prev_flags(c);
+    save_prev_flags(c, move);
     if (move) {
         launch_advect(c->pos, c->vel, c->n, float(dt), c->stream);
         if (c->has_motion && c->nb > 0) {
@@ -528,7 +570,8 @@ template<int DIM> int do_initialize(swc_ctx * c) {
     std::memcpy(&a0, &dbits, sizeof(double));
     c->alpha0 = dbits ? a0 : -1e6;
     setup_phys(c);
-    // no previous pressure: empty prefix
+    // no previous pressure: empty prefix, no extrapolation history
+    c->extrap_steps = 0;
     CK(cudaMemsetAsync(c->nv_prev, 0, sizeof(int), c->stream));
     CK(cudaMemsetAsync(c->N.x, 0, sizeof(float) * size_t(c->L.nbricks) * (DIM == 3 ? 512 : 256), c->stream));
     CK(cudaMemsetAsync(c->N.flag, 0, size_t(c->L.nbricks) * (DIM == 3 ? 512 : 256), c->stream));
@@ -574,6 +617,7 @@ int swc_create(const swc_scene * s, const swc_solver_opts * o, swc_ctx ** out) {
     if ((s->dim != 2 && s->dim != 3) || !(s->particle_radius > 0) || !(s->grid_spacing > 0) || !(s->mass > 0) ||
         s->grid_size[0] < 1 || s->grid_size[1] < 1 || (s->dim == 3 && s->grid_size[2] < 1))
         return SWC_BAD_ARG;
+    if (o && (o->warm_start < SWC_WARM_PREFIX || o->warm_start > SWC_WARM_EXTRAPOLATE)) return SWC_BAD_ARG;
     auto * c  = new swc_ctx();
     c->dim    = s->dim;
     c->scene  = *s;
@@ -640,6 +684,7 @@ int swc_create(const swc_scene * s, const swc_solver_opts * o, swc_ctx ** out) {
         return fail(rc);
     if (c->opts.keep_virtual_velocity && (rc = dalloc(c, &c->N.vbar, slots))) return fail(rc);
     if (c->opts.keep_features && (rc = ensure_learn_buffers(c))) return fail(rc);
+    if (c->opts.warm_start == SWC_WARM_EXTRAPOLATE && (rc = ensure_extrap_buffers(c))) return fail(rc);
     c->B.nseg = (long long) L.ny * L.nz * L.bnx;
     if ((rc = dalloc(c, &c->B.flag, L.nbricks)) || (rc = dalloc(c, &c->B.flag_prev, L.nbricks)) ||
         (rc = dalloc(c, &c->B.list, L.nbricks)) || (rc = dalloc(c, &c->B.count, 1)) ||
@@ -696,6 +741,9 @@ void swc_destroy(swc_ctx * c) {
     free_sort(c->sortB);
     dfree(c->N.flag);
     dfree(c->N.flag_prev);
+    dfree(c->N.flag_m2);
+    dfree(c->N.xm1);
+    dfree(c->B.flag_m2);
     dfree(c->N.V);
     dfree(c->N.D);
     dfree(c->N.rho);
@@ -761,7 +809,8 @@ int swc_set_stream(swc_ctx * c, void * stream) {
 }
 
 int swc_set_solver_opts(swc_ctx * c, const swc_solver_opts * o) {
-    if (!valid_ctx(c) || !o) return SWC_BAD_ARG;
+    if (!valid_ctx(c) || !o || o->warm_start < SWC_WARM_PREFIX || o->warm_start > SWC_WARM_EXTRAPOLATE)
+        return SWC_BAD_ARG;
     const bool need_vbar = o->keep_virtual_velocity && !c->N.vbar;
     const bool need_feat = o->keep_features && !c->N.nreal;
     c->opts = *o;
@@ -775,6 +824,10 @@ int swc_set_solver_opts(swc_ctx * c, const swc_solver_opts * o) {
     }
     if (need_vbar && (rc = dalloc(c, &c->N.vbar, slots))) return rc;
     if (need_feat && (rc = ensure_learn_buffers(c))) return rc;
+    if (o->warm_start == SWC_WARM_EXTRAPOLATE && !c->N.xm1) {
+        CK(cudaStreamSynchronize(c->stream));
+        if ((rc = ensure_extrap_buffers(c))) return rc;
+    }
     return SWC_OK;
 }
 
@@ -1141,7 +1194,8 @@ int swc_get_phase_times(swc_ctx * c, double * ms, int n) {
 }
 
 int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
-    if (!valid_ctx(c) || !mean_ms || reps <= 0 || !c->initialized || which < 0 || which > 6) return SWC_BAD_ARG;
+    if (!valid_ctx(c) || !mean_ms || reps <= 0 || !c->initialized || which < 0 || which > 7) return SWC_BAD_ARG;
+    if (which == 7 && !(c->mlp_ready && c->slot_of_valid)) return SWC_BAD_ARG;  // needs a learned projection first
     CK(cudaStreamSynchronize(c->stream));
     // keep the solver state: run the CG kernels against a scratch copy of the scalars
     CgState saved{};
@@ -1156,7 +1210,7 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
     CK(cudaMemcpy(c->cg, &run, sizeof(CgState), cudaMemcpyHostToDevice));
     float * x_save = nullptr;
     const size_t slots = size_t(c->L.nbricks) * (c->dim == 3 ? 512 : 256);
-    if (which == 1) {
+    if (which == 1 || which == 7) {
         CK(cudaMalloc(&x_save, sizeof(float) * slots * 2));
         cudaMemcpy(x_save, c->N.x, sizeof(float) * slots, cudaMemcpyDeviceToDevice);
         cudaMemcpy(x_save + slots, c->N.r, sizeof(float) * slots, cudaMemcpyDeviceToDevice);
@@ -1167,6 +1221,12 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
         cudaMemcpy(vel_save, c->vel, sizeof(float4) * c->n, cudaMemcpyDeviceToDevice);
     }
     auto launch = [&]() {
+        if (which == 7) {
+            launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->slot_of, c->B.seg_off + c->B.nseg,
+                                     (long long) slots, c->cg, float(1.0 / c->alpha0), float(1.0 / c->rho0), 1.f / 32.f,
+                                     c->dim == 3 ? 1.f / 251.f : 1.f / 45.f, nullptr, c->mlp_err, c->stream);
+            return;
+        }
         if (c->dim == 3) {
             switch (which) {
             case 0: launch_cg_spmv<3>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->sgrid, c->stream); break;

@@ -38,11 +38,14 @@ struct NodeArrays {
     float4 *        vbar      = nullptr;  // optional: virtual velocity (debug / export)
     unsigned short * nreal    = nullptr;  // optional: real neighbours within h
     unsigned short * nvirt    = nullptr;  // optional: active virtual neighbours within H (self included)
+    float *         xm1       = nullptr;  // extrapolated warm start: pressure of the step before the previous
+    unsigned char * flag_m2   = nullptr;  // extrapolated warm start: active two steps back
 };
 
 struct BrickArrays {
     unsigned char * flag      = nullptr;  // active this step
     unsigned char * flag_prev = nullptr;
+    unsigned char * flag_m2   = nullptr;  // active two steps back (extrapolated warm start)
     int *           list      = nullptr;  // active brick ids, ascending
     int *           count     = nullptr;  // device: number of active bricks
     int *           seg       = nullptr;  // per (row, brick column) active-node counts
@@ -125,10 +128,11 @@ template<int DIM>
 void launch_diag_max_f64(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const StencilD & S,
                          unsigned long long * out_bits, int grid, cudaStream_t st);
 // warm-start modes
-enum { kWarmPrefix = 0, kWarmNode = 1, kWarmZero = 2, kWarmGiven = 3 };
+enum { kWarmPrefix = 0, kWarmNode = 1, kWarmZero = 2, kWarmGiven = 3, kWarmExtrap = 4 };
+// history (kWarmExtrap): N.xm1 / N.flag_m2 / B.flag_m2 hold the step before the previous one
 template<int DIM>
 void launch_warm_start(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int mode, const float * pcomp,
-                       const int * nv_prev, const float * given, int grid, cudaStream_t st);
+                       const int * nv_prev, const float * given, int grid, cudaStream_t st, bool history = false);
 template<int DIM>
 void launch_compact_export(const Lattice & L, const BrickArrays & B, const NodeArrays & N, float * pcomp,
                            long long * node_id, double * rho, double * vol, double * vbar, double * div,
@@ -165,10 +169,11 @@ void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeAr
 
 // ---- k_mlp.cu (learned warm start) ----
 void launch_mlp_forward_array(long long n, const float * params, const float * norm, const float * feat, float * out,
-                              float * z1s, float * h1s, float * z2s, int * err, int grid, cudaStream_t st);
+                              float * z1s, float * h1s, float * z2s, int * err, cudaStream_t st);
 void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const int * slot_of,
-                              const int * nv, const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal,
-                              float inv_nvirt, float * feat_out, int * err, int grid, cudaStream_t st);
+                              const int * nv, long long rows_max, const CgState * cg, float inv_alpha0,
+                              float inv_rho0, float inv_nreal, float inv_nvirt, float * feat_out, int * err,
+                              cudaStream_t st);
 void launch_node_features(const NodeArrays & N, const int * slot_of, const int * nv, long long rows_max,
                           const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal, float inv_nvirt,
                           float * feat_out, cudaStream_t st);

@@ -28,7 +28,6 @@ struct swc_trainer {
     float *z1 = nullptr, *h1 = nullptr, *z2 = nullptr, *dz1 = nullptr, *dz2 = nullptr, *dy = nullptr, *sq = nullptr;
     int *  idx = nullptr, *err = nullptr;
     long long adam_t = 0;
-    int    grid = 152 * 2;
 };
 
 namespace {
@@ -43,7 +42,7 @@ template<class T> void tfree(T *& p) {
 
 int forward_batch(swc_trainer * t, const float * feat, long long n, float * out, bool save) {
     launch_mlp_forward_array(n, t->params, t->norm, feat, out, save ? t->z1 : nullptr, save ? t->h1 : nullptr,
-                             save ? t->z2 : nullptr, t->err, t->grid, t->st);
+                             save ? t->z2 : nullptr, t->err, t->st);
     return cudaGetLastError() == cudaSuccess ? SWC_OK : SWC_CUDA_ERROR;
 }
 
@@ -64,10 +63,6 @@ int swc_trainer_create(int64_t capacity, int32_t batch, swc_trainer ** out) {
     auto t = new swc_trainer();
     t->cap   = capacity;
     t->batch = batch;
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    t->grid  = sms * 2;
     const size_t B = size_t(batch);
     bool ok = cudaStreamCreateWithFlags(&t->st, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && talloc(&t->feat, size_t(capacity) * 6) && talloc(&t->tgt, size_t(capacity)) && talloc(&t->params, kP) &&

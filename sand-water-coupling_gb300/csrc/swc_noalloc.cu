@@ -103,12 +103,8 @@ extern "C" int swc_mlp_gradient_noalloc(const float * d_params, const float * d_
     int rc = scratch_for_current_device(s);
     if (rc) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (cudaMemsetAsync(s.err, 0, sizeof(int), st) != cudaSuccess) return SWC_CUDA_ERROR;
-    launch_mlp_forward_array(n, d_params, d_norm, d_features, s.pred, s.z1, s.h1, s.z2, s.err,
-                             std::min(sms * 2, int((n + 127) / 128)), st);
+    launch_mlp_forward_array(n, d_params, d_norm, d_features, s.pred, s.z1, s.h1, s.z2, s.err, st);
     launch_mlp_backward(n, d_params, d_norm, d_features, s.pred, d_targets, s.z1, s.h1, s.z2, s.dz1, s.dz2, s.dy, s.sq,
                         d_grad, st);
     k_noalloc_loss<<<1, 256, 0, st>>>(n, d_loss);

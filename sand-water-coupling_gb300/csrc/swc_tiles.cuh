@@ -116,8 +116,9 @@ template<int DIM> struct RowGeom {
 // Halo tile with 16-byte loads: the tile is read as 4-node x-segments, each of
 // which lies inside one brick and is 16-byte aligned in the brick layout.
 // get4(slot) returns the 4 values starting at `slot`; nodes outside the lattice
-// or in inactive bricks read as zero.
-template<int DIM, int NT = RowGeom<DIM>::NT, class Get4>
+// or in inactive bricks read as zero.  PITCH: row pitch of the tile in floats
+// (a multiple of 4).
+template<int DIM, int NT = RowGeom<DIM>::NT, int PITCH = BrickGeom<DIM>::PX, class Get4>
 __device__ __forceinline__ void load_tile4(const Lattice & L, const unsigned char * __restrict__ bflag, int3 bc,
                                            float * tile, Get4 get4) {
     using G            = BrickGeom<DIM>;
@@ -135,7 +136,7 @@ __device__ __forceinline__ void load_tile4(const Lattice & L, const unsigned cha
             if (bflag[nbk])
                 v = get4((long long) nbk * G::BN + (x - nbx * G::BX) + G::BX * ((y - nby * G::BY) + G::BY * (z - nbz * G::BZ)));
         }
-        *reinterpret_cast<float4 *>(tile + 4 * sx + G::PX * (ty + G::TY * tz)) = v;
+        *reinterpret_cast<float4 *>(tile + 4 * sx + PITCH * (ty + G::TY * tz)) = v;
     }
 }
 

@@ -19,8 +19,9 @@ SWC_CUDA_ERROR = 4
 SWC_NOT_INITIALIZED = 5
 SWC_OUT_OF_MEMORY = 6
 
-WARM_PREFIX, WARM_NODE, WARM_ZERO, WARM_LEARNED = 0, 1, 2, 3
-WARM_NAMES = {"prefix": WARM_PREFIX, "node": WARM_NODE, "zero": WARM_ZERO, "learned": WARM_LEARNED}
+WARM_PREFIX, WARM_NODE, WARM_ZERO, WARM_LEARNED, WARM_EXTRAPOLATE = 0, 1, 2, 3, 4
+WARM_NAMES = {"prefix": WARM_PREFIX, "node": WARM_NODE, "zero": WARM_ZERO, "learned": WARM_LEARNED,
+              "extrapolate": WARM_EXTRAPOLATE}
 
 
 class Scene(C.Structure):

@@ -207,6 +207,38 @@ def test_warm_start_modes_agree(swc_mod, oracle_mod):
     assert results["node"][1] <= results["zero"][1]
 
 
+def test_extrapolated_warm_start(swc_mod):
+    """Warm start extrapolated in time per lattice node (2 p_{n-1} - p_{n-2}): the
+    same solution as the node-mapped start to the CG tolerance; the node-mapped
+    start on the first advance (no history) and after a standalone project() or a
+    switch into the mode, the extrapolation from the next advance on."""
+    base = SCENES["block_3d_n24"]().rounded_to_float32()
+    out = {}
+    for mode in ("node", "extrapolate"):
+        liq = swc_mod.DualParticleSphLiquid(base, warm_start=mode, compute_true_residual=True)
+        liq.initialize()
+        its, used = [], []
+        for _ in range(8):
+            st = liq.advance(base.dt)
+            assert st["status"] == 0 and st["true_rel_residual"] < 5 * base.tolerance
+            its.append(st["cg_iterations"])
+            used.append(st["warm_start_used"])
+        out[mode] = (liq.getParticles()[1], np.array(its), used)
+        if mode == "extrapolate":
+            liq.project()
+            assert [liq.advance(base.dt)["warm_start_used"] for _ in range(2)] == [1, 4]
+        else:
+            liq.setSolverOptions(warm_start="extrapolate")
+            assert [liq.advance(base.dt)["warm_start_used"] for _ in range(2)] == [1, 4]
+        liq.close()
+    v_node, it_node, _ = out["node"]
+    v_ex, it_ex, used = out["extrapolate"]
+    assert used == [1] + [4] * 7  # SWC_WARM_NODE, then SWC_WARM_EXTRAPOLATE
+    assert rel(v_ex, v_node) < 1e-4
+    assert it_ex[2:].mean() <= it_node[2:].mean() + 1.0
+    print(f"\nCG iterations  node-mapped: {it_node.tolist()}  extrapolated: {it_ex.tolist()}")
+
+
 def test_deterministic_repeat(swc_mod):
     s = SCENES["block_3d_n16"]().rounded_to_float32()
     outs = []
@@ -243,6 +275,9 @@ def test_status_codes(swc_mod):
     assert liq3.project()["status"] == 0
     with pytest.raises(swc_mod.SwcError):
         liq3.setParticles(x[:10], v[:10])  # count change after initialize
+    with pytest.raises(swc_mod.SwcError) as e:
+        liq3.setSolverOptions(warm_start=5)  # no such warm-start mode
+    assert e.value.status == 3
 
 
 def test_frame_roundtrip(swc_mod, tmp_path):
