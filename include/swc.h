@@ -173,27 +173,37 @@ int swc_get_phase_times(swc_ctx * ctx, double * ms, int n);
 int swc_time_kernel(swc_ctx * ctx, int which, int reps, double * mean_ms);
 
 /* ---- Learned CG warm start (no counterpart in the reference) -------------
- * A per-virtual-particle MLP 6 -> 64 -> 64 -> 1 (SiLU), BF16 tensor-core
- * forward with FP32 accumulation, predicts the change of each node's pressure
- * from the previous step.  Features of active node I (raw, before the
- * normalisation carried with the network):
- *   f0 = D_I / sD            f1 = alpha_hat_I / alpha0    f2 = nreal_I / 32
- *   f3 = nvirt_I / 251 (45 in 2D)   f4 = p_prev_I alpha_hat_I / sD   f5 = rho_I / rho0
- * with sD the RMS of D over active nodes, p_prev the previous pressure of the
- * same node (0 for new nodes), nreal / nvirt the real particles within h and
- * active virtual particles within H (self included).  Target / prediction:
- *   t = (p_I - p_prev_I) alpha_hat_I / sD,  warm start p0_I = p_prev_I + t sD / alpha_hat_I.
- * Parameters (SWC_MLP_PARAMS floats): W1[64][6], b1[64], W2[64][64], b2[64], w3[64], b3.
- * Normalisation (SWC_MLP_NORM floats): feature mean[6], feature std[6], target mean, target std. */
-#define SWC_MLP_PARAMS 4673
-#define SWC_MLP_NORM 14
+ * A per-virtual-particle MLP 8 -> 64 -> 64 -> 1 (SiLU), BF16 tensor-core
+ * forward with FP32 accumulation, predicts a correction of the time-
+ * extrapolated pressure of each node.  With p1, p2, p3 the pressures of the
+ * same lattice node one, two and three advance steps back (0 where the node
+ * was inactive or the history is shorter), the base start is
+ *   p_base_I = 2 p1 - p2 where the node has two steps of history, else p1.
+ * In units w = alpha_hat_I / sD (sD the RMS of D over active nodes):
+ *   d1 = (p_base - p1) w,  d2 = (p1 - 2 p2 + p3) w (0 without three steps),
+ *   q = p1 w,  s = sqrt(d1^2 + d2^2) + SWC_MLP_SCALE_EPS (the node's history scale).
+ * Features of active node I (raw, before the normalisation carried with the
+ * network):
+ *   f0 = D_I / sD     f1 = alpha_hat_I / alpha0    f2 = nreal_I / 32 (real particles within h)
+ *   f3 = d1 / s       f4 = d2 / s                  f5 = ln s
+ *   f6 = q / (|q| + s)                             f7 = rho_I / rho0
+ * Target / prediction, in units of the history scale (so every step weighs the
+ * same however small its change):
+ *   t = (p_I - p_base_I) w / s,  warm start p0_I = p_base_I + t s / w.
+ * Parameters (SWC_MLP_PARAMS floats): W1[64][8], b1[64], W2[64][64], b2[64], w3[64], b3.
+ * Normalisation (SWC_MLP_NORM floats): feature mean[8], feature std[8], target mean, target std. */
+#define SWC_MLP_IN 8
+#define SWC_MLP_PARAMS (64 * SWC_MLP_IN + 64 + 64 * 64 + 64 + 64 + 1)
+#define SWC_MLP_NORM (2 * SWC_MLP_IN + 2)
+#define SWC_MLP_SCALE_EPS 1e-4f
 /* Network used by SWC_WARM_LEARNED.  Each learned solve computes the initial
- * residual of both the prediction and the node-mapped previous pressure and
- * starts CG from the smaller (stats.warm_start_used tells which). */
+ * residual of both the prediction and the base start and starts CG from the
+ * smaller unless learned_no_fallback is set (stats.warm_start_used tells
+ * which: LEARNED, else EXTRAPOLATE or NODE for the base). */
 int swc_set_mlp(swc_ctx * ctx, const float * params, const float * norm);
 /* Training data of the last projection (needs keep_features): features
- * (n x 6, reference order) and targets (n) as defined above.  Returns the
- * count in *n (<= capacity). */
+ * (n x SWC_MLP_IN, reference order) and targets (n) as defined above.  Returns
+ * the count in *n (<= capacity). */
 int swc_get_features(swc_ctx * ctx, float * features, float * targets, int64_t capacity, int64_t * n);
 
 /* Device-side training of the network (forward on tensor cores, FP32 backward,
@@ -216,7 +226,7 @@ int swc_mlp_gradient(const float * params, const float * norm, const float * fea
  * device memory when they need it (frameworks that plan all device memory up
  * front, callers under a fixed memory budget).  No counterpart in the reference.
  * It allocates nothing: all pointers are device pointers supplied by the caller
- * (params[SWC_MLP_PARAMS], norm[SWC_MLP_NORM], features[n][6], targets[n],
+ * (params[SWC_MLP_PARAMS], norm[SWC_MLP_NORM], features[n][SWC_MLP_IN], targets[n],
  * grad[SWC_MLP_PARAMS] and loss[1] out), work is queued on `stream` (NULL: the
  * default stream) and its scratch lives in fixed device arrays for at most
  * SWC_MLP_NOALLOC_MAX_ROWS rows (about 2.7 MB per device, held until the process

@@ -4,7 +4,7 @@ The reference has no learned component; this restates the network the GPU
 kernels implement so their forward pass, gradients and Adam steps can be
 checked:
 
-    x  = (f - f_mean) / f_std                      6 features
+    x  = (f - f_mean) / f_std                      8 features
     z1 = W1 x + b1,  h1 = silu(z1)                 64
     z2 = W2 h1 + b2, h2 = silu(z2)                 64
     y  = w3 . h2 + b3
@@ -15,15 +15,15 @@ silu(z) = z / (1 + exp(-z)) (Elfwing et al. 2018); Adam as in Kingma & Ba
 (round to nearest even) where the tensor-core path does, so the GPU forward can
 be compared with a tight tolerance.
 
-Parameter vector layout (float32, length 4673):
-    W1[64][6], b1[64], W2[64][64], b2[64], w3[64], b3
-Normalisation vector (length 14): f_mean[6], f_std[6], t_mean, t_std.
+Parameter vector layout (float32, length 4801):
+    W1[64][8], b1[64], W2[64][64], b2[64], w3[64], b3
+Normalisation vector (length 18): f_mean[8], f_std[8], t_mean, t_std.
 """
 from __future__ import annotations
 
 import numpy as np
 
-N_IN, N_H = 6, 64
+N_IN, N_H = 8, 64
 N_PARAMS = N_H * N_IN + N_H + N_H * N_H + N_H + N_H + 1
 
 
@@ -72,7 +72,7 @@ def init_params(seed=0):
 def forward(params, norm, feats, bf16=False, cache=False):
     W1, b1, W2, b2, w3, b3 = unpack(params)
     norm = np.asarray(norm, dtype=np.float64)
-    x = (np.asarray(feats, dtype=np.float64) - norm[:6]) / norm[6:12]
+    x = (np.asarray(feats, dtype=np.float64) - norm[:N_IN]) / norm[N_IN:2 * N_IN]
     if bf16:
         x, W1, W2 = bf16_round(x), bf16_round(W1), bf16_round(W2)
     z1 = x @ W1.T + b1
@@ -82,7 +82,7 @@ def forward(params, norm, feats, bf16=False, cache=False):
     z2 = h1 @ W2.T + b2
     h2 = silu(z2)
     y = h2 @ w3 + b3
-    t = norm[12] + norm[13] * y
+    t = norm[2 * N_IN] + norm[2 * N_IN + 1] * y
     if cache:
         return t, (x, z1, h1, z2, h2, y)
     return t
@@ -93,7 +93,7 @@ def loss_and_grad(params, norm, feats, target):
     W1, b1, W2, b2, w3, b3 = unpack(params)
     norm = np.asarray(norm, dtype=np.float64)
     _, (x, z1, h1, z2, h2, y) = forward(params, norm, feats, cache=True)
-    ty = (np.asarray(target, dtype=np.float64) - norm[12]) / norm[13]
+    ty = (np.asarray(target, dtype=np.float64) - norm[2 * N_IN]) / norm[2 * N_IN + 1]
     n = y.shape[0]
     e = y - ty
     loss = float(np.mean(e * e))

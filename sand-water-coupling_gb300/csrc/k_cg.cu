@@ -48,20 +48,16 @@ template<int DIM> __device__ __forceinline__ long long row_base(int b, int ly, i
     return (long long) b * G::BN + G::BX * (ly + G::BY * lz);
 }
 
-// alpha_hat_I = max(-sum_J alpha_IJ, alpha0) (calculateCoef, VirtualParticle.cpp:149-169);
-// optionally the number of active virtual neighbours within H (self included).
+// alpha_hat_I = max(-sum_J alpha_IJ, alpha0) (calculateCoef, VirtualParticle.cpp:149-169).
 template<int DIM>
 __global__ void __launch_bounds__(KG<DIM>::BT) k_ahat(Lattice L, Phys P, const int * __restrict__ blist,
                                                       const int * __restrict__ bcount,
                                                       const unsigned char * __restrict__ bflag, NodeArrays N,
-                                                      Stencil S, unsigned short * __restrict__ nvirt) {
+                                                      Stencil S) {
     using G = BrickGeom<DIM>;
     __shared__ __align__(16) float tile[G::TILE];
     const int nb = *bcount;
     const int t = threadIdx.x, ly = t % G::BY, lz = t / G::BY;
-    Stencil ones;
-#pragma unroll
-    for (int k = 0; k < 16; k++) ones.c[k] = 1.f;
     for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
         const int b   = blist[bi];
         const int3 bc = brick_coords(L, b);
@@ -81,23 +77,6 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_ahat(Lattice L, Phys P, const i
                 a.z = f.z ? fmaxf(-acc[4 * k + 2], P.alpha0) : 1.f;
                 a.w = f.w ? fmaxf(-acc[4 * k + 3], P.alpha0) : 1.f;
                 st4(N.ahat, base + 4 * k, a);
-            }
-        }
-        if (nvirt) {
-            // V_J > 0 exactly on active nodes: count them with a unit stencil
-            __syncthreads();
-            load_tile4<DIM>(L, bflag, bc, tile, [&](long long s) {
-                const float4 v = ld4(N.V, s);
-                return make_float4(v.x > 0.f, v.y > 0.f, v.z > 0.f, v.w > 0.f);
-            });
-            __syncthreads();
-            if (t < KG<DIM>::NT) {
-                float acc[G::BX];
-                stencil_row<DIM>(tile, ly, lz, ones, acc);
-                const long long base = row_base<DIM>(b, ly, lz);
-#pragma unroll
-                for (int i = 0; i < G::BX; i++)
-                    nvirt[base + i] = N.flag[base + i] ? (unsigned short) (acc[i] + 1.5f) : 0;
             }
         }
     }
@@ -459,8 +438,8 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_true_residual(Lattice L, const 
 // ---------------------------------------------------------------------------
 template<int DIM>
 void launch_ahat(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
-                 unsigned short * nvirt, int sgrid, cudaStream_t st) {
-    k_ahat<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, P, B.list, B.count, B.flag, N, S, nvirt);
+                 int sgrid, cudaStream_t st) {
+    k_ahat<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, P, B.list, B.count, B.flag, N, S);
 }
 template<int DIM>
 void launch_apply_operator(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
@@ -534,7 +513,7 @@ void launch_rhs_norm(const BrickArrays & B, const NodeArrays & N, CgState * cg, 
 
 #define SWC_INST(D)                                                                                                    \
     template void launch_ahat<D>(const Lattice &, const Phys &, const BrickArrays &, const NodeArrays &,               \
-                                 const Stencil &, unsigned short *, int, cudaStream_t);                                \
+                                 const Stencil &, int, cudaStream_t);                                                  \
     template void launch_apply_operator<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,   \
                                            const float *, float *, int, cudaStream_t);                                 \
     template void launch_cg_init<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,         \

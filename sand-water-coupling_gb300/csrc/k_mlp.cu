@@ -1,8 +1,8 @@
-// k_mlp.cu -- learned CG warm start: a per-virtual-particle MLP 6 -> 64 -> 64 -> 1
-// (SiLU) predicting the pressure change of a node from local features.  No
-// counterpart in the reference; CG still iterates to the same tolerance and the
-// node-mapped previous pressure is kept whenever the prediction starts from a
-// larger residual.
+// k_mlp.cu -- learned CG warm start: a per-virtual-particle MLP 8 -> 64 -> 64 -> 1
+// (SiLU) predicting a correction of a node's time-extrapolated pressure from
+// local features and the node's pressure history.  No counterpart in the
+// reference; CG still iterates to the same tolerance and the extrapolated base
+// start is kept whenever the prediction starts from a larger residual.
 //
 // Forward pass on the 5th-generation tensor cores: M = 128 rows (nodes) per tile,
 // BF16 operands staged in shared memory in the K-major no-swizzle canonical
@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cstdio>
 
+#include "../../include/swc.h"
 #include "swc_kernels.h"
 
 namespace swc {
@@ -120,25 +121,47 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     return *reinterpret_cast<const uint32_t *>(&v);
 }
 
-constexpr int kMlpIn = 6, kMlpH = 64;
+constexpr int kMlpIn = SWC_MLP_IN, kMlpH = 64;
 constexpr int kMlpParams = kMlpH * kMlpIn + kMlpH + kMlpH * kMlpH + kMlpH + kMlpH + 1;
+static_assert(kMlpParams == SWC_MLP_PARAMS && 2 * kMlpIn + 2 == SWC_MLP_NORM, "MLP layout");
+static_assert(kMlpIn <= 8, "the X row holds the features in its first 16-byte core-matrix row");
 constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kMlpH * kMlpIn, kOffW2 = kOffB1 + kMlpH, kOffB2 = kOffW2 + kMlpH * kMlpH,
               kOffW3 = kOffB2 + kMlpH, kOffB3 = kOffW3 + kMlpH;
 constexpr int kMlpNT = 128;  // threads = rows per tile
 
-// Per-node raw features (see the host documentation of swc_get_features).
+// Per-node features (the definitions of include/swc.h) from the raw node
+// values D, alpha_hat, n_real, p_base (x after the history warm start), p1
+// (xm1), p1 - 2 p2 + p3 (d2p) and rho, held in g[0..6].  Returns the node's
+// history scale s (the unit of the target).
 struct FeatScale {
-    float inv_sD, inv_alpha0, inv_rho0, inv_nreal, inv_nvirt;
+    float inv_sD, inv_alpha0, inv_rho0, inv_nreal;
 };
-
-__device__ __forceinline__ void node_features(const NodeArrays & N, long long s, const FeatScale & F, float (&f)[6]) {
-    const float ah = N.ahat[s];
-    f[0] = N.D[s] * F.inv_sD;
-    f[1] = ah * F.inv_alpha0;
-    f[2] = (N.nreal ? float(N.nreal[s]) : 0.f) * F.inv_nreal;
-    f[3] = (N.nvirt ? float(N.nvirt[s]) : 0.f) * F.inv_nvirt;
-    f[4] = N.x[s] * ah * F.inv_sD;  // x holds the node-mapped previous pressure here
-    f[5] = N.rho[s] * F.inv_rho0;
+constexpr float kMlpScaleEps = SWC_MLP_SCALE_EPS;
+static_assert(kMlpIn == 8, "feature layout");
+__device__ __forceinline__ void node_raw(const NodeArrays & N, long long s, float (&g)[kMlpIn]) {
+    g[0] = N.D[s];
+    g[1] = N.ahat[s];
+    g[2] = N.nreal ? float(N.nreal[s]) : 0.f;
+    g[3] = N.x[s];
+    g[4] = N.xm1[s];
+    g[5] = N.d2p ? N.d2p[s] : 0.f;
+    g[6] = N.rho[s];
+    g[7] = 0.f;
+}
+__device__ __forceinline__ float node_features(const float (&g)[kMlpIn], const FeatScale & F, float (&f)[kMlpIn]) {
+    const float w  = g[1] * F.inv_sD;
+    const float d1 = (g[3] - g[4]) * w, d2 = g[5] * w, q = g[4] * w;
+    const float sc = sqrtf(fmaf(d1, d1, d2 * d2)) + kMlpScaleEps;
+    const float is = 1.f / sc;
+    f[0] = g[0] * F.inv_sD;
+    f[1] = g[1] * F.inv_alpha0;
+    f[2] = g[2] * F.inv_nreal;
+    f[3] = d1 * is;
+    f[4] = d2 * is;
+    f[5] = __logf(sc);
+    f[6] = q / (fabsf(q) + sc);
+    f[7] = g[6] * F.inv_rho0;
+    return sc;
 }
 
 // Modes of the forward kernel.
@@ -157,11 +180,11 @@ __device__ __forceinline__ float tanh_fast(float h) {
     return t;
 }
 
-// params: FP32 vector (layout above); norm: f_mean[6], f_std[6], t_mean, t_std.
-// kMlpFromArray: rows of feat[n][6] -> out[n] (prediction t); with SAVE, the
-//   pre-activations z1, z2 and h1 (bf16-rounded) for training.
+// params: FP32 vector (layout above); norm: f_mean[kMlpIn], f_std[kMlpIn], t_mean, t_std.
+// kMlpFromArray: rows of feat[n][kMlpIn] -> out[n] (prediction t); with SAVE,
+//   the pre-activations z1, z2 and h1 (bf16-rounded) for training.
 // kMlpFromNodes: rows = active nodes (slot_of[I]); writes the warm start
-//   x[s] = p_prev + t * sD / alpha_hat into N.x (and feat_out when non-null).
+//   x[s] = p_base + t * sD / alpha_hat into N.x (and feat_out when non-null).
 //
 // Arithmetic: W1, b1, W2, b2 are scaled by 1/2 when staged (exact in bf16 and
 // FP32), so the accumulators hold h = z/2 and silu(z) = h + h tanh(h) is one
@@ -175,11 +198,11 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
                   float * __restrict__ h1s, float * __restrict__ z2s, NodeArrays N, const int * __restrict__ slot_of,
                   const int * __restrict__ nv, const CgState * __restrict__ cg, FeatScale F0,
                   float * __restrict__ feat_out, int * __restrict__ err) {
-    __shared__ __align__(1024) uint8_t sw1[kMlpH * 16 * 2];   // W1/2 [64 x 16] bf16 (K padded 6 -> 16)
+    __shared__ __align__(1024) uint8_t sw1[kMlpH * 16 * 2];   // W1/2 [64 x 16] bf16 (K padded to 16)
     __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpH * 2];  // W2/2 [64 x 64]
     __shared__ __align__(1024) uint8_t sh[kMlpNT * kMlpH * 2];  // H1 [128 x 64]; X [128 x 16] in its first 4 KB
     __shared__ float2 sb1[kMlpH / 2], sb2[kMlpH / 2], sw3[kMlpH / 2];  // b1/2, b2/2, w3 as pairs
-    __shared__ float snorm[14];
+    __shared__ float snorm[SWC_MLP_NORM];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
     __shared__ int s_fail;
@@ -218,7 +241,7 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
         sb2[tid] = make_float2(0.5f * params[kOffB2 + 2 * tid], 0.5f * params[kOffB2 + 2 * tid + 1]);
         sw3[tid] = make_float2(params[kOffW3 + 2 * tid], params[kOffW3 + 2 * tid + 1]);
     }
-    if (tid < 14) snorm[tid] = norm[tid];
+    if (tid < SWC_MLP_NORM) snorm[tid] = norm[tid];
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     fence_async_smem();
     tc_fence_before();
@@ -228,11 +251,11 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
     const uint32_t tacc = tmem_base + (uint32_t(warp * 32) << 16);  // this warp's 32 lanes
     const uint64_t dW1 = smem_desc(smem_u32(sw1), 128, 256), dW2 = smem_desc(smem_u32(sw2), 128, 1024);
     const uint64_t dX = smem_desc(smem_u32(sx), 128, 256), dH = smem_desc(smem_u32(sh), 128, 1024);
-    float mean[6], inv_std[6];
+    float mean[kMlpIn], inv_std[kMlpIn];
 #pragma unroll
-    for (int k = 0; k < 6; k++) {
+    for (int k = 0; k < kMlpIn; k++) {
         mean[k]    = snorm[k];
-        inv_std[k] = 1.f / snorm[6 + k];
+        inv_std[k] = 1.f / snorm[kMlpIn + k];
     }
 
     long long rows = n;
@@ -245,55 +268,47 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
     }
     uint32_t phase = 0;
     const long long ntiles = (rows + kMlpNT - 1) / kMlpNT;
-    // Raw inputs of a tile row, gathered one tile ahead: the six features in
-    // array mode; D, alpha_hat, n_real, n_virt, p_prev, rho at slot_of[r] in node mode.
-    auto gather = [&](long long r, float (&g)[6], long long & gs) {
+    // Inputs of a tile row, gathered one tile ahead: the features in array
+    // mode; the raw node values of node_raw at slot_of[r] in node mode.
+    auto gather = [&](long long r, float (&g)[kMlpIn], long long & gs) {
 #pragma unroll
-        for (int k = 0; k < 6; k++) g[k] = 0.f;
+        for (int k = 0; k < kMlpIn; k++) g[k] = 0.f;
         gs = 0;
         if (r >= rows) return;
         if (MODE == kMlpFromArray) {
 #pragma unroll
-            for (int k = 0; k < 6; k++) g[k] = feat[r * 6 + k];
+            for (int k = 0; k < kMlpIn; k++) g[k] = feat[r * kMlpIn + k];
         } else {
-            gs   = slot_of[r];
-            g[0] = N.D[gs];
-            g[1] = N.ahat[gs];
-            g[2] = N.nreal ? float(N.nreal[gs]) : 0.f;
-            g[3] = N.nvirt ? float(N.nvirt[gs]) : 0.f;
-            g[4] = N.x[gs];  // node-mapped previous pressure
-            g[5] = N.rho[gs];
+            gs = slot_of[r];
+            node_raw(N, gs, g);
         }
     };
-    float fn[6];
+    float gn[kMlpIn];
     long long sn = 0;
-    gather(blockIdx.x * (long long) kMlpNT + tid, fn, sn);
+    gather(blockIdx.x * (long long) kMlpNT + tid, gn, sn);
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const long long row = tile * kMlpNT + tid;
         const bool valid    = row < rows;
-        float f[6];
-#pragma unroll
-        for (int k = 0; k < 6; k++) f[k] = fn[k];
-        const float ah = fn[1], pp = fn[4];
-        const long long s = sn;
-        if (MODE == kMlpFromNodes) {  // raw inputs -> features (as node_features)
-            f[0] = f[0] * F.inv_sD;
-            f[1] = ah * F.inv_alpha0;
-            f[2] = f[2] * F.inv_nreal;
-            f[3] = f[3] * F.inv_nvirt;
-            f[4] = pp * ah * F.inv_sD;
-            f[5] = f[5] * F.inv_rho0;
+        const long long s   = sn;
+        const float ah = gn[1], base = gn[3];
+        float f[kMlpIn];
+        float sc = 1.f;
+        if (MODE == kMlpFromNodes) {
+            sc = node_features(gn, F, f);
             if (valid && feat_out) {
 #pragma unroll
-                for (int k = 0; k < 6; k++) feat_out[row * 6 + k] = f[k];
+                for (int k = 0; k < kMlpIn; k++) feat_out[row * kMlpIn + k] = f[k];
             }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kMlpIn; k++) f[k] = gn[k];
         }
         // X row: normalised features in bf16, K padded to 16
-        float xn[6];
+        float xn[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int k = 0; k < 6; k++) xn[k] = valid ? (f[k] - mean[k]) * inv_std[k] : 0.f;
+        for (int k = 0; k < kMlpIn; k++) xn[k] = valid ? (f[k] - mean[k]) * inv_std[k] : 0.f;
         *reinterpret_cast<uint4 *>(sx + canon_off(tid, 0, 16)) =
-            make_uint4(pack_bf16(xn[0], xn[1]), pack_bf16(xn[2], xn[3]), pack_bf16(xn[4], xn[5]), 0u);
+            make_uint4(pack_bf16(xn[0], xn[1]), pack_bf16(xn[2], xn[3]), pack_bf16(xn[4], xn[5]), pack_bf16(xn[6], xn[7]));
         *reinterpret_cast<uint4 *>(sx + canon_off(tid, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
         fence_async_smem();
         tc_fence_before();
@@ -304,7 +319,7 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
             mma_commit(&mbar);
         }
         // the next tile's gathers are in flight while this tile's MMAs run
-        gather((tile + gridDim.x) * kMlpNT + tid, fn, sn);
+        gather((tile + gridDim.x) * kMlpNT + tid, gn, sn);
         if (!mbar_wait(&mbar, phase)) s_fail = 1;
         phase ^= 1u;
         tc_fence_after();
@@ -364,10 +379,10 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
                 y2             = fma2(sw3[c], a, y2);
             }
         }
-        const float t = snorm[12] + snorm[13] * (b3 + (y2.x + y2.y));
+        const float t = snorm[2 * kMlpIn] + snorm[2 * kMlpIn + 1] * (b3 + (y2.x + y2.y));
         if (valid) {
             if (MODE == kMlpFromArray) out[row] = t;
-            else N.x[s] = pp + t / (F.inv_sD * ah);
+            else N.x[s] = base + sc * t / (F.inv_sD * ah);
         }
         tc_fence_before();
         __syncthreads();
@@ -400,7 +415,7 @@ __global__ void __launch_bounds__(128) k_mlp_backward_rows(long long n, const fl
     for (int e = threadIdx.x; e < kMlpH * kMlpH; e += blockDim.x) w2t[e % kMlpH][e / kMlpH] = params[kOffW2 + e];
     if (threadIdx.x < kMlpH) w3[threadIdx.x] = params[kOffW3 + threadIdx.x];
     __syncthreads();
-    const float tm = norm[12], ts = norm[13];
+    const float tm = norm[2 * kMlpIn], ts = norm[2 * kMlpIn + 1];
     for (long long r = blockIdx.x * (long long) blockDim.x + threadIdx.x; r < n; r += (long long) gridDim.x * blockDim.x) {
         const float y  = (pred[r] - tm) / ts;
         const float ty = (target[r] - tm) / ts;
@@ -505,10 +520,11 @@ __global__ void __launch_bounds__(256) k_slot_of(Lattice L, const int * __restri
     }
 }
 
-// Target of the learned warm start for logging: (p - p_prev) alpha_hat / sD, with
-// p_prev the value kept in `prev` (node-mapped previous pressure).
+// Target of the learned warm start for logging: (p - p_base) alpha_hat / (sD s),
+// with p_base the base start kept in `prev` and s the node's history scale.
 __global__ void k_mlp_targets(const int * __restrict__ nv, const int * __restrict__ slot_of,
                               const float * __restrict__ x, const float * __restrict__ prev,
+                              const float * __restrict__ xm1, const float * __restrict__ d2p,
                               const float * __restrict__ ahat, const CgState * __restrict__ cg,
                               float * __restrict__ target) {
     const long long rows = *nv;
@@ -516,32 +532,36 @@ __global__ void k_mlp_targets(const int * __restrict__ nv, const int * __restric
     const float inv = sD > 0 ? float(1.0 / sD) : 0.f;
     for (long long r = blockIdx.x * (long long) blockDim.x + threadIdx.x; r < rows; r += (long long) gridDim.x * blockDim.x) {
         const long long s = slot_of[r];
-        target[r]         = (x[s] - prev[s]) * ahat[s] * inv;
+        const float w     = ahat[s] * inv;
+        const float d1 = (prev[s] - xm1[s]) * w, d2 = (d2p ? d2p[s] : 0.f) * w;
+        const float sc    = sqrtf(fmaf(d1, d1, d2 * d2)) + kMlpScaleEps;
+        target[r]         = (x[s] - prev[s]) * w / sc;
     }
 }
 
-// Features of every active node (training-data logging), x holding p_prev.
+// Features of every active node (training-data logging), x holding p_base.
 __global__ void k_node_features(NodeArrays N, const int * __restrict__ slot_of, const int * __restrict__ nv,
                                 const CgState * __restrict__ cg, FeatScale F, float * __restrict__ feat_out) {
     const long long rows = *nv;
     const double sD      = rows > 0 ? sqrt(cg->bb / double(rows)) : 1.0;
     F.inv_sD             = sD > 0 ? float(1.0 / sD) : 0.f;
     for (long long r = blockIdx.x * (long long) blockDim.x + threadIdx.x; r < rows; r += (long long) gridDim.x * blockDim.x) {
-        float f[6];
-        node_features(N, slot_of[r], F, f);
+        float g[kMlpIn], f[kMlpIn];
+        node_raw(N, slot_of[r], g);
+        node_features(g, F, f);
 #pragma unroll
-        for (int k = 0; k < 6; k++) feat_out[r * 6 + k] = f[k];
+        for (int k = 0; k < kMlpIn; k++) feat_out[r * kMlpIn + k] = f[k];
     }
 }
 
-// Batch gather for training: dst[i] = src[idx[i]] (6 features), dst_t[i] = src_t[idx[i]].
+// Batch gather for training: dst[i] = src[idx[i]] (kMlpIn features), dst_t[i] = src_t[idx[i]].
 __global__ void k_gather_rows(const float * __restrict__ src, const float * __restrict__ src_t,
                               const int * __restrict__ idx, long long n, float * __restrict__ dst,
                               float * __restrict__ dst_t) {
     for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
         const long long j = idx[i];
 #pragma unroll
-        for (int k = 0; k < 6; k++) dst[i * 6 + k] = src[j * 6 + k];
+        for (int k = 0; k < kMlpIn; k++) dst[i * kMlpIn + k] = src[j * kMlpIn + k];
         dst_t[i] = src_t[j];
     }
 }
@@ -550,10 +570,10 @@ __global__ void k_gather_rows(const float * __restrict__ src, const float * __re
 // Launchers
 // ---------------------------------------------------------------------------
 void launch_node_features(const NodeArrays & N, const int * slot_of, const int * nv, long long rows_max,
-                          const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal, float inv_nvirt,
-                          float * feat_out, cudaStream_t st) {
+                          const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal, float * feat_out,
+                          cudaStream_t st) {
     if (rows_max <= 0) return;
-    FeatScale F{0.f, inv_alpha0, inv_rho0, inv_nreal, inv_nvirt};
+    FeatScale F{0.f, inv_alpha0, inv_rho0, inv_nreal};
     k_node_features<<<int(std::min<long long>((rows_max + 255) / 256, 152 * 8)), 256, 0, st>>>(N, slot_of, nv, cg, F,
                                                                                              feat_out);
 }
@@ -639,9 +659,8 @@ void launch_mlp_forward_array(long long n, const float * params, const float * n
 }
 void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const int * slot_of,
                               const int * nv, long long rows_max, const CgState * cg, float inv_alpha0,
-                              float inv_rho0, float inv_nreal, float inv_nvirt, float * feat_out, int * err,
-                              cudaStream_t st) {
-    FeatScale F{0.f, inv_alpha0, inv_rho0, inv_nreal, inv_nvirt};
+                              float inv_rho0, float inv_nreal, float * feat_out, int * err, cudaStream_t st) {
+    FeatScale F{0.f, inv_alpha0, inv_rho0, inv_nreal};
     launch_forward<kMlpFromNodes, false>(rows_max, params, norm, nullptr, nullptr, nullptr, nullptr, nullptr, N,
                                          slot_of, nv, cg, F, feat_out, err, st);
 }
@@ -664,10 +683,11 @@ void launch_slot_of(const Lattice & L, const BrickArrays & B, const NodeArrays &
     k_slot_of<DIM><<<grid, 256, 0, st>>>(L, B.list, B.count, B.seg_off, N.flag, slot_of);
 }
 void launch_mlp_targets(long long rows_max, const int * nv, const int * slot_of, const float * x, const float * prev,
-                        const float * ahat, const CgState * cg, float * target, cudaStream_t st) {
+                        const float * xm1, const float * d2p, const float * ahat, const CgState * cg, float * target,
+                        cudaStream_t st) {
     if (rows_max <= 0) return;
-    k_mlp_targets<<<int(std::min<long long>((rows_max + 255) / 256, 152 * 8)), 256, 0, st>>>(nv, slot_of, x, prev,
-                                                                                           ahat, cg, target);
+    k_mlp_targets<<<int(std::min<long long>((rows_max + 255) / 256, 152 * 8)), 256, 0, st>>>(nv, slot_of, x, prev, xm1,
+                                                                                           d2p, ahat, cg, target);
 }
 template void launch_slot_of<2>(const Lattice &, const BrickArrays &, const NodeArrays &, int *, int, cudaStream_t);
 template void launch_slot_of<3>(const Lattice &, const BrickArrays &, const NodeArrays &, int *, int, cudaStream_t);

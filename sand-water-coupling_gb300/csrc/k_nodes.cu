@@ -308,19 +308,22 @@ __global__ void __launch_bounds__(kNT) k_diag_max_f64(Lattice L, const int * __r
 //   node:   previous pressure of the same node, 0 if it was inactive
 //   zero:   0
 //   given:  caller-supplied values in brick layout
-//   extrap: linear extrapolation in time of the same node's pressure,
-//           2 p_{n-1} - p_{n-2} where the node was active in both previous
-//           steps (bflag_m2 non-null: the history is valid), else p_{n-1}, else
-//           0; p_{n-1} is kept in xm1 for the next step.  xm1 is written for
-//           every slot of an active brick; slots whose value is stale there are
-//           masked by the activity flags of the next step.
+//   extrap: linear extrapolation in time of the same node's pressure.  With
+//           p1, p2, p3 the node's pressure one, two, three steps back (x,
+//           xm1, xm2 on entry; a value counts where the node was active at
+//           that step and `history` covers it), p0 = 2 p1 - p2 with two steps,
+//           p1 with one, else 0.  The history shifts (xm1 = p1, xm2 = p2, both
+//           0 where inactive) and, when d2p is allocated, d2p = p1 - 2 p2 + p3
+//           (0 without three steps).  Every slot of an active brick is
+//           written; a slot's history is read only when the node was active
+//           at every step it spans, which also means its brick was visited
+//           (and its history shifted) at each of those steps.
 // ---------------------------------------------------------------------------
 template<int DIM>
 __global__ void __launch_bounds__(kNT) k_warm_start(Lattice L, const int * __restrict__ blist,
                                                     const int * __restrict__ bcount, const int * __restrict__ seg_off,
-                                                    const unsigned char * __restrict__ bflag_prev,
-                                                    const unsigned char * __restrict__ bflag_m2, NodeArrays N,
-                                                    int mode, const float * __restrict__ pcomp,
+                                                    BrickArrays B, NodeArrays N, int mode, int history,
+                                                    const float * __restrict__ pcomp,
                                                     const int * __restrict__ nv_prev, const float * __restrict__ given) {
     using G      = BrickGeom<DIM>;
     const int nb = *bcount;
@@ -338,17 +341,21 @@ __global__ void __launch_bounds__(kNT) k_warm_start(Lattice L, const int * __res
                                                            bc.y * G::BY + ly, bc.z * G::BZ + lz, l);
                     v = I < np ? pcomp[I] : 0.f;
                 } else if (mode == kWarmNode) {
-                    v = (bflag_prev[b] && N.flag_prev[s]) ? N.x[s] : 0.f;
+                    v = (B.flag_prev[b] && N.flag_prev[s]) ? N.x[s] : 0.f;
                 } else if (mode == kWarmGiven) {
                     v = given[s];
-                } else if (mode == kWarmExtrap) {
-                    if (bflag_prev[b] && N.flag_prev[s]) {
-                        const float p1 = N.x[s];
-                        v = (bflag_m2 && bflag_m2[b] && N.flag_m2[s]) ? fmaf(2.f, p1, -N.xm1[s]) : p1;
-                    }
                 }
             }
-            if (mode == kWarmExtrap) N.xm1[s] = N.x[s];
+            if (mode == kWarmExtrap) {
+                const bool a1  = B.flag_prev[b] && N.flag_prev[s];
+                const bool a2  = a1 && history >= 1 && B.flag_m2[b] && N.flag_m2[s];
+                const bool a3  = a2 && history >= 2 && B.flag_m3[b] && N.flag_m3[s];
+                const float p1 = a1 ? N.x[s] : 0.f, p2 = a2 ? N.xm1[s] : 0.f, p3 = a3 ? N.xm2[s] : 0.f;
+                if (N.flag[s]) v = a2 ? fmaf(2.f, p1, -p2) : p1;
+                if (N.d2p) N.d2p[s] = a3 ? (p1 - 2.f * p2) + p3 : 0.f;
+                N.xm2[s] = p2;
+                N.xm1[s] = p1;
+            }
             N.x[s] = v;
         }
     }
@@ -712,9 +719,9 @@ void launch_diag_max_f64(const Lattice & L, const BrickArrays & B, const NodeArr
 
 template<int DIM>
 void launch_warm_start(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int mode, const float * pcomp,
-                       const int * nv_prev, const float * given, int grid, cudaStream_t st, bool history) {
-    k_warm_start<DIM><<<grid, kNT, 0, st>>>(L, B.list, B.count, B.seg_off, B.flag_prev,
-                                            history ? B.flag_m2 : nullptr, N, mode, pcomp, nv_prev, given);
+                       const int * nv_prev, const float * given, int grid, cudaStream_t st, int history) {
+    k_warm_start<DIM><<<grid, kNT, 0, st>>>(L, B.list, B.count, B.seg_off, B, N, mode, history, pcomp, nv_prev,
+                                            given);
 }
 
 template<int DIM>
@@ -757,7 +764,7 @@ void launch_zero_active(const Lattice & L, const BrickArrays & B, float * a, int
     template void launch_diag_max_f64<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const StencilD &,   \
                                          unsigned long long *, int, cudaStream_t);                                     \
     template void launch_warm_start<D>(const Lattice &, const BrickArrays &, const NodeArrays &, int, const float *,   \
-                                       const int *, const float *, int, cudaStream_t, bool);                           \
+                                       const int *, const float *, int, cudaStream_t, int);                            \
     template void launch_compact_export<D>(const Lattice &, const BrickArrays &, const NodeArrays &, float *,          \
                                            long long *, double *, double *, double *, double *, double *, double *,    \
                                            unsigned short *, int, cudaStream_t);                                       \

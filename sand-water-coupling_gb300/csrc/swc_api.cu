@@ -180,17 +180,22 @@ void free_sort(SortScratch & S) {
     dfree(S.id2);
 }
 
-// History of the extrapolated warm start (allocated on demand, zero history).
+// Pressure history of the extrapolated and learned warm starts (allocated on
+// demand, empty history).
 int ensure_extrap_buffers(swc_ctx * c) {
     if (c->N.xm1) return SWC_OK;
     const size_t slots = size_t(c->L.nbricks) * (c->dim == 3 ? 512 : 256);
     int rc;
-    if ((rc = dalloc(c, &c->N.flag_m2, slots)) || (rc = dalloc(c, &c->B.flag_m2, size_t(c->L.nbricks))) ||
-        (rc = dalloc(c, &c->N.xm1, slots)))
+    if ((rc = dalloc(c, &c->N.flag_m2, slots)) || (rc = dalloc(c, &c->N.flag_m3, slots)) ||
+        (rc = dalloc(c, &c->B.flag_m2, size_t(c->L.nbricks))) || (rc = dalloc(c, &c->B.flag_m3, size_t(c->L.nbricks))) ||
+        (rc = dalloc(c, &c->N.xm2, slots)) || (rc = dalloc(c, &c->N.xm1, slots)))
         return rc;
     CK(cudaMemset(c->N.flag_m2, 0, slots));
+    CK(cudaMemset(c->N.flag_m3, 0, slots));
     CK(cudaMemset(c->B.flag_m2, 0, size_t(c->L.nbricks)));
+    CK(cudaMemset(c->B.flag_m3, 0, size_t(c->L.nbricks)));
     CK(cudaMemset(c->N.xm1, 0, sizeof(float) * slots));
+    CK(cudaMemset(c->N.xm2, 0, sizeof(float) * slots));
     c->extrap_steps = 0;
     // the CG graphs captured the old NodeArrays: recapture
     if (c->g1) cudaGraphExecDestroy(c->g1);
@@ -205,11 +210,13 @@ int ensure_learn_buffers(swc_ctx * c) {
     const size_t slots = size_t(c->L.nbricks) * (c->dim == 3 ? 512 : 256);
     int rc;
     if ((rc = dalloc(c, &c->mlp_err, 1)) || (rc = dalloc(c, &c->slot_of, size_t(c->L.ncells))) ||
-        (rc = dalloc(c, &c->xprev, slots)) || (rc = dalloc(c, &c->feat_buf, size_t(c->L.ncells) * 6)) ||
+        (rc = dalloc(c, &c->xprev, slots)) || (rc = dalloc(c, &c->feat_buf, size_t(c->L.ncells) * SWC_MLP_IN)) ||
         (rc = dalloc(c, &c->tgt_buf, size_t(c->L.ncells))))
         return rc;
     if (!c->N.nreal && (rc = dalloc(c, &c->N.nreal, slots))) return rc;
-    if (!c->N.nvirt && (rc = dalloc(c, &c->N.nvirt, slots))) return rc;
+    if ((rc = ensure_extrap_buffers(c))) return rc;
+    if (!c->N.d2p && (rc = dalloc(c, &c->N.d2p, slots))) return rc;
+    CK(cudaMemset(c->N.d2p, 0, sizeof(float) * slots));
     CK(cudaMemset(c->mlp_err, 0, sizeof(int)));
     // the CG graphs captured the old NodeArrays (feature pointers): recapture
     if (c->g1) cudaGraphExecDestroy(c->g1);
@@ -287,7 +294,7 @@ template<int DIM> void run_generate(swc_ctx * c, bool with_ahat) {
     launch_node_gather<DIM>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel, c->bcellStart,
                             c->bnear, c->ggrid, c->queues, c->stream);
     launch_segments<DIM>(c->L, c->B, c->N, c->scan_tiles, c->grid, c->stream);
-    if (with_ahat) launch_ahat<DIM>(c->L, c->P, c->B, c->N, c->S, c->N.nvirt, c->rgrid, c->stream);
+    if (with_ahat) launch_ahat<DIM>(c->L, c->P, c->B, c->N, c->S, c->rgrid, c->stream);
 }
 
 int capture_graphs(swc_ctx * c) {
@@ -370,6 +377,14 @@ template<int DIM> int run_cg(swc_ctx * c, swc_stats * st, bool initialized) {
     return status;
 }
 
+// The projection keeps a pressure history (extrapolated or learned warm start,
+// training-data logging).
+bool history_on(const swc_ctx * c) {
+    const int mode = c->opts.warm_start;
+    return c->N.xm1 && (mode == SWC_WARM_EXTRAPOLATE || (mode == SWC_WARM_LEARNED && c->mlp_ready) ||
+                        (c->opts.keep_features && c->feat_buf));
+}
+
 // The shared tail of advance / project: virtual generation, projection, G_i.
 template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     mark(c, 3);
@@ -381,21 +396,24 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     const bool logging = c->opts.keep_features != 0 && c->feat_buf;
     const int * nv     = c->B.seg_off + c->B.nseg;
     const size_t slots = size_t(c->L.nbricks) * BrickGeom<DIM>::BN;
-    int used           = mode == SWC_WARM_LEARNED ? SWC_WARM_NODE : mode;
+    int used           = mode;
     bool initialized   = false;
-    // extrapolation in time needs the previous advance's history; without it the node-mapped start
-    const bool extrap  = mode == SWC_WARM_EXTRAPOLATE && c->N.xm1;
-    const bool history = extrap && c->extrap_shifted && c->extrap_steps >= 1;
-    const int wmode    = (mode == SWC_WARM_LEARNED || (mode == SWC_WARM_EXTRAPOLATE && !extrap)) ? kWarmNode : mode;
-    if (mode == SWC_WARM_EXTRAPOLATE && !history) used = SWC_WARM_NODE;
+    // Pressure history (extrapolated and learned warm starts, logged features):
+    // the base start is 2 p1 - p2 with two steps of history, p1 (node-mapped)
+    // with fewer; the history spans consecutive advance calls.
+    const bool hist_on  = history_on(c);
+    const int history   = (hist_on && c->extrap_shifted) ? std::min(c->extrap_steps, 2) : 0;
+    const int base_used = history >= 1 ? SWC_WARM_EXTRAPOLATE : SWC_WARM_NODE;
+    if (mode == SWC_WARM_EXTRAPOLATE || mode == SWC_WARM_LEARNED) used = base_used;
     if (learned || logging) {
-        // node-mapped previous pressure: the fallback, feature f4 and the target reference
-        launch_warm_start<DIM>(c->L, c->B, c->N, kWarmNode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
+        // base start (and history shift): the fallback, the network's base and the target reference
+        launch_warm_start<DIM>(c->L, c->B, c->N, kWarmExtrap, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream,
+                               history);
         CK(cudaMemcpyAsync(c->xprev, c->N.x, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
         launch_slot_of<DIM>(c->L, c->B, c->N, c->slot_of, c->grid, c->stream);
         c->slot_of_valid = true;
         // |b|^2 for sD and (for the fallback test) the initial residual of the
-        // node-mapped start, read back with the learned start's (one host synchronisation)
+        // base start, read back with the learned start's (one host synchronisation)
         const bool no_fallback = learned && c->opts.learned_no_fallback && !logging;
         if (no_fallback) launch_rhs_norm<DIM>(c->B, c->N, c->cg, c->partials, c->grid, c->stream);
         else {
@@ -404,42 +422,48 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
             CK(cudaMemcpyAsync(&c->hcg->rr_node, &c->cg->rr0, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         }
         int rc = SWC_OK;
-        const float inv_a0 = float(1.0 / c->alpha0), inv_r0 = float(1.0 / c->rho0), inv_nr = 1.f / 32.f,
-                    inv_nv = DIM == 3 ? 1.f / 251.f : 1.f / 45.f;
+        const float inv_a0 = float(1.0 / c->alpha0), inv_r0 = float(1.0 / c->rho0), inv_nr = 1.f / 32.f;
         if (logging)
-            launch_node_features(c->N, c->slot_of, nv, c->L.ncells, c->cg, inv_a0, inv_r0, inv_nr, inv_nv,
-                                 c->feat_buf, c->stream);
+            launch_node_features(c->N, c->slot_of, nv, c->L.ncells, c->cg, inv_a0, inv_r0, inv_nr, c->feat_buf,
+                                 c->stream);
         if (learned) {
             launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->slot_of, nv, (long long) slots, c->cg, inv_a0,
-                                     inv_r0, inv_nr, inv_nv, nullptr, c->mlp_err, c->stream);
+                                     inv_r0, inv_nr, nullptr, c->mlp_err, c->stream);
             CK(cudaMemcpyAsync(&c->hcg->mlp_err, c->mlp_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
             if ((rc = cg_init_sync<DIM>(c))) return rc;
             const int err        = c->hcg->mlp_err;
-            const double rr_node = c->hcg->rr_node, rr_mlp = c->hcg->st.rr0;
-            if (err || !(rr_mlp == rr_mlp) || (!c->opts.learned_no_fallback && !(rr_mlp <= rr_node))) {
-                // the prediction starts from a larger residual (or failed): keep the node-mapped start
+            const double rr_base = c->hcg->rr_node, rr_mlp = c->hcg->st.rr0;
+            if (err || !(rr_mlp == rr_mlp) || (!c->opts.learned_no_fallback && !(rr_mlp <= rr_base))) {
+                // the prediction starts from a larger residual (or failed): keep the base start
                 CK(cudaMemcpyAsync(c->N.x, c->xprev, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
                 if ((rc = cg_init_sync<DIM>(c))) return rc;
-                used = SWC_WARM_NODE;
+                used = base_used;
             } else used = SWC_WARM_LEARNED;
             initialized = true;
-        } else if (mode == SWC_WARM_NODE || mode == SWC_WARM_LEARNED) {
-            if ((rc = cg_init_sync<DIM>(c))) return rc;  // host copy of the node-mapped start's state
+        } else if (mode == SWC_WARM_EXTRAPOLATE || mode == SWC_WARM_LEARNED) {
+            if ((rc = cg_init_sync<DIM>(c))) return rc;  // host copy of the base start's state
             initialized = true;
+        } else if (mode == SWC_WARM_NODE) {
+            // node-mapped previous pressure, kept in xm1 by the history shift
+            CK(cudaMemcpyAsync(c->N.x, c->N.xm1, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
         } else {
-            launch_warm_start<DIM>(c->L, c->B, c->N, wmode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream,
-                                   history);
+            launch_warm_start<DIM>(c->L, c->B, c->N, mode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
         }
+    } else if (hist_on) {
+        launch_warm_start<DIM>(c->L, c->B, c->N, kWarmExtrap, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream,
+                               history);
     } else {
-        launch_warm_start<DIM>(c->L, c->B, c->N, wmode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream, history);
+        launch_warm_start<DIM>(c->L, c->B, c->N, mode == SWC_WARM_LEARNED || mode == SWC_WARM_EXTRAPOLATE ? kWarmNode : mode,
+                               c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
     }
     mark(c, 5);
     int rc = run_cg<DIM>(c, st, initialized);
-    c->extrap_steps   = (extrap && c->extrap_shifted && (rc == SWC_OK || rc == SWC_CG_NOT_CONVERGED)) ? c->extrap_steps + 1 : 0;
+    c->extrap_steps   = (hist_on && c->extrap_shifted && (rc == SWC_OK || rc == SWC_CG_NOT_CONVERGED)) ? c->extrap_steps + 1 : 0;
     c->extrap_shifted = false;
     if (st) st->warm_start_used = used;
     if (logging && (rc == SWC_OK || rc == SWC_CG_NOT_CONVERGED)) {
-        launch_mlp_targets(c->L.ncells, nv, c->slot_of, c->N.x, c->xprev, c->N.ahat, c->cg, c->tgt_buf, c->stream);
+        launch_mlp_targets(c->L.ncells, nv, c->slot_of, c->N.x, c->xprev, c->N.xm1, c->N.d2p, c->N.ahat, c->cg,
+                           c->tgt_buf, c->stream);
         c->features_valid = true;
     }
     if (rc != SWC_OK && rc != SWC_CG_NOT_CONVERGED && rc != SWC_NAN_DETECTED) return rc;
@@ -474,9 +498,12 @@ void save_prev_flags(swc_ctx * c, bool move) {
     using namespace swc;
     const size_t bn = c->dim == 3 ? BrickGeom<3>::BN : BrickGeom<2>::BN;
     c->extrap_shifted = false;
-    if (move && c->opts.warm_start == SWC_WARM_EXTRAPOLATE && c->N.xm1) {
-        cudaMemcpyAsync(c->N.flag_m2, c->N.flag_prev, size_t(c->L.nbricks) * bn, cudaMemcpyDeviceToDevice, c->stream);
-        cudaMemcpyAsync(c->B.flag_m2, c->B.flag_prev, size_t(c->L.nbricks), cudaMemcpyDeviceToDevice, c->stream);
+    if (move && history_on(c)) {
+        const size_t nn = size_t(c->L.nbricks) * bn, nbk = size_t(c->L.nbricks);
+        cudaMemcpyAsync(c->N.flag_m3, c->N.flag_m2, nn, cudaMemcpyDeviceToDevice, c->stream);
+        cudaMemcpyAsync(c->B.flag_m3, c->B.flag_m2, nbk, cudaMemcpyDeviceToDevice, c->stream);
+        cudaMemcpyAsync(c->N.flag_m2, c->N.flag_prev, nn, cudaMemcpyDeviceToDevice, c->stream);
+        cudaMemcpyAsync(c->B.flag_m2, c->B.flag_prev, nbk, cudaMemcpyDeviceToDevice, c->stream);
         c->extrap_shifted = true;
     }
     cudaMemcpyAsync(c->N.flag_prev, c->N.flag, size_t(c->L.nbricks) * bn, cudaMemcpyDeviceToDevice, c->stream);
@@ -742,8 +769,12 @@ void swc_destroy(swc_ctx * c) {
     dfree(c->N.flag);
     dfree(c->N.flag_prev);
     dfree(c->N.flag_m2);
+    dfree(c->N.flag_m3);
     dfree(c->N.xm1);
+    dfree(c->N.xm2);
+    dfree(c->N.d2p);
     dfree(c->B.flag_m2);
+    dfree(c->B.flag_m3);
     dfree(c->N.V);
     dfree(c->N.D);
     dfree(c->N.rho);
@@ -755,7 +786,6 @@ void swc_destroy(swc_ctx * c) {
     dfree(c->N.u);
     dfree(c->N.vbar);
     dfree(c->N.nreal);
-    dfree(c->N.nvirt);
     dfree(c->mlp_params);
     dfree(c->mlp_norm);
     dfree(c->mlp_err);
@@ -1077,9 +1107,9 @@ int swc_set_pressure(swc_ctx * c, const double * p, int64_t n) {
 
 int swc_set_mlp(swc_ctx * c, const float * params, const float * norm) {
     if (!valid_ctx(c) || !params || !norm) return SWC_BAD_ARG;
-    for (int k = 6; k < 12; k++)
+    for (int k = SWC_MLP_IN; k < 2 * SWC_MLP_IN; k++)
         if (!(norm[k] > 0)) return SWC_BAD_ARG;
-    if (!(norm[13] > 0)) return SWC_BAD_ARG;
+    if (!(norm[2 * SWC_MLP_IN + 1] > 0)) return SWC_BAD_ARG;
     int rc;
     CK(cudaStreamSynchronize(c->stream));
     if ((rc = ensure_learn_buffers(c))) return rc;
@@ -1101,7 +1131,7 @@ int swc_get_features(swc_ctx * c, float * features, float * targets, int64_t cap
     if (nv < 0) return SWC_CUDA_ERROR;
     *n = nv;
     if (capacity < nv) return SWC_BAD_ARG;
-    if (nv > 0 && features) CK(cudaMemcpy(features, c->feat_buf, sizeof(float) * 6 * nv, cudaMemcpyDeviceToHost));
+    if (nv > 0 && features) CK(cudaMemcpy(features, c->feat_buf, sizeof(float) * SWC_MLP_IN * nv, cudaMemcpyDeviceToHost));
     if (nv > 0 && targets) CK(cudaMemcpy(targets, c->tgt_buf, sizeof(float) * nv, cudaMemcpyDeviceToHost));
     return SWC_OK;
 }
@@ -1224,7 +1254,7 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
         if (which == 7) {
             launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->slot_of, c->B.seg_off + c->B.nseg,
                                      (long long) slots, c->cg, float(1.0 / c->alpha0), float(1.0 / c->rho0), 1.f / 32.f,
-                                     c->dim == 3 ? 1.f / 251.f : 1.f / 45.f, nullptr, c->mlp_err, c->stream);
+                                     nullptr, c->mlp_err, c->stream);
             return;
         }
         if (c->dim == 3) {

@@ -37,15 +37,19 @@ struct NodeArrays {
     float *         u         = nullptr;  // V * d, the halo source of the SpMV
     float4 *        vbar      = nullptr;  // optional: virtual velocity (debug / export)
     unsigned short * nreal    = nullptr;  // optional: real neighbours within h
-    unsigned short * nvirt    = nullptr;  // optional: active virtual neighbours within H (self included)
-    float *         xm1       = nullptr;  // extrapolated warm start: pressure of the step before the previous
-    unsigned char * flag_m2   = nullptr;  // extrapolated warm start: active two steps back
+    // pressure history of the extrapolated / learned warm starts (see k_warm_start)
+    float *         xm1       = nullptr;  // p one step back (0 where inactive then)
+    float *         xm2       = nullptr;  // p two steps back
+    float *         d2p       = nullptr;  // optional: second difference p1 - 2 p2 + p3 (learned features)
+    unsigned char * flag_m2   = nullptr;  // active two steps back
+    unsigned char * flag_m3   = nullptr;  // active three steps back
 };
 
 struct BrickArrays {
     unsigned char * flag      = nullptr;  // active this step
     unsigned char * flag_prev = nullptr;
-    unsigned char * flag_m2   = nullptr;  // active two steps back (extrapolated warm start)
+    unsigned char * flag_m2   = nullptr;  // active two / three steps back (pressure history)
+    unsigned char * flag_m3   = nullptr;
     int *           list      = nullptr;  // active brick ids, ascending
     int *           count     = nullptr;  // device: number of active bricks
     int *           seg       = nullptr;  // per (row, brick column) active-node counts
@@ -123,16 +127,16 @@ void launch_segments(const Lattice & L, const BrickArrays & B, const NodeArrays 
                      cudaStream_t st);
 template<int DIM>
 void launch_ahat(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
-                 unsigned short * nvirt, int sgrid, cudaStream_t st);
+                 int sgrid, cudaStream_t st);
 template<int DIM>
 void launch_diag_max_f64(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const StencilD & S,
                          unsigned long long * out_bits, int grid, cudaStream_t st);
 // warm-start modes
 enum { kWarmPrefix = 0, kWarmNode = 1, kWarmZero = 2, kWarmGiven = 3, kWarmExtrap = 4 };
-// history (kWarmExtrap): N.xm1 / N.flag_m2 / B.flag_m2 hold the step before the previous one
+// history (kWarmExtrap): steps of valid pressure history before this one (0, 1 or 2)
 template<int DIM>
 void launch_warm_start(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int mode, const float * pcomp,
-                       const int * nv_prev, const float * given, int grid, cudaStream_t st, bool history = false);
+                       const int * nv_prev, const float * given, int grid, cudaStream_t st, int history = 0);
 template<int DIM>
 void launch_compact_export(const Lattice & L, const BrickArrays & B, const NodeArrays & N, float * pcomp,
                            long long * node_id, double * rho, double * vol, double * vbar, double * div,
@@ -172,11 +176,10 @@ void launch_mlp_forward_array(long long n, const float * params, const float * n
                               float * z1s, float * h1s, float * z2s, int * err, cudaStream_t st);
 void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const int * slot_of,
                               const int * nv, long long rows_max, const CgState * cg, float inv_alpha0,
-                              float inv_rho0, float inv_nreal, float inv_nvirt, float * feat_out, int * err,
-                              cudaStream_t st);
+                              float inv_rho0, float inv_nreal, float * feat_out, int * err, cudaStream_t st);
 void launch_node_features(const NodeArrays & N, const int * slot_of, const int * nv, long long rows_max,
-                          const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal, float inv_nvirt,
-                          float * feat_out, cudaStream_t st);
+                          const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal, float * feat_out,
+                          cudaStream_t st);
 void launch_mlp_backward(long long n, const float * params, const float * norm, const float * feat,
                          const float * pred, const float * target, const float * z1s, const float * h1s,
                          const float * z2s, float * dz1, float * dz2, float * dy, float * sq_err, float * grad,
@@ -187,7 +190,8 @@ template<int DIM>
 void launch_slot_of(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int * slot_of, int grid,
                     cudaStream_t st);
 void launch_mlp_targets(long long rows_max, const int * nv, const int * slot_of, const float * x, const float * prev,
-                        const float * ahat, const CgState * cg, float * target, cudaStream_t st);
+                        const float * xm1, const float * d2p, const float * ahat, const CgState * cg, float * target,
+                        cudaStream_t st);
 void launch_gather_rows(const float * src, const float * src_t, const int * idx, long long n, float * dst,
                         float * dst_t, cudaStream_t st);
 

@@ -15,7 +15,7 @@
 using namespace swc;
 
 namespace {
-constexpr int kP = SWC_MLP_PARAMS, kN = SWC_MLP_NORM, kH = 64;
+constexpr int kP = SWC_MLP_PARAMS, kN = SWC_MLP_NORM, kH = 64, kIn = SWC_MLP_IN;
 }
 
 struct swc_trainer {
@@ -65,9 +65,9 @@ int swc_trainer_create(int64_t capacity, int32_t batch, swc_trainer ** out) {
     t->batch = batch;
     const size_t B = size_t(batch);
     bool ok = cudaStreamCreateWithFlags(&t->st, cudaStreamNonBlocking) == cudaSuccess;
-    ok = ok && talloc(&t->feat, size_t(capacity) * 6) && talloc(&t->tgt, size_t(capacity)) && talloc(&t->params, kP) &&
+    ok = ok && talloc(&t->feat, size_t(capacity) * kIn) && talloc(&t->tgt, size_t(capacity)) && talloc(&t->params, kP) &&
          talloc(&t->norm, kN) && talloc(&t->m, kP) && talloc(&t->v, kP) && talloc(&t->grad, kP) &&
-         talloc(&t->bfeat, B * 6) && talloc(&t->btgt, B) && talloc(&t->pred, B) && talloc(&t->z1, B * kH) &&
+         talloc(&t->bfeat, B * kIn) && talloc(&t->btgt, B) && talloc(&t->pred, B) && talloc(&t->z1, B * kH) &&
          talloc(&t->h1, B * kH) && talloc(&t->z2, B * kH) && talloc(&t->dz1, B * kH) && talloc(&t->dz2, B * kH) &&
          talloc(&t->dy, B) && talloc(&t->sq, B) && talloc(&t->idx, size_t(capacity)) && talloc(&t->err, 1);
     if (!ok) {
@@ -97,7 +97,7 @@ void swc_trainer_destroy(swc_trainer * t) {
 int swc_trainer_add(swc_trainer * t, const float * f, const float * y, int64_t n) {
     if (!t || n < 0 || (n > 0 && (!f || !y))) return SWC_BAD_ARG;
     if (t->n + n > t->cap) return SWC_BAD_ARG;
-    if (cudaMemcpyAsync(t->feat + t->n * 6, f, sizeof(float) * 6 * n, cudaMemcpyHostToDevice, t->st) != cudaSuccess ||
+    if (cudaMemcpyAsync(t->feat + t->n * kIn, f, sizeof(float) * kIn * n, cudaMemcpyHostToDevice, t->st) != cudaSuccess ||
         cudaMemcpyAsync(t->tgt + t->n, y, sizeof(float) * n, cudaMemcpyHostToDevice, t->st) != cudaSuccess)
         return SWC_CUDA_ERROR;
     cudaStreamSynchronize(t->st);
@@ -155,14 +155,14 @@ int swc_trainer_fit(swc_trainer * t, int32_t epochs, float lr, uint64_t seed, fl
             pred_h.resize(t->n);
             for (long long b0 = 0; b0 < t->n; b0 += t->batch) {
                 const long long nb = std::min<long long>(t->batch, t->n - b0);
-                int rc = forward_batch(t, t->feat + b0 * 6, nb, t->pred, false);
+                int rc = forward_batch(t, t->feat + b0 * kIn, nb, t->pred, false);
                 if (rc) return rc;
                 cudaMemcpyAsync(pred_h.data() + b0, t->pred, sizeof(float) * nb, cudaMemcpyDeviceToHost, t->st);
             }
             if (int rc = check_err(t)) return rc;
             double s = 0;
             for (long long i = 0; i < t->n; i++) {
-                const double d = (double(pred_h[i]) - tgt_h[i]) / norm_h[13];
+                const double d = (double(pred_h[i]) - tgt_h[i]) / norm_h[2 * kIn + 1];
                 s += d * d;
             }
             epoch_loss[e] = float(s / double(t->n));
@@ -181,11 +181,11 @@ int swc_mlp_forward(const float * params, const float * norm, const float * f, i
         swc_trainer_destroy(t);
         return rc;
     }
-    cudaMemcpy(t->feat, f, sizeof(float) * 6 * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(t->feat, f, sizeof(float) * kIn * n, cudaMemcpyHostToDevice);
     std::vector<float> tmp;
     for (long long b0 = 0; b0 < n && !rc; b0 += t->batch) {
         const long long nb = std::min<long long>(t->batch, n - b0);
-        rc = forward_batch(t, t->feat + b0 * 6, nb, t->pred, false);
+        rc = forward_batch(t, t->feat + b0 * kIn, nb, t->pred, false);
         cudaMemcpyAsync(out + b0, t->pred, sizeof(float) * nb, cudaMemcpyDeviceToHost, t->st);
     }
     if (!rc) rc = check_err(t);
@@ -203,7 +203,7 @@ int swc_mlp_gradient(const float * params, const float * norm, const float * f, 
         swc_trainer_destroy(t);
         return rc;
     }
-    cudaMemcpy(t->bfeat, f, sizeof(float) * 6 * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(t->bfeat, f, sizeof(float) * kIn * n, cudaMemcpyHostToDevice);
     cudaMemcpy(t->btgt, y, sizeof(float) * n, cudaMemcpyHostToDevice);
     rc = forward_batch(t, t->bfeat, n, t->pred, true);
     if (!rc) {

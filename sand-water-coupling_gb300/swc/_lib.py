@@ -20,6 +20,12 @@ SWC_NOT_INITIALIZED = 5
 SWC_OUT_OF_MEMORY = 6
 
 WARM_PREFIX, WARM_NODE, WARM_ZERO, WARM_LEARNED, WARM_EXTRAPOLATE = 0, 1, 2, 3, 4
+
+# learned warm-start network sizes (SWC_MLP_IN / SWC_MLP_PARAMS / SWC_MLP_NORM)
+MLP_IN = 8
+MLP_SCALE_EPS = 1e-4
+MLP_PARAMS = 64 * MLP_IN + 64 + 64 * 64 + 64 + 64 + 1
+MLP_NORM = 2 * MLP_IN + 2
 WARM_NAMES = {"prefix": WARM_PREFIX, "node": WARM_NODE, "zero": WARM_ZERO, "learned": WARM_LEARNED,
               "extrapolate": WARM_EXTRAPOLATE}
 

@@ -1,12 +1,12 @@
 """Learned CG warm start: training-data collection and device-side training.
 
-The network (6 -> 64 -> 64 -> 1, SiLU) predicts, per active virtual particle,
-the change of its pressure from the previous step in units of sD / alpha_hat_I
-(see include/swc.h for the feature definitions).  Training data are logged by
-the plain solver (warm start from the node-mapped previous pressure, CG to the
-configured tolerance); training runs on the GPU through swc_trainer_* (tensor-
-core forward, FP32 backward, Adam).  A trained model is a pair (params[4673],
-norm[14]) stored in an .npz file.
+The network (8 -> 64 -> 64 -> 1, SiLU) predicts, per active virtual particle, a
+correction of the pressure extrapolated in time from the node's previous
+pressures, in units of sD / alpha_hat_I (see include/swc.h for the feature
+definitions).  Training data are logged by the plain solver started from that
+extrapolated pressure (CG to the configured tolerance); training runs on the GPU
+through swc_trainer_* (tensor-core forward, FP32 backward, Adam).  A trained
+model is a pair (params[N_PARAMS], norm[N_NORM]) stored in an .npz file.
 """
 from __future__ import annotations
 
@@ -17,8 +17,9 @@ import numpy as np
 from . import _lib
 from .liquid import DualParticleSphLiquid
 
-N_PARAMS = 4673
-N_NORM = 14
+N_IN = _lib.MLP_IN
+N_PARAMS = _lib.MLP_PARAMS
+N_NORM = _lib.MLP_NORM
 
 
 def _fp(a):
@@ -28,7 +29,7 @@ def _fp(a):
 def init_params(seed: int = 0) -> np.ndarray:
     """He-style initialisation (small output layer)."""
     rng = np.random.default_rng(seed)
-    W1 = rng.normal(0, np.sqrt(2.0 / 6), size=(64, 6))
+    W1 = rng.normal(0, np.sqrt(2.0 / N_IN), size=(64, N_IN))
     W2 = rng.normal(0, np.sqrt(2.0 / 64), size=(64, 64))
     w3 = rng.normal(0, np.sqrt(1.0 / 64), size=64) * 0.1
     p = np.concatenate([W1.ravel(), np.zeros(64), W2.ravel(), np.zeros(64), w3, [0.0]])
@@ -45,13 +46,21 @@ def normalisation(features: np.ndarray, targets: np.ndarray) -> np.ndarray:
     return np.concatenate([fm, fs, [t.mean(), ts]]).astype(np.float32)
 
 
+# rows kept for training: a pressure history of at least two steps (history scale
+# s above ten times its floor, feature f5 = ln s) and a target within +-TARGET_CLIP
+MIN_LOG_SCALE = float(np.log(10 * _lib.MLP_SCALE_EPS))
+TARGET_CLIP = 50.0
+
+
 def collect(scene, steps: int, every: int = 1, keep_fraction: float = 1.0, seed: int = 0, tolerance=None):
     """Run the plain solver on `scene` and log (features, targets) of the projections.
 
-    The solver starts CG from the node-mapped previous pressure (the reference
-    of the learned correction).  `keep_fraction` subsamples nodes per step."""
+    The solver starts CG from the pressure extrapolated in time (the base of the
+    learned correction).  Rows without history (where the network's correction
+    vanishes with the scale s) and outlying targets are dropped;
+    `keep_fraction` subsamples the remaining nodes per step."""
     rng = np.random.default_rng(seed)
-    liq = DualParticleSphLiquid(scene, warm_start="node", keep_features=True, tolerance=tolerance)
+    liq = DualParticleSphLiquid(scene, warm_start="extrapolate", keep_features=True, tolerance=tolerance)
     liq.initialize()
     fs, ts = [], []
     for k in range(steps):
@@ -59,6 +68,8 @@ def collect(scene, steps: int, every: int = 1, keep_fraction: float = 1.0, seed:
         if k % every:
             continue
         f, t = liq.features()
+        m = (f[:, 5] > MIN_LOG_SCALE) & (np.abs(t) < TARGET_CLIP)
+        f, t = f[m], t[m]
         if keep_fraction < 1.0 and f.shape[0] > 0:
             m = rng.random(f.shape[0]) < keep_fraction
             f, t = f[m], t[m]
@@ -164,4 +175,8 @@ def save(path, params, norm, **meta):
 
 def load_model(path):
     d = np.load(path)
-    return d["params"], d["norm"]
+    p, q = d["params"], d["norm"]
+    if p.size != N_PARAMS or q.size != N_NORM:
+        raise ValueError(f"{path}: network of {p.size} parameters / {q.size} normalisation values; "
+                         f"expected {N_PARAMS} / {N_NORM}")
+    return p, q

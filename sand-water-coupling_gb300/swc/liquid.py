@@ -253,15 +253,18 @@ class DualParticleSphLiquid:
 
     def setMlp(self, params, norm):
         """Network of the learned warm start (see swc.learn)."""
-        p = np.ascontiguousarray(params, dtype=np.float32)
-        q = np.ascontiguousarray(norm, dtype=np.float32)
+        p = np.ascontiguousarray(params, dtype=np.float32).ravel()
+        q = np.ascontiguousarray(norm, dtype=np.float32).ravel()
+        if p.size != _lib.MLP_PARAMS or q.size != _lib.MLP_NORM:
+            raise ValueError(f"network of {p.size} parameters / {q.size} normalisation values; "
+                             f"expected {_lib.MLP_PARAMS} / {_lib.MLP_NORM}")
         fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
         self._check(self.L.swc_set_mlp(self.h, fp(p), fp(q)), "swc_set_mlp")
 
     def features(self):
-        """(features[n, 6], targets[n]) logged by the last projection (keep_features=True)."""
+        """(features[n, MLP_IN], targets[n]) logged by the last projection (keep_features=True)."""
         n = self.numVirtual()
-        f = np.empty((max(n, 1), 6), dtype=np.float32)
+        f = np.empty((max(n, 1), _lib.MLP_IN), dtype=np.float32)
         t = np.empty(max(n, 1), dtype=np.float32)
         got = C.c_int64()
         fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))

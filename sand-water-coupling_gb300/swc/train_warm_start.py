@@ -3,13 +3,13 @@
 Training data: 3D dam-break variants (block height along x drawn from
 U(0.64, 1.28), square cross-section sized to ~`--particles` particles) and,
 with `--block-seeds`, random-velocity projection blocks of `--block-n`^3
-particles, each run by the plain solver (CG from the node-mapped previous
-pressure to the scene tolerance) with feature logging; a random `--keep`
-fraction of the active nodes of every step is kept.  Training: Adam, learning
-rate 1e-3, `--epochs` epochs, on the GPU (swc_trainer_*).  Evaluation: the
-128^3 projection block with a held-out seed (1234), CG iterations per step from
-the node-mapped, learned (with and without the residual fallback) and zero
-starts.
+particles, each run by the plain solver (CG from the pressure extrapolated in
+time to the scene tolerance) with feature logging; a random `--keep` fraction
+of the active nodes of every step is kept.  Training: Adam, learning rate 1e-3,
+`--epochs` epochs, on the GPU (swc_trainer_*).  Evaluation: the 128^3
+projection block with a held-out seed (1234), CG iterations per step from the
+node-mapped, extrapolated, learned (with and without the residual fallback)
+and zero starts.
 
     python -m swc.train_warm_start --out swc/models/warm_start.npz
 """
@@ -59,8 +59,9 @@ def evaluate(params, norm, n=128, seed=1234, steps=20):
     """Mean CG iterations per step on the n^3 block (first step excluded: no previous p)."""
     sc = scenes.projection_block_3d(n=n, seed=seed)
     out = {}
-    for key, mode, no_fallback in (("node", "node", False), ("learned", "learned", False),
-                                   ("learned_no_fallback", "learned", True), ("zero", "zero", False)):
+    for key, mode, no_fallback in (("node", "node", False), ("extrapolate", "extrapolate", False),
+                                   ("learned", "learned", False), ("learned_no_fallback", "learned", True),
+                                   ("zero", "zero", False)):
         liq = DualParticleSphLiquid(sc, warm_start=mode, tolerance=sc.tolerance, learned_no_fallback=no_fallback)
         if mode == "learned":
             liq.setMlp(params, norm)

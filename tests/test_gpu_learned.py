@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 
 def _synthetic(n=5000, seed=0):
     rng = np.random.default_rng(seed)
-    f = rng.normal(size=(n, 6)).astype(np.float32)
+    f = rng.normal(size=(n, M.N_IN)).astype(np.float32)
     t = (np.tanh(f[:, 0]) + 0.5 * f[:, 4] - 0.2 * f[:, 1] * f[:, 5]).astype(np.float32)
     norm = np.concatenate([f.mean(0), f.std(0), [t.mean(), t.std()]]).astype(np.float32)
     return f, t, norm
@@ -62,14 +62,14 @@ def test_learned_warm_start_end_to_end(swc_mod):
 
     train_scene = scenes.projection_block_3d(n=24, seed=11, steps=12)
     f, t = learn.collect(train_scene, steps=12)
-    assert f.shape[1] == 6 and f.shape[0] == t.shape[0] > 1000
+    assert f.shape[1] == learn.N_IN and f.shape[0] == t.shape[0] > 1000
     assert np.all(np.isfinite(f)) and np.all(np.isfinite(t))
     p, q, loss = learn.train(f, t, epochs=20, lr=1e-3, batch=4096, seed=0)
     assert loss[-1] <= loss[0]
 
     test_scene = scenes.projection_block_3d(n=24, seed=99).rounded_to_float32()
     out = {}
-    for mode in ("node", "learned"):
+    for mode in ("node", "extrapolate", "learned"):
         liq = swc_mod.DualParticleSphLiquid(test_scene, warm_start=mode, compute_true_residual=True)
         if mode == "learned":
             liq.setMlp(p, q)
@@ -83,11 +83,62 @@ def test_learned_warm_start_end_to_end(swc_mod):
         out[mode] = (liq.getParticles()[1], np.array(its), used)
         liq.close()
     v_node, it_node, _ = out["node"]
+    v_ex, it_ex, _ = out["extrapolate"]
     v_learn, it_learn, used = out["learned"]
     assert np.linalg.norm(v_learn - v_node) / np.linalg.norm(v_node) < 1e-4
-    # the residual-based fallback never starts from a worse residual than the plain solver
-    assert it_learn[1:].mean() <= it_node[1:].mean() + 1.0
-    print(f"\nCG iterations  node-mapped: {it_node.tolist()}  learned: {it_learn.tolist()}  used: {used}")
+    # the residual-based fallback never starts from a worse residual than its base start
+    assert it_learn[1:].mean() <= it_ex[1:].mean() + 1.0
+    assert used[0] == 1 and all(u in (3, 4) for u in used[1:])  # NODE (no history), then LEARNED / EXTRAPOLATE
+    print(f"\nCG iterations  node-mapped: {it_node.tolist()}  extrapolated: {it_ex.tolist()}  "
+          f"learned: {it_learn.tolist()}  used: {used}")
+
+
+def test_history_features_match_pressure_history(swc_mod):
+    """The logged features and targets follow their definitions (include/swc.h)
+    when recomputed on the host from the pressures of the previous projections,
+    matched by lattice node id: the two-level history shift, its activity masks,
+    the extrapolated base and the history scale."""
+    from swc import _lib
+
+    sc = scenes.projection_block_3d(n=16, seed=5).rounded_to_float32()
+    liq = swc_mod.DualParticleSphLiquid(sc, warm_start="extrapolate", keep_features=True)
+    liq.initialize()
+    hist = []
+    for k in range(6):
+        liq.advance(sc.dt)
+        v = liq.virtual()
+        f, t = liq.features()
+        ids, p, ah, D = v["node"], v["p"], v["alpha_hat"], v["div"]
+        assert f.shape == (ids.shape[0], _lib.MLP_IN)
+        sD = np.sqrt(np.mean(D.astype(np.float64) ** 2))
+        w = ah / sD
+        prev = [dict(zip(h["node"].tolist(), h["p"].tolist())) for h in hist[::-1]]  # one, two, three steps back
+
+        def back(j):
+            return np.array([prev[j].get(i, 0.0) if j < len(prev) else 0.0 for i in ids.tolist()])
+
+        def alive(j):
+            return np.array([j < len(prev) and i in prev[j] for i in ids.tolist()])
+
+        a1 = alive(0)
+        a2 = a1 & alive(1)
+        a3 = a2 & alive(2)
+        p1, p2, p3 = back(0) * a1, back(1) * a2, back(2) * a3
+        base = np.where(a2, 2 * p1 - p2, p1)
+        d1, d2, q = (base - p1) * w, np.where(a3, p1 - 2 * p2 + p3, 0.0) * w, p1 * w
+        s = np.sqrt(d1 * d1 + d2 * d2) + _lib.MLP_SCALE_EPS
+        # FP32 pressures on the device: compare in the units of each quantity
+        tol = 2e-5 * np.abs(p).max() * np.abs(w).max()
+        np.testing.assert_allclose(f[:, 3] * s, d1, atol=tol)
+        np.testing.assert_allclose(f[:, 4] * s, d2, atol=tol)
+        np.testing.assert_allclose(np.exp(f[:, 5]), s, rtol=1e-3, atol=tol)
+        np.testing.assert_allclose(f[:, 6] * (np.abs(q) + s), q, atol=tol)
+        np.testing.assert_allclose(t * s, (p - base) * w, atol=tol)
+        np.testing.assert_allclose(f[:, 0], D / sD, rtol=1e-4, atol=1e-6)
+        if k >= 3:
+            assert a3.sum() > 0.5 * ids.shape[0]
+        hist.append(v)
+    liq.close()
 
 
 def test_committed_model_without_fallback(swc_mod):

@@ -6,7 +6,7 @@ from oracle import mlp_oracle as M
 
 def _data(n=64, seed=0):
     rng = np.random.default_rng(seed)
-    f = rng.normal(size=(n, 6))
+    f = rng.normal(size=(n, M.N_IN))
     t = np.sin(f[:, 0]) + 0.3 * f[:, 4] - 0.1 * f[:, 1] ** 2
     norm = np.concatenate([f.mean(0), f.std(0), [t.mean(), t.std()]])
     return f, t, norm

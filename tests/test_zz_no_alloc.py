@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 
 def _batch(n, seed):
     rng = np.random.default_rng(seed)
-    f = rng.normal(size=(n, 6)).astype(np.float32)
+    f = rng.normal(size=(n, 8)).astype(np.float32)  # SWC_MLP_IN features
     t = (np.tanh(f[:, 0]) + 0.5 * f[:, 4] - 0.2 * f[:, 1] * f[:, 5]).astype(np.float32)
     norm = np.concatenate([f.mean(0), f.std(0), [t.mean(), t.std()]]).astype(np.float32)
     return f, t, norm
