@@ -45,8 +45,9 @@ typedef enum swc_warm_start {
     SWC_WARM_NODE    = 1, /* previous pressure of the same lattice node (0 for new nodes) */
     SWC_WARM_ZERO    = 2,
     SWC_WARM_LEARNED = 3, /* MLP prediction; falls back to NODE when its initial residual is larger */
-    SWC_WARM_EXTRAPOLATE = 4 /* 2 p_{n-1} - p_{n-2} of the same lattice node (NODE where the node or the
-                                history is new; the history spans consecutive swc_advance calls) */
+    SWC_WARM_EXTRAPOLATE = 4 /* the same lattice node's pressure extrapolated in time: 3 p_{n-1} - 3 p_{n-2}
+                                + p_{n-3} with three steps of history, 2 p_{n-1} - p_{n-2} with two, NODE
+                                with less (the history spans consecutive swc_advance calls) */
 } swc_warm_start;
 
 typedef struct swc_ctx swc_ctx;
@@ -177,10 +178,12 @@ int swc_time_kernel(swc_ctx * ctx, int which, int reps, double * mean_ms);
  * forward with FP32 accumulation, predicts a correction of the time-
  * extrapolated pressure of each node.  With p1, p2, p3 the pressures of the
  * same lattice node one, two and three advance steps back (0 where the node
- * was inactive or the history is shorter), the base start is
- *   p_base_I = 2 p1 - p2 where the node has two steps of history, else p1.
+ * was inactive or the history is shorter), the base start is the
+ * SWC_WARM_EXTRAPOLATE start
+ *   p_base_I = p1 + (p1 - p2) + (p1 - 2 p2 + p3)   (quadratic; the differences
+ *              that need more history than the node has are 0).
  * In units w = alpha_hat_I / sD (sD the RMS of D over active nodes):
- *   d1 = (p_base - p1) w,  d2 = (p1 - 2 p2 + p3) w (0 without three steps),
+ *   d1 = (p1 - p2) w (0 without two steps),  d2 = (p1 - 2 p2 + p3) w (0 without three),
  *   q = p1 w,  s = sqrt(d1^2 + d2^2) + SWC_MLP_SCALE_EPS (the node's history scale).
  * Features of active node I (raw, before the normalisation carried with the
  * network):

@@ -150,7 +150,7 @@ __device__ __forceinline__ void node_raw(const NodeArrays & N, long long s, floa
 }
 __device__ __forceinline__ float node_features(const float (&g)[kMlpIn], const FeatScale & F, float (&f)[kMlpIn]) {
     const float w  = g[1] * F.inv_sD;
-    const float d1 = (g[3] - g[4]) * w, d2 = g[5] * w, q = g[4] * w;
+    const float d1 = ((g[3] - g[4]) - g[5]) * w, d2 = g[5] * w, q = g[4] * w;  // p_base = p1 + d1 + d2
     const float sc = sqrtf(fmaf(d1, d1, d2 * d2)) + kMlpScaleEps;
     const float is = 1.f / sc;
     f[0] = g[0] * F.inv_sD;
@@ -183,8 +183,9 @@ __device__ __forceinline__ float tanh_fast(float h) {
 // params: FP32 vector (layout above); norm: f_mean[kMlpIn], f_std[kMlpIn], t_mean, t_std.
 // kMlpFromArray: rows of feat[n][kMlpIn] -> out[n] (prediction t); with SAVE,
 //   the pre-activations z1, z2 and h1 (bf16-rounded) for training.
-// kMlpFromNodes: rows = active nodes (slot_of[I]); writes the warm start
-//   x[s] = p_base + t * sD / alpha_hat into N.x (and feat_out when non-null).
+// kMlpFromNodes: rows = the slots of the active bricks in brick order (slot
+//   blist[r / BN] * BN + r % BN, contiguous within a brick); writes the warm
+//   start x[s] = p_base + t s sD / alpha_hat into N.x at active nodes.
 //
 // Arithmetic: W1, b1, W2, b2 are scaled by 1/2 when staged (exact in bf16 and
 // FP32), so the accumulators hold h = z/2 and silu(z) = h + h tanh(h) is one
@@ -195,9 +196,9 @@ template<int MODE, bool SAVE>
 __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
     k_mlp_forward(long long n, const float * __restrict__ params, const float * __restrict__ norm,
                   const float * __restrict__ feat, float * __restrict__ out, float * __restrict__ z1s,
-                  float * __restrict__ h1s, float * __restrict__ z2s, NodeArrays N, const int * __restrict__ slot_of,
-                  const int * __restrict__ nv, const CgState * __restrict__ cg, FeatScale F0,
-                  float * __restrict__ feat_out, int * __restrict__ err) {
+                  float * __restrict__ h1s, float * __restrict__ z2s, NodeArrays N, const int * __restrict__ blist,
+                  const int * __restrict__ bcount, int bn_log2, const int * __restrict__ nv,
+                  const CgState * __restrict__ cg, FeatScale F0, int * __restrict__ err) {
     __shared__ __align__(1024) uint8_t sw1[kMlpH * 16 * 2];   // W1/2 [64 x 16] bf16 (K padded to 16)
     __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpH * 2];  // W2/2 [64 x 64]
     __shared__ __align__(1024) uint8_t sh[kMlpNT * kMlpH * 2];  // H1 [128 x 64]; X [128 x 16] in its first 4 KB
@@ -261,44 +262,46 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
     long long rows = n;
     FeatScale F = F0;
     if (MODE == kMlpFromNodes) {
-        rows = *nv;
+        rows = (long long) *bcount << bn_log2;
         // sD = RMS of the right-hand side over active nodes
-        const double sD = rows > 0 ? sqrt(cg->bb / double(rows)) : 1.0;
+        const int na    = *nv;
+        const double sD = na > 0 ? sqrt(cg->bb / double(na)) : 1.0;
         F.inv_sD        = sD > 0 ? float(1.0 / sD) : 0.f;
     }
     uint32_t phase = 0;
     const long long ntiles = (rows + kMlpNT - 1) / kMlpNT;
     // Inputs of a tile row, gathered one tile ahead: the features in array
-    // mode; the raw node values of node_raw at slot_of[r] in node mode.
-    auto gather = [&](long long r, float (&g)[kMlpIn], long long & gs) {
+    // mode; the raw node values of node_raw at the row's slot in node mode
+    // (`ga`: the node is active).
+    auto gather = [&](long long r, float (&g)[kMlpIn], long long & gs, bool & ga) {
 #pragma unroll
         for (int k = 0; k < kMlpIn; k++) g[k] = 0.f;
         gs = 0;
+        ga = false;
         if (r >= rows) return;
         if (MODE == kMlpFromArray) {
 #pragma unroll
             for (int k = 0; k < kMlpIn; k++) g[k] = feat[r * kMlpIn + k];
+            ga = true;
         } else {
-            gs = slot_of[r];
+            gs = ((long long) blist[r >> bn_log2] << bn_log2) | (r & ((1 << bn_log2) - 1));
+            ga = N.flag[gs] != 0;
             node_raw(N, gs, g);
         }
     };
     float gn[kMlpIn];
     long long sn = 0;
-    gather(blockIdx.x * (long long) kMlpNT + tid, gn, sn);
+    bool an      = false;
+    gather(blockIdx.x * (long long) kMlpNT + tid, gn, sn, an);
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const long long row = tile * kMlpNT + tid;
-        const bool valid    = row < rows;
+        const bool valid    = an;
         const long long s   = sn;
         const float ah = gn[1], base = gn[3];
         float f[kMlpIn];
         float sc = 1.f;
         if (MODE == kMlpFromNodes) {
             sc = node_features(gn, F, f);
-            if (valid && feat_out) {
-#pragma unroll
-                for (int k = 0; k < kMlpIn; k++) feat_out[row * kMlpIn + k] = f[k];
-            }
         } else {
 #pragma unroll
             for (int k = 0; k < kMlpIn; k++) f[k] = gn[k];
@@ -319,7 +322,7 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
             mma_commit(&mbar);
         }
         // the next tile's gathers are in flight while this tile's MMAs run
-        gather((tile + gridDim.x) * kMlpNT + tid, gn, sn);
+        gather((tile + gridDim.x) * kMlpNT + tid, gn, sn, an);
         if (!mbar_wait(&mbar, phase)) s_fail = 1;
         phase ^= 1u;
         tc_fence_after();
@@ -533,7 +536,8 @@ __global__ void k_mlp_targets(const int * __restrict__ nv, const int * __restric
     for (long long r = blockIdx.x * (long long) blockDim.x + threadIdx.x; r < rows; r += (long long) gridDim.x * blockDim.x) {
         const long long s = slot_of[r];
         const float w     = ahat[s] * inv;
-        const float d1 = (prev[s] - xm1[s]) * w, d2 = (d2p ? d2p[s] : 0.f) * w;
+        const float dd = d2p ? d2p[s] : 0.f;
+        const float d1 = ((prev[s] - xm1[s]) - dd) * w, d2 = dd * w;
         const float sc    = sqrtf(fmaf(d1, d1, d2 * d2)) + kMlpScaleEps;
         target[r]         = (x[s] - prev[s]) * w / sc;
     }
@@ -639,30 +643,30 @@ static int num_sms_cached() {
 template<int MODE, bool SAVE>
 static void launch_forward(long long rows_max, const float * params, const float * norm, const float * feat,
                            float * out, float * z1s, float * h1s, float * z2s, const NodeArrays & N,
-                           const int * slot_of, const int * nv, const CgState * cg, const FeatScale & F,
-                           float * feat_out, int * err, cudaStream_t st) {
+                           const int * blist, const int * bcount, int bn_log2, const int * nv, const CgState * cg,
+                           const FeatScale & F, int * err, cudaStream_t st) {
     const MlpLaunch s     = mlp_launch_shape<MODE, SAVE>();
     const long long tiles = std::max<long long>(1, (rows_max + kMlpNT - 1) / kMlpNT);
     const int grid        = int(std::min<long long>(tiles, (long long) s.per_sm * num_sms_cached()));
     k_mlp_forward<MODE, SAVE><<<grid, kMlpNT, s.dyn, st>>>(rows_max, params, norm, feat, out, z1s, h1s, z2s, N,
-                                                           slot_of, nv, cg, F, feat_out, err);
+                                                           blist, bcount, bn_log2, nv, cg, F, err);
 }
 void launch_mlp_forward_array(long long n, const float * params, const float * norm, const float * feat, float * out,
                               float * z1s, float * h1s, float * z2s, int * err, cudaStream_t st) {
     if (n <= 0) return;
     if (z1s || h1s || z2s)
         launch_forward<kMlpFromArray, true>(n, params, norm, feat, out, z1s, h1s, z2s, NodeArrays{}, nullptr, nullptr,
-                                            nullptr, FeatScale{}, nullptr, err, st);
+                                            0, nullptr, nullptr, FeatScale{}, err, st);
     else
         launch_forward<kMlpFromArray, false>(n, params, norm, feat, out, nullptr, nullptr, nullptr, NodeArrays{},
-                                             nullptr, nullptr, nullptr, FeatScale{}, nullptr, err, st);
+                                             nullptr, nullptr, 0, nullptr, nullptr, FeatScale{}, err, st);
 }
-void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const int * slot_of,
-                              const int * nv, long long rows_max, const CgState * cg, float inv_alpha0,
-                              float inv_rho0, float inv_nreal, float * feat_out, int * err, cudaStream_t st) {
+void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const BrickArrays & B,
+                              int bn_log2, long long slots_max, const CgState * cg, float inv_alpha0, float inv_rho0,
+                              float inv_nreal, int * err, cudaStream_t st) {
     FeatScale F{0.f, inv_alpha0, inv_rho0, inv_nreal};
-    launch_forward<kMlpFromNodes, false>(rows_max, params, norm, nullptr, nullptr, nullptr, nullptr, nullptr, N,
-                                         slot_of, nv, cg, F, feat_out, err, st);
+    launch_forward<kMlpFromNodes, false>(slots_max, params, norm, nullptr, nullptr, nullptr, nullptr, nullptr, N, B.list,
+                                         B.count, bn_log2, B.seg_off + B.nseg, cg, F, err, st);
 }
 void launch_mlp_backward(long long n, const float * params, const float * norm, const float * feat,
                          const float * pred, const float * target, const float * z1s, const float * h1s,

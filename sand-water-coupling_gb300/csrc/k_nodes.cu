@@ -308,13 +308,13 @@ __global__ void __launch_bounds__(kNT) k_diag_max_f64(Lattice L, const int * __r
 //   node:   previous pressure of the same node, 0 if it was inactive
 //   zero:   0
 //   given:  caller-supplied values in brick layout
-//   extrap: linear extrapolation in time of the same node's pressure.  With
-//           p1, p2, p3 the node's pressure one, two, three steps back (x,
-//           xm1, xm2 on entry; a value counts where the node was active at
-//           that step and `history` covers it), p0 = 2 p1 - p2 with two steps,
-//           p1 with one, else 0.  The history shifts (xm1 = p1, xm2 = p2, both
-//           0 where inactive) and, when d2p is allocated, d2p = p1 - 2 p2 + p3
-//           (0 without three steps).  Every slot of an active brick is
+//   extrap: extrapolation in time of the same node's pressure.  With p1, p2,
+//           p3 the node's pressure one, two, three steps back (x, xm1, xm2 on
+//           entry; a value counts where the node was active at that step and
+//           `history` covers it), p0 = 3 p1 - 3 p2 + p3 (quadratic) with three
+//           steps, 2 p1 - p2 with two, p1 with one, else 0.  The history shifts
+//           (xm1 = p1, xm2 = p2, both 0 where inactive) and, when d2p is
+//           allocated, d2p = p1 - 2 p2 + p3 (0 without three steps).  Every slot of an active brick is
 //           written; a slot's history is read only when the node was active
 //           at every step it spans, which also means its brick was visited
 //           (and its history shifted) at each of those steps.
@@ -351,8 +351,9 @@ __global__ void __launch_bounds__(kNT) k_warm_start(Lattice L, const int * __res
                 const bool a2  = a1 && history >= 1 && B.flag_m2[b] && N.flag_m2[s];
                 const bool a3  = a2 && history >= 2 && B.flag_m3[b] && N.flag_m3[s];
                 const float p1 = a1 ? N.x[s] : 0.f, p2 = a2 ? N.xm1[s] : 0.f, p3 = a3 ? N.xm2[s] : 0.f;
-                if (N.flag[s]) v = a2 ? fmaf(2.f, p1, -p2) : p1;
-                if (N.d2p) N.d2p[s] = a3 ? (p1 - 2.f * p2) + p3 : 0.f;
+                const float d1 = a2 ? p1 - p2 : 0.f, d2 = a3 ? (p1 - 2.f * p2) + p3 : 0.f;
+                if (N.flag[s]) v = (p1 + d1) + d2;
+                if (N.d2p) N.d2p[s] = d2;
                 N.xm2[s] = p2;
                 N.xm1[s] = p1;
             }

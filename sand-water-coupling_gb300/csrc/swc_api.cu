@@ -5,6 +5,7 @@
 // checks.
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <cstdio>
 #include <cstring>
 #include <numbers>
@@ -89,7 +90,6 @@ struct swc_ctx {
     float * feat_buf   = nullptr;  // logged features (reference order, 6 per node)
     float * tgt_buf    = nullptr;  // logged targets
     bool    features_valid = false;
-    bool    slot_of_valid  = false;  // slot_of / node count are those of the last projection
     // extrapolated warm start: consecutive advance steps whose solution history
     // (N.xm1, flags two steps back) is valid, and whether this step shifted the flags
     int     extrap_steps   = 0;
@@ -337,20 +337,32 @@ template<int DIM> int run_cg(swc_ctx * c, swc_stats * st, bool initialized) {
         if (rc) return rc;
     }
     if (!initialized) {
-        int rc = cg_init_sync<DIM>(c);
-        if (rc) return rc;
+        // initial residual on the device; its state comes back with the first
+        // convergence check (the iteration kernels are no-ops once CG is done)
+        const int * nv = c->B.seg_off + c->B.nseg;
+        launch_cg_init<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->opts.tolerance, c->opts.max_iterations, nv,
+                            c->rgrid, c->stream);
+        c->hcg->st.done     = 0;
+        c->hcg->st.iter     = 0;
+        c->hcg->st.max_iter = c->opts.max_iterations >= 0 ? c->opts.max_iterations : std::numeric_limits<int>::max();
     }
-    const double rr0 = c->hcg->st.rr0, bb = c->hcg->st.bb;
-    int first        = c->opts.check_interval > 0 ? c->opts.check_interval : std::max(4, c->last_iters);
+    int first   = c->opts.check_interval > 0 ? c->opts.check_interval : std::max(4, c->last_iters);
+    bool counts = initialized;
     while (!c->hcg->st.done) {
         const int room = c->hcg->st.max_iter - c->hcg->st.iter;
         int m          = std::min(first, std::max(room, 1));
         for (; m >= 8; m -= 8) CK(cudaGraphLaunch(c->g8, c->stream));
         for (; m > 0; m--) CK(cudaGraphLaunch(c->g1, c->stream));
         CK(cudaMemcpyAsync(&c->hcg->st, c->cg, sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
+        if (!counts) {
+            CK(cudaMemcpyAsync(&c->hcg->nv, c->B.seg_off + c->B.nseg, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaMemcpyAsync(&c->hcg->nbricks, c->B.count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+            counts = true;
+        }
         CK(cudaStreamSynchronize(c->stream));
         first = c->opts.check_interval > 0 ? c->opts.check_interval : 8;
     }
+    const double rr0 = c->hcg->st.rr0, bb = c->hcg->st.bb;
     const CgState & h = c->hcg->st;
     int status        = SWC_OK;
     if (h.done == 4) launch_zero_active<DIM>(c->L, c->B, c->N.x, c->grid, c->stream);  // b = 0 -> x = 0
@@ -388,7 +400,6 @@ bool history_on(const swc_ctx * c) {
 // The shared tail of advance / project: virtual generation, projection, G_i.
 template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     mark(c, 3);
-    c->slot_of_valid = false;
     run_generate<DIM>(c, true);
     mark(c, 4);
     const int mode     = c->opts.warm_start;
@@ -398,9 +409,11 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     const size_t slots = size_t(c->L.nbricks) * BrickGeom<DIM>::BN;
     int used           = mode;
     bool initialized   = false;
+    bool mlp_checked   = false;
     // Pressure history (extrapolated and learned warm starts, logged features):
-    // the base start is 2 p1 - p2 with two steps of history, p1 (node-mapped)
-    // with fewer; the history spans consecutive advance calls.
+    // the base start is 3 p1 - 3 p2 + p3 with three steps of history, 2 p1 - p2
+    // with two, p1 (node-mapped) with fewer; the history spans consecutive
+    // advance calls.
     const bool hist_on  = history_on(c);
     const int history   = (hist_on && c->extrap_shifted) ? std::min(c->extrap_steps, 2) : 0;
     const int base_used = history >= 1 ? SWC_WARM_EXTRAPOLATE : SWC_WARM_NODE;
@@ -409,12 +422,12 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
         // base start (and history shift): the fallback, the network's base and the target reference
         launch_warm_start<DIM>(c->L, c->B, c->N, kWarmExtrap, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream,
                                history);
-        CK(cudaMemcpyAsync(c->xprev, c->N.x, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
-        launch_slot_of<DIM>(c->L, c->B, c->N, c->slot_of, c->grid, c->stream);
-        c->slot_of_valid = true;
+        const bool no_fallback = learned && c->opts.learned_no_fallback && !logging;
+        if (!no_fallback)
+            CK(cudaMemcpyAsync(c->xprev, c->N.x, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
+        if (logging) launch_slot_of<DIM>(c->L, c->B, c->N, c->slot_of, c->grid, c->stream);
         // |b|^2 for sD and (for the fallback test) the initial residual of the
         // base start, read back with the learned start's (one host synchronisation)
-        const bool no_fallback = learned && c->opts.learned_no_fallback && !logging;
         if (no_fallback) launch_rhs_norm<DIM>(c->B, c->N, c->cg, c->partials, c->grid, c->stream);
         else {
             launch_cg_init<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->opts.tolerance, c->opts.max_iterations,
@@ -427,19 +440,26 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
             launch_node_features(c->N, c->slot_of, nv, c->L.ncells, c->cg, inv_a0, inv_r0, inv_nr, c->feat_buf,
                                  c->stream);
         if (learned) {
-            launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->slot_of, nv, (long long) slots, c->cg, inv_a0,
-                                     inv_r0, inv_nr, nullptr, c->mlp_err, c->stream);
+            launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->B, DIM == 3 ? 9 : 8, (long long) slots, c->cg,
+                                     inv_a0, inv_r0, inv_nr, c->mlp_err, c->stream);
             CK(cudaMemcpyAsync(&c->hcg->mlp_err, c->mlp_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-            if ((rc = cg_init_sync<DIM>(c))) return rc;
-            const int err        = c->hcg->mlp_err;
-            const double rr_base = c->hcg->rr_node, rr_mlp = c->hcg->st.rr0;
-            if (err || !(rr_mlp == rr_mlp) || (!c->opts.learned_no_fallback && !(rr_mlp <= rr_base))) {
-                // the prediction starts from a larger residual (or failed): keep the base start
-                CK(cudaMemcpyAsync(c->N.x, c->xprev, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
+            if (no_fallback) {
+                // CG initialises from the prediction without a host round trip; the
+                // tensor-core pass's error flag is read with CG's first check
+                used        = SWC_WARM_LEARNED;
+                mlp_checked = true;
+            } else {
                 if ((rc = cg_init_sync<DIM>(c))) return rc;
-                used = base_used;
-            } else used = SWC_WARM_LEARNED;
-            initialized = true;
+                const int err        = c->hcg->mlp_err;
+                const double rr_base = c->hcg->rr_node, rr_mlp = c->hcg->st.rr0;
+                if (err || !(rr_mlp == rr_mlp) || (!c->opts.learned_no_fallback && !(rr_mlp <= rr_base))) {
+                    // the prediction starts from a larger residual (or failed): keep the base start
+                    CK(cudaMemcpyAsync(c->N.x, c->xprev, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
+                    if ((rc = cg_init_sync<DIM>(c))) return rc;
+                    used = base_used;
+                } else used = SWC_WARM_LEARNED;
+                initialized = true;
+            }
         } else if (mode == SWC_WARM_EXTRAPOLATE || mode == SWC_WARM_LEARNED) {
             if ((rc = cg_init_sync<DIM>(c))) return rc;  // host copy of the base start's state
             initialized = true;
@@ -458,6 +478,10 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     }
     mark(c, 5);
     int rc = run_cg<DIM>(c, st, initialized);
+    if (mlp_checked && c->hcg->mlp_err) {
+        c->err = "learned warm start: the tensor-core pass timed out; CG ran from its output";
+        used   = base_used;
+    }
     c->extrap_steps   = (hist_on && c->extrap_shifted && (rc == SWC_OK || rc == SWC_CG_NOT_CONVERGED)) ? c->extrap_steps + 1 : 0;
     c->extrap_shifted = false;
     if (st) st->warm_start_used = used;
@@ -499,11 +523,11 @@ void save_prev_flags(swc_ctx * c, bool move) {
     const size_t bn = c->dim == 3 ? BrickGeom<3>::BN : BrickGeom<2>::BN;
     c->extrap_shifted = false;
     if (move && history_on(c)) {
-        const size_t nn = size_t(c->L.nbricks) * bn, nbk = size_t(c->L.nbricks);
-        cudaMemcpyAsync(c->N.flag_m3, c->N.flag_m2, nn, cudaMemcpyDeviceToDevice, c->stream);
-        cudaMemcpyAsync(c->B.flag_m3, c->B.flag_m2, nbk, cudaMemcpyDeviceToDevice, c->stream);
-        cudaMemcpyAsync(c->N.flag_m2, c->N.flag_prev, nn, cudaMemcpyDeviceToDevice, c->stream);
-        cudaMemcpyAsync(c->B.flag_m2, c->B.flag_prev, nbk, cudaMemcpyDeviceToDevice, c->stream);
+        // rotate the history buffers (no kernel reads them inside the captured CG graphs)
+        std::swap(c->N.flag_m3, c->N.flag_m2);
+        std::swap(c->N.flag_m2, c->N.flag_prev);
+        std::swap(c->B.flag_m3, c->B.flag_m2);
+        std::swap(c->B.flag_m2, c->B.flag_prev);
         c->extrap_shifted = true;
     }
     cudaMemcpyAsync(c->N.flag_prev, c->N.flag, size_t(c->L.nbricks) * bn, cudaMemcpyDeviceToDevice, c->stream);
@@ -1225,7 +1249,7 @@ int swc_get_phase_times(swc_ctx * c, double * ms, int n) {
 
 int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
     if (!valid_ctx(c) || !mean_ms || reps <= 0 || !c->initialized || which < 0 || which > 7) return SWC_BAD_ARG;
-    if (which == 7 && !(c->mlp_ready && c->slot_of_valid)) return SWC_BAD_ARG;  // needs a learned projection first
+    if (which == 7 && !c->mlp_ready) return SWC_BAD_ARG;  // needs a network (swc_set_mlp)
     CK(cudaStreamSynchronize(c->stream));
     // keep the solver state: run the CG kernels against a scratch copy of the scalars
     CgState saved{};
@@ -1252,9 +1276,9 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
     }
     auto launch = [&]() {
         if (which == 7) {
-            launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->slot_of, c->B.seg_off + c->B.nseg,
-                                     (long long) slots, c->cg, float(1.0 / c->alpha0), float(1.0 / c->rho0), 1.f / 32.f,
-                                     nullptr, c->mlp_err, c->stream);
+            launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->B, c->dim == 3 ? 9 : 8, (long long) slots,
+                                     c->cg, float(1.0 / c->alpha0), float(1.0 / c->rho0), 1.f / 32.f, c->mlp_err,
+                                     c->stream);
             return;
         }
         if (c->dim == 3) {

@@ -174,9 +174,11 @@ void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeAr
 // ---- k_mlp.cu (learned warm start) ----
 void launch_mlp_forward_array(long long n, const float * params, const float * norm, const float * feat, float * out,
                               float * z1s, float * h1s, float * z2s, int * err, cudaStream_t st);
-void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const int * slot_of,
-                              const int * nv, long long rows_max, const CgState * cg, float inv_alpha0,
-                              float inv_rho0, float inv_nreal, float * feat_out, int * err, cudaStream_t st);
+// node mode: every slot of the active bricks (inactive slots are skipped), the
+// active-node count at B.seg_off[B.nseg]
+void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const BrickArrays & B,
+                              int bn_log2, long long slots_max, const CgState * cg, float inv_alpha0, float inv_rho0,
+                              float inv_nreal, int * err, cudaStream_t st);
 void launch_node_features(const NodeArrays & N, const int * slot_of, const int * nv, long long rows_max,
                           const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal, float * feat_out,
                           cudaStream_t st);

@@ -124,8 +124,9 @@ def test_history_features_match_pressure_history(swc_mod):
         a2 = a1 & alive(1)
         a3 = a2 & alive(2)
         p1, p2, p3 = back(0) * a1, back(1) * a2, back(2) * a3
-        base = np.where(a2, 2 * p1 - p2, p1)
-        d1, d2, q = (base - p1) * w, np.where(a3, p1 - 2 * p2 + p3, 0.0) * w, p1 * w
+        dp1, dp2 = np.where(a2, p1 - p2, 0.0), np.where(a3, p1 - 2 * p2 + p3, 0.0)
+        base = p1 + dp1 + dp2  # quadratic extrapolation where the history allows
+        d1, d2, q = dp1 * w, dp2 * w, p1 * w
         s = np.sqrt(d1 * d1 + d2 * d2) + _lib.MLP_SCALE_EPS
         # FP32 pressures on the device: compare in the units of each quantity
         tol = 2e-5 * np.abs(p).max() * np.abs(w).max()

@@ -208,7 +208,7 @@ def test_warm_start_modes_agree(swc_mod, oracle_mod):
 
 
 def test_extrapolated_warm_start(swc_mod):
-    """Warm start extrapolated in time per lattice node (2 p_{n-1} - p_{n-2}): the
+    """Warm start extrapolated in time per lattice node (quadratic, 3 p1 - 3 p2 + p3): the
     same solution as the node-mapped start to the CG tolerance; the node-mapped
     start on the first advance (no history) and after a standalone project() or a
     switch into the mode, the extrapolation from the next advance on."""
