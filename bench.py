@@ -11,10 +11,12 @@ events on the library's stream) with the state resident in HBM; ``e2e`` runs the
 same steps through the public API with host FP64 buffers (pinned), the
 host->device copy of each step's particle state and the device->host read of
 its result inside the timed region.  The headline form is the learned warm
-start (the trained model in swc/models/, prediction kept without the residual
-fallback); ``forms`` reports plain CG from the node-mapped previous pressure,
-from the reference's stale prefix and from zero, and the learned start with
-the fallback, all on the same scene and steps.
+start (the trained model in swc/models/: a per-node correction of the
+pressure extrapolated in time, kept when it starts CG from a smaller residual
+than the extrapolation itself); ``forms`` reports plain CG from the
+node-mapped previous pressure, from the reference's stale prefix and from
+zero, the extrapolated start alone and the learned start without the
+residual test, all on the same scene and steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl swc|reference]
 
@@ -409,7 +411,7 @@ def main():
                     help="only the timed steps (for profiler captures); prints a reduced line")
     args = ap.parse_args()
     if args.warm_start == "auto":
-        args.warm_start = "learned_no_fallback" if os.path.exists(MODEL) else "node"
+        args.warm_start = "learned" if os.path.exists(MODEL) else "node"
     if args.impl == "reference":
         if args.steps > 10:
             args.steps = 10  # each reference step is seconds of CPU work

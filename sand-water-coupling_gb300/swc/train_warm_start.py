@@ -85,13 +85,13 @@ def main(argv=None):
     ap.add_argument("--particles", type=int, default=400_000)
     ap.add_argument("--keep", type=float, default=0.02)
     ap.add_argument("--every", type=int, default=1)
-    ap.add_argument("--block-seeds", type=int, default=0)
+    ap.add_argument("--block-seeds", type=int, default=12)
     ap.add_argument("--block-n", type=int, default=80)
     ap.add_argument("--block-steps", type=int, default=100)
-    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--eval-n", type=int, default=128)
-    ap.add_argument("--eval-steps", type=int, default=20)
+    ap.add_argument("--eval-steps", type=int, default=50)
     args = ap.parse_args(argv)
 
     f, t, info = collect_dataset(args.seeds, args.steps, args.particles, args.keep, args.every, args.block_seeds,
