@@ -60,9 +60,10 @@ def peaks():
 
 
 SM_MAX_MHZ = 2070.0
-# ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_cg_spmv launch on the
-# 128^3 block (32,769,792 B at 2,246,535 active nodes), per active node
-DRAM_BYTES_PER_NODE = {"cg_spmv": 32769792 / 2246535}
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 128^3 block,
+# per active node of the captured launch: k_cg_spmv 32,769,792 B at 2,246,535 nodes,
+# k_node_gather 88,687,616 + 14,859,776 B at 2,246,538 nodes (profiles/)
+DRAM_BYTES_PER_NODE = {"cg_spmv": 32769792 / 2246535, "virtual_gather": (88687616 + 14859776) / 2246538}
 
 
 class ClockSampler:
@@ -279,14 +280,14 @@ def run_gpu_arm(args):
         "pressure_gradient": 32 * n + 8 * nv + 48 * nb,  # pos, vel r/w; V, p; boundary pos/vel/nrm
         "density": 16 * n + 4 * n + 4 * n,
         "forces": 32 * n + 16 * n,
-        "mlp_forward": 28 * nv,  # slot_of, D, alpha_hat, n_real, n_virt, p_prev, rho read; p0 written
+        "mlp_forward": 32 * nv,  # per slot: flag, D, alpha_hat, n_real, p_base, p1, d2, rho read; p0 written
     }
     cg_ms = kern["cg_direction"] + kern["cg_spmv"] + kern["cg_update"]
     dominant = max(("cg_spmv", "virtual_gather", "pressure_gradient"),
                    key=lambda k: kern[k] * (np.mean(iters) if k == "cg_spmv" else 1))
     ach = alg[dominant] / (kern[dominant] / 1e3) / 1e9
-    # DRAM bytes (read + write) per active node of one launch, from the ncu capture of
-    # the same workload summarised in profiles/k_cg_spmv_block128.md
+    # DRAM bytes (read + write) per active node of one launch, from the ncu captures of
+    # the same workload summarised in profiles/
     traffic = DRAM_BYTES_PER_NODE[dominant] * nv if dominant in DRAM_BYTES_PER_NODE else None
     roofline = {"kernel": dominant, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                 "frac": ach / hbm, "peak_source": peak_kind, "traffic": traffic,
