@@ -48,40 +48,6 @@ template<int DIM> __device__ __forceinline__ long long row_base(int b, int ly, i
     return (long long) b * G::BN + G::BX * (ly + G::BY * lz);
 }
 
-// alpha_hat_I = max(-sum_J alpha_IJ, alpha0) (calculateCoef, VirtualParticle.cpp:149-169).
-template<int DIM>
-__global__ void __launch_bounds__(KG<DIM>::BT) k_ahat(Lattice L, Phys P, const int * __restrict__ blist,
-                                                      const int * __restrict__ bcount,
-                                                      const unsigned char * __restrict__ bflag, NodeArrays N,
-                                                      Stencil S) {
-    using G = BrickGeom<DIM>;
-    __shared__ __align__(16) float tile[G::TILE];
-    const int nb = *bcount;
-    const int t = threadIdx.x, ly = t % G::BY, lz = t / G::BY;
-    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
-        const int b   = blist[bi];
-        const int3 bc = brick_coords(L, b);
-        __syncthreads();
-        load_tile4<DIM>(L, bflag, bc, tile, [&](long long s) { return ld4(N.V, s); });
-        __syncthreads();
-        if (t < KG<DIM>::NT) {
-            float acc[G::BX];
-            stencil_row<DIM>(tile, ly, lz, S, acc);
-            const long long base = row_base<DIM>(b, ly, lz);
-#pragma unroll
-            for (int k = 0; k < G::BX / 4; k++) {
-                const uchar4 f = *reinterpret_cast<const uchar4 *>(N.flag + base + 4 * k);
-                float4 a;
-                a.x = f.x ? fmaxf(-acc[4 * k], P.alpha0) : 1.f;
-                a.y = f.y ? fmaxf(-acc[4 * k + 1], P.alpha0) : 1.f;
-                a.z = f.z ? fmaxf(-acc[4 * k + 2], P.alpha0) : 1.f;
-                a.w = f.w ? fmaxf(-acc[4 * k + 3], P.alpha0) : 1.f;
-                st4(N.ahat, base + 4 * k, a);
-            }
-        }
-    }
-}
-
 // y = A v (test hook).
 template<int DIM>
 __global__ void __launch_bounds__(KG<DIM>::BT) k_apply_operator(Lattice L, const int * __restrict__ blist,
@@ -118,73 +84,22 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_apply_operator(Lattice L, const
     }
 }
 
-// CG start: r = b - A x0, d0 = r, |r|^2, |b|^2, threshold and iteration cap
-// (Eigen's stopping rule: |r|^2 < max(tol, eps/|b|)^2 |b|^2, cap 2 N_v).
+// The base start won the residual test: x = xb, r = d = rb (all slots of the
+// active bricks, 16-byte streaming).
 template<int DIM>
-__global__ void __launch_bounds__(KG<DIM>::BT) k_cg_init(Lattice L, const int * __restrict__ blist,
-                                                         const int * __restrict__ bcount,
-                                                         const unsigned char * __restrict__ bflag, NodeArrays N,
-                                                         Stencil S, CgState * cg, double * __restrict__ partials,
-                                                         double tol, int max_iterations, const int * __restrict__ nv) {
+__global__ void __launch_bounds__(kUT) k_cg_pick_base(const int * __restrict__ blist, const int * __restrict__ bcount,
+                                                      NodeArrays N, const float * __restrict__ xb,
+                                                      const float * __restrict__ rb, const CgState * __restrict__ cg) {
     using G = BrickGeom<DIM>;
-    constexpr int BT = KG<DIM>::BT;
-    __shared__ __align__(16) float tile[G::TILE];
-    __shared__ double red[BT / 32 + 1];
-    __shared__ int last;
+    constexpr int Q = G::BN / 4;
+    if (cg->start != 1) return;
     const int nb = *bcount;
-    const int t = threadIdx.x, ly = t % G::BY, lz = t / G::BY;
-    FF rr{0.f, 0.f}, bb{0.f, 0.f};
-    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x) {
-        const int b   = blist[bi];
-        const int3 bc = brick_coords(L, b);
-        __syncthreads();
-        load_tile4<DIM>(L, bflag, bc, tile, [&](long long s) { return mul4(ld4(N.V, s), ld4(N.x, s)); });
-        __syncthreads();
-        if (t < KG<DIM>::NT) {
-            float acc[G::BX];
-            stencil_row<DIM>(tile, ly, lz, S, acc);
-            const long long base = row_base<DIM>(b, ly, lz);
-#pragma unroll
-            for (int k = 0; k < G::BX / 4; k++) {
-                const float4 xv = ld4(N.x, base + 4 * k), a = ld4(N.ahat, base + 4 * k), bv = ld4(N.D, base + 4 * k);
-                const uchar4 f = *reinterpret_cast<const uchar4 *>(N.flag + base + 4 * k);
-                float r[4];
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const float q = compb(f, j) ? fmaf(comp(a, j), comp(xv, j), acc[4 * k + j]) : comp(xv, j);
-                    r[j]          = comp(bv, j) - q;
-                    ff_add_prod(rr, r[j], r[j]);
-                    ff_add_prod(bb, comp(bv, j), comp(bv, j));
-                }
-                const float4 r4 = make_float4(r[0], r[1], r[2], r[3]);
-                st4(N.r, base + 4 * k, r4);
-                st4(N.d, base + 4 * k, r4);
-            }
-        }
-    }
-    double part[2] = {block_sum_ff<BT>(rr, red), 0.0};
-    part[1]        = block_sum_ff<BT>(bb, red);
-    double tot[2];
-    if (grid_reduce<BT, 2>(part, partials, &cg->ticket[0], tot, red, &last) && threadIdx.x == 0) {
-        const double srr = tot[0], sbb = tot[1];
-        cg->bb      = sbb;
-        cg->rr      = srr;
-        cg->rr0     = srr;
-        cg->rr_prev = 0;
-        cg->pq      = 0;
-        cg->iter    = 0;
-        const int n  = *nv;
-        cg->max_iter = max_iterations >= 0 ? max_iterations : 2 * n;
-        const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
-        if (n == 0 || sbb == 0.0) {
-            cg->threshold = 0;
-            cg->done      = sbb == 0.0 ? 4 : 1;  // 4: zero right-hand side -> x = 0
-        } else {
-            const double tt = fmax(tol, eps / sqrt(sbb));
-            cg->threshold   = fmax(tt * tt * sbb, dmin);
-            cg->done        = srr < cg->threshold ? 1 : (srr != srr ? 3 : 0);
-            if (cg->done == 0 && cg->max_iter <= 0) cg->done = 2;
-        }
+    for (long long e = blockIdx.x * (long long) kUT + threadIdx.x; e < (long long) nb * Q; e += (long long) gridDim.x * kUT) {
+        const long long s = (long long) blist[e / Q] * G::BN + 4 * (e % Q);
+        const float4 r = ld4(rb, s);
+        st4(N.x, s, ld4(xb, s));
+        st4(N.r, s, r);
+        st4(N.d, s, r);
     }
 }
 
@@ -325,6 +240,145 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_cg_spmv(Lattice L, const int * 
     }
 }
 
+// Row-stencil passes on the SpMV's tile pipeline (neighbour table, halo tile
+// of `src` copied with cp.async one brick ahead, static brick striding over a
+// resident grid); the stencil arithmetic is stencil_row's, so the results equal
+// the single-buffered versions bit for bit.
+//   kRowsAhat:  alpha_hat = max(-sum_J alpha_IJ, alpha0) from src = V
+//               (calculateCoef, VirtualParticle.cpp:149-169).
+//   kRowsResid: r = b - A x from src = V x: r (and d when non-null) written,
+//               |r|^2 and |b|^2 summed (deterministic) into sums[0..1].
+enum { kRowsAhat = 0, kRowsResid = 1 };
+template<int DIM, int OP>
+__global__ void __launch_bounds__(KG<DIM>::BT) k_rows_tiled(Lattice L, Phys P, const int * __restrict__ blist,
+                                                            const int * __restrict__ bcount,
+                                                            const unsigned char * __restrict__ bflag, NodeArrays N,
+                                                            Stencil S, const float * __restrict__ src,
+                                                            const float * __restrict__ xin, float * __restrict__ r_out,
+                                                            float * __restrict__ d_out, double * __restrict__ sums,
+                                                            double * __restrict__ partials,
+                                                            unsigned int * __restrict__ ticket) {
+    using G = BrickGeom<DIM>;
+    using T = SpmvTile<DIM>;
+    constexpr int BT = KG<DIM>::BT;
+    __shared__ __align__(16) float tile[2][T::TILE];
+    __shared__ int tab[2][27];
+    __shared__ double red[BT / 32 + 1];
+    __shared__ int last;
+    const int nb = *bcount;
+    const int t = threadIdx.x, ly = t % G::BY, lz = t / G::BY;
+    FF rr{0.f, 0.f}, bb{0.f, 0.f};
+    if (blockIdx.x < nb) neighbour_table<DIM>(L, bflag, blist[blockIdx.x], tab[0]);
+    __syncthreads();
+    if (blockIdx.x < nb) prefetch_u_tile<DIM>(tab[0], src, tile[0]);
+    cp_async_commit();
+    int k = 0;
+    for (int bi = blockIdx.x; bi < nb; bi += gridDim.x, k ^= 1) {
+        const int nxt = bi + gridDim.x;
+        if (nxt < nb) neighbour_table<DIM>(L, bflag, blist[nxt], tab[k ^ 1]);
+        __syncthreads();
+        if (nxt < nb) prefetch_u_tile<DIM>(tab[k ^ 1], src, tile[k ^ 1]);
+        cp_async_commit();
+        cp_async_wait1();  // the current tile has landed
+        __syncthreads();
+        const int b = blist[bi];
+        if (t < KG<DIM>::NT) {
+            float acc[G::BX];
+            stencil_row_t<DIM, T::PX, T::TY, T::HY, T::HZ>(tile[k], ly, lz, S, acc);
+            const long long base = row_base<DIM>(b, ly, lz);
+#pragma unroll
+            for (int kk = 0; kk < G::BX / 4; kk++) {
+                const uchar4 f = *reinterpret_cast<const uchar4 *>(N.flag + base + 4 * kk);
+                if (OP == kRowsAhat) {
+                    float4 a;
+                    a.x = f.x ? fmaxf(-acc[4 * kk], P.alpha0) : 1.f;
+                    a.y = f.y ? fmaxf(-acc[4 * kk + 1], P.alpha0) : 1.f;
+                    a.z = f.z ? fmaxf(-acc[4 * kk + 2], P.alpha0) : 1.f;
+                    a.w = f.w ? fmaxf(-acc[4 * kk + 3], P.alpha0) : 1.f;
+                    st4(N.ahat, base + 4 * kk, a);
+                } else {
+                    const float4 xv = ld4(xin, base + 4 * kk), a = ld4(N.ahat, base + 4 * kk),
+                                 bv = ld4(N.D, base + 4 * kk);
+                    float r[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const float q = compb(f, j) ? fmaf(comp(a, j), comp(xv, j), acc[4 * kk + j]) : comp(xv, j);
+                        r[j]          = comp(bv, j) - q;
+                        ff_add_prod(rr, r[j], r[j]);
+                        ff_add_prod(bb, comp(bv, j), comp(bv, j));
+                    }
+                    const float4 r4 = make_float4(r[0], r[1], r[2], r[3]);
+                    st4(r_out, base + 4 * kk, r4);
+                    if (d_out) st4(d_out, base + 4 * kk, r4);
+                }
+            }
+        }
+        __syncthreads();  // tile[k] and tab[k] are refilled two iterations later
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    if (OP == kRowsResid) {
+        double part[2] = {block_sum_ff<BT>(rr, red), 0.0};
+        part[1]        = block_sum_ff<BT>(bb, red);
+        double tot[2];
+        if (grid_reduce<BT, 2>(part, partials, ticket, tot, red, &last) && threadIdx.x == 0) {
+            sums[0] = tot[0];
+            sums[1] = tot[1];
+        }
+    }
+}
+
+// u = V x over the slots of the active bricks (16-byte streaming).
+template<int DIM>
+__global__ void __launch_bounds__(kUT) k_vmul(const int * __restrict__ blist, const int * __restrict__ bcount,
+                                              const float * __restrict__ V, const float * __restrict__ x,
+                                              float * __restrict__ u) {
+    using G = BrickGeom<DIM>;
+    constexpr int Q = G::BN / 4;
+    const long long total = (long long) (*bcount) * Q;
+    for (long long e = blockIdx.x * (long long) kUT + threadIdx.x; e < total; e += (long long) gridDim.x * kUT) {
+        const long long s = (long long) blist[e / Q] * G::BN + 4 * (e % Q);
+        st4(u, s, mul4(ld4(V, s), ld4(x, s)));
+    }
+}
+
+// CG start state from the residual sums (Eigen's stopping rule:
+// |r|^2 < max(tol, eps/|b|)^2 |b|^2, cap 2 N_v).  With a second candidate
+// (sums_b, the base start of the learned warm start) the prediction is kept
+// when the network reported no error, its residual is finite and, unless
+// keep_prediction, not larger than the base's; cg->start records the choice
+// (0 prediction, 1 base) for k_cg_pick_base and the host.
+__global__ void k_cg_start(CgState * cg, const double * __restrict__ sums_l, const double * __restrict__ sums_b,
+                           const int * __restrict__ mlp_err, int keep_prediction, double tol, int max_iterations,
+                           const int * __restrict__ nv) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double srr_l = sums_l[0], sbb = sums_l[1];
+    bool keep = true;
+    if (sums_b) {
+        const double srr_b = sums_b[0];
+        keep = (!mlp_err || *mlp_err == 0) && srr_l == srr_l && (keep_prediction || srr_l <= srr_b);
+    }
+    const double srr = keep ? srr_l : sums_b[0];
+    cg->start   = keep ? 0 : 1;
+    cg->bb      = sbb;
+    cg->rr      = srr;
+    cg->rr0     = srr;
+    cg->rr_prev = 0;
+    cg->pq      = 0;
+    cg->iter    = 0;
+    const int n  = *nv;
+    cg->max_iter = max_iterations >= 0 ? max_iterations : 2 * n;
+    const double eps = 2.220446049250313e-16, dmin = 2.2250738585072014e-308;
+    if (n == 0 || sbb == 0.0) {
+        cg->threshold = 0;
+        cg->done      = sbb == 0.0 ? 4 : 1;  // 4: zero right-hand side -> x = 0
+    } else {
+        const double tt = fmax(tol, eps / sqrt(sbb));
+        cg->threshold   = fmax(tt * tt * sbb, dmin);
+        cg->done        = srr < cg->threshold ? 1 : (srr != srr ? 3 : 0);
+        if (cg->done == 0 && cg->max_iter <= 0) cg->done = 2;
+    }
+}
+
 // Iteration part 2: alpha = rr / pq; x += alpha d_i; r -= alpha q; rr = r.r;
 // convergence test |r|^2 < threshold (16-byte streaming).
 template<int DIM>
@@ -439,18 +493,40 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_true_residual(Lattice L, const 
 template<int DIM>
 void launch_ahat(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
                  int sgrid, cudaStream_t st) {
-    k_ahat<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, P, B.list, B.count, B.flag, N, S);
+    k_rows_tiled<DIM, kRowsAhat><<<sgrid, KG<DIM>::BT, 0, st>>>(L, P, B.list, B.count, B.flag, N, S, N.V, nullptr, nullptr,
+                                                                nullptr, nullptr, nullptr, nullptr);
 }
 template<int DIM>
 void launch_apply_operator(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
                            const float * in, float * out, int sgrid, cudaStream_t st) {
     k_apply_operator<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, B.list, B.count, B.flag, N, S, in, out);
 }
+// r = b - A x: u = V x staged in N.u (free until the first CG direction pass),
+// the tiled residual pass, the start state.
 template<int DIM>
 void launch_cg_init(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
-                    double * partials, double tol, int max_iterations, const int * nv, int sgrid, cudaStream_t st) {
-    k_cg_init<DIM><<<sgrid, KG<DIM>::BT, 0, st>>>(L, B.list, B.count, B.flag, N, S, cg, partials, tol, max_iterations,
-                                                  nv);
+                    double * partials, double tol, int max_iterations, const int * nv, int sgrid, int ugrid,
+                    cudaStream_t st) {
+    k_vmul<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N.V, N.x, N.u);
+    k_rows_tiled<DIM, kRowsResid><<<sgrid, KG<DIM>::BT, 0, st>>>(L, Phys{}, B.list, B.count, B.flag, N, S, N.u, N.x,
+                                                                 N.r, N.d, cg->sums, partials, &cg->ticket[0]);
+    k_cg_start<<<1, 32, 0, st>>>(cg, cg->sums, nullptr, nullptr, 0, tol, max_iterations, nv);
+}
+// Both candidates' residuals (prediction in N.x -> N.r, N.d; base xb -> rb), the
+// start state keeping the better one, and the base copied in when it wins.
+template<int DIM>
+void launch_cg_init_pick(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
+                         const float * xb, float * rb, const int * mlp_err, bool keep_prediction, CgState * cg,
+                         double * partials, double tol, int max_iterations, const int * nv, int sgrid, int ugrid,
+                         cudaStream_t st) {
+    k_vmul<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N.V, N.x, N.u);
+    k_rows_tiled<DIM, kRowsResid><<<sgrid, KG<DIM>::BT, 0, st>>>(L, Phys{}, B.list, B.count, B.flag, N, S, N.u, N.x,
+                                                                 N.r, N.d, cg->sums, partials, &cg->ticket[0]);
+    k_vmul<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N.V, xb, N.u);
+    k_rows_tiled<DIM, kRowsResid><<<sgrid, KG<DIM>::BT, 0, st>>>(L, Phys{}, B.list, B.count, B.flag, N, S, N.u, xb, rb,
+                                                                 nullptr, cg->sums + 2, partials, &cg->ticket[0]);
+    k_cg_start<<<1, 32, 0, st>>>(cg, cg->sums, cg->sums + 2, mlp_err, keep_prediction ? 1 : 0, tol, max_iterations, nv);
+    k_cg_pick_base<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N, xb, rb, cg);
 }
 // Launch with programmatic stream serialization: the kernel's blocks may be
 // dispatched while the previous kernel on the stream drains; the kernel itself
@@ -517,7 +593,10 @@ void launch_rhs_norm(const BrickArrays & B, const NodeArrays & N, CgState * cg, 
     template void launch_apply_operator<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,   \
                                            const float *, float *, int, cudaStream_t);                                 \
     template void launch_cg_init<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,         \
-                                    CgState *, double *, double, int, const int *, int, cudaStream_t);                 \
+                                    CgState *, double *, double, int, const int *, int, int, cudaStream_t);            \
+    template void launch_cg_init_pick<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,    \
+                                         const float *, float *, const int *, bool, CgState *, double *, double, int,  \
+                                         const int *, int, int, cudaStream_t);                                         \
     template void launch_cg_spmv<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,         \
                                     CgState *, double *, int, cudaStream_t);                                           \
     template void launch_cg_update<D>(const BrickArrays &, const NodeArrays &, CgState *, double *, int, cudaStream_t); \

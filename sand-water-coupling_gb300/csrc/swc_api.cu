@@ -25,7 +25,6 @@ struct HostCg {
     CgState st;
     int     nv;
     int     nbricks;
-    double  rr_node;  // initial |r|^2 of the node-mapped start (learned-start fallback test)
     int     mlp_err;
 };
 
@@ -294,7 +293,7 @@ template<int DIM> void run_generate(swc_ctx * c, bool with_ahat) {
     launch_node_gather<DIM>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel, c->bcellStart,
                             c->bnear, c->ggrid, c->queues, c->stream);
     launch_segments<DIM>(c->L, c->B, c->N, c->scan_tiles, c->grid, c->stream);
-    if (with_ahat) launch_ahat<DIM>(c->L, c->P, c->B, c->N, c->S, c->rgrid, c->stream);
+    if (with_ahat) launch_ahat<DIM>(c->L, c->P, c->B, c->N, c->S, c->sgrid, c->stream);
 }
 
 int capture_graphs(swc_ctx * c) {
@@ -319,35 +318,29 @@ int capture_graphs(swc_ctx * c) {
 
 // CG solve from the warm start in N.x; fills stats.
 // CG start from the current N.x; the device state is mirrored into hcg.
-template<int DIM> int cg_init_sync(swc_ctx * c) {
-    const int * nv = c->B.seg_off + c->B.nseg;
-    launch_cg_init<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->opts.tolerance, c->opts.max_iterations, nv,
-                        c->rgrid, c->stream);
-    CK(cudaMemcpyAsync(&c->hcg->st, c->cg, sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(&c->hcg->nv, nv, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(&c->hcg->nbricks, c->B.count, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    return SWC_OK;
-}
+// CG start state on entry of run_cg: none (run_cg launches the initialisation),
+// on the device only (launched by the caller), or also copied to the host.
+enum { kInitNone = 0, kInitDevice = 1, kInitHost = 2 };
 
-template<int DIM> int run_cg(swc_ctx * c, swc_stats * st, bool initialized) {
+template<int DIM> int run_cg(swc_ctx * c, swc_stats * st, int init_mode) {
     if (!c->g1) {
         CK(cudaStreamSynchronize(c->stream));
         int rc = capture_graphs(c);
         if (rc) return rc;
     }
-    if (!initialized) {
+    if (init_mode != kInitHost) {
         // initial residual on the device; its state comes back with the first
         // convergence check (the iteration kernels are no-ops once CG is done)
         const int * nv = c->B.seg_off + c->B.nseg;
-        launch_cg_init<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->opts.tolerance, c->opts.max_iterations, nv,
-                            c->rgrid, c->stream);
+        if (init_mode == kInitNone)
+            launch_cg_init<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->opts.tolerance, c->opts.max_iterations,
+                                nv, c->sgrid, c->grid, c->stream);
         c->hcg->st.done     = 0;
         c->hcg->st.iter     = 0;
         c->hcg->st.max_iter = c->opts.max_iterations >= 0 ? c->opts.max_iterations : std::numeric_limits<int>::max();
     }
     int first   = c->opts.check_interval > 0 ? c->opts.check_interval : std::max(4, c->last_iters);
-    bool counts = initialized;
+    bool counts = init_mode == kInitHost;
     while (!c->hcg->st.done) {
         const int room = c->hcg->st.max_iter - c->hcg->st.iter;
         int m          = std::min(first, std::max(room, 1));
@@ -408,8 +401,8 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     const int * nv     = c->B.seg_off + c->B.nseg;
     const size_t slots = size_t(c->L.nbricks) * BrickGeom<DIM>::BN;
     int used           = mode;
-    bool initialized   = false;
-    bool mlp_checked   = false;
+    int init_mode      = kInitNone;
+    bool mlp_checked   = false, picked = false;
     // Pressure history (extrapolated and learned warm starts, logged features):
     // the base start is 3 p1 - 3 p2 + p3 with three steps of history, 2 p1 - p2
     // with two, p1 (node-mapped) with fewer; the history spans consecutive
@@ -426,15 +419,7 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
         if (!no_fallback)
             CK(cudaMemcpyAsync(c->xprev, c->N.x, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
         if (logging) launch_slot_of<DIM>(c->L, c->B, c->N, c->slot_of, c->grid, c->stream);
-        // |b|^2 for sD and (for the fallback test) the initial residual of the
-        // base start, read back with the learned start's (one host synchronisation)
-        if (no_fallback) launch_rhs_norm<DIM>(c->B, c->N, c->cg, c->partials, c->grid, c->stream);
-        else {
-            launch_cg_init<DIM>(c->L, c->B, c->N, c->S, c->cg, c->partials, c->opts.tolerance, c->opts.max_iterations,
-                                nv, c->rgrid, c->stream);
-            CK(cudaMemcpyAsync(&c->hcg->rr_node, &c->cg->rr0, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-        }
-        int rc = SWC_OK;
+        launch_rhs_norm<DIM>(c->B, c->N, c->cg, c->partials, c->grid, c->stream);  // |b|^2 for sD
         const float inv_a0 = float(1.0 / c->alpha0), inv_r0 = float(1.0 / c->rho0), inv_nr = 1.f / 32.f;
         if (logging)
             launch_node_features(c->N, c->slot_of, nv, c->L.ncells, c->cg, inv_a0, inv_r0, inv_nr, c->feat_buf,
@@ -443,30 +428,21 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
             launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->B, DIM == 3 ? 9 : 8, (long long) slots, c->cg,
                                      inv_a0, inv_r0, inv_nr, c->mlp_err, c->stream);
             CK(cudaMemcpyAsync(&c->hcg->mlp_err, c->mlp_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+            mlp_checked = true;  // the error flag is read with CG's first check
             if (no_fallback) {
-                // CG initialises from the prediction without a host round trip; the
-                // tensor-core pass's error flag is read with CG's first check
-                used        = SWC_WARM_LEARNED;
-                mlp_checked = true;
+                used = SWC_WARM_LEARNED;  // CG initialises from the prediction
             } else {
-                if ((rc = cg_init_sync<DIM>(c))) return rc;
-                const int err        = c->hcg->mlp_err;
-                const double rr_base = c->hcg->rr_node, rr_mlp = c->hcg->st.rr0;
-                if (err || !(rr_mlp == rr_mlp) || (!c->opts.learned_no_fallback && !(rr_mlp <= rr_base))) {
-                    // the prediction starts from a larger residual (or failed): keep the base start
-                    CK(cudaMemcpyAsync(c->N.x, c->xprev, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
-                    if ((rc = cg_init_sync<DIM>(c))) return rc;
-                    used = base_used;
-                } else used = SWC_WARM_LEARNED;
-                initialized = true;
+                // residual test on the device: both starts' residuals, the smaller kept
+                launch_cg_init_pick<DIM>(c->L, c->B, c->N, c->S, c->xprev, c->N.q, c->mlp_err, false, c->cg,
+                                         c->partials, c->opts.tolerance, c->opts.max_iterations, nv, c->sgrid,
+                                         c->grid, c->stream);
+                init_mode = kInitDevice;
+                picked    = true;
             }
-        } else if (mode == SWC_WARM_EXTRAPOLATE || mode == SWC_WARM_LEARNED) {
-            if ((rc = cg_init_sync<DIM>(c))) return rc;  // host copy of the base start's state
-            initialized = true;
         } else if (mode == SWC_WARM_NODE) {
             // node-mapped previous pressure, kept in xm1 by the history shift
             CK(cudaMemcpyAsync(c->N.x, c->N.xm1, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
-        } else {
+        } else if (mode != SWC_WARM_EXTRAPOLATE && mode != SWC_WARM_LEARNED) {
             launch_warm_start<DIM>(c->L, c->B, c->N, mode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
         }
     } else if (hist_on) {
@@ -477,9 +453,11 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
                                c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
     }
     mark(c, 5);
-    int rc = run_cg<DIM>(c, st, initialized);
+    int rc = run_cg<DIM>(c, st, init_mode);
+    if (picked) used = c->hcg->st.start == 0 ? SWC_WARM_LEARNED : base_used;
     if (mlp_checked && c->hcg->mlp_err) {
-        c->err = "learned warm start: the tensor-core pass timed out; CG ran from its output";
+        c->err = picked ? "learned warm start: the tensor-core pass timed out; CG ran from the base start"
+                        : "learned warm start: the tensor-core pass timed out; CG ran from its output";
         used   = base_used;
     }
     c->extrap_steps   = (hist_on && c->extrap_shifted && (rc == SWC_OK || rc == SWC_CG_NOT_CONVERGED)) ? c->extrap_steps + 1 : 0;
@@ -718,7 +696,7 @@ int swc_create(const swc_scene * s, const swc_solver_opts * o, swc_ctx ** out) {
         c->ggrid      = std::max(1, std::min(L.nbricks, c->num_sms * go));
         c->pgrid      = std::max(1, std::min(L.nbricks, c->num_sms * po));
     }
-    const size_t npart = 2 * size_t(std::max({c->grid, c->sgrid, c->rgrid})) + 8;
+    const size_t npart = 3 * size_t(std::max({c->grid, c->sgrid, c->rgrid})) + 8;
     setup_phys(c);
     int rc = SWC_OK;
     const size_t slots = size_t(L.nbricks) * bx * by * bz;

@@ -446,7 +446,8 @@ struct CgState {
     int    iter;       // completed iterations (SpMV count in the loop)
     int    done;       // 0 running, 1 converged, 2 max iterations, 3 breakdown / NaN
     int    max_iter;
-    int    pad;
+    int    start;      // start kept by k_cg_start: 0 prediction, 1 base
+    double sums[4];    // residual sums of the CG start: |r|^2, |b|^2 (prediction / only start), |r|^2, |b|^2 (base)
     unsigned int ticket[4];
     int    is_last[4];
 };

@@ -144,7 +144,16 @@ void launch_compact_export(const Lattice & L, const BrickArrays & B, const NodeA
 // CG
 template<int DIM>
 void launch_cg_init(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
-                    double * partials, double tol, int max_iterations, const int * nv, int sgrid, cudaStream_t st);
+                    double * partials, double tol, int max_iterations, const int * nv, int sgrid, int ugrid,
+                    cudaStream_t st);
+// CG start from the better of two candidates (x: prediction, xb: base start) by
+// their residuals, decided on the device (cg->start: 0 prediction, 1 base); rb is
+// scratch for the base's residual.  keep_prediction skips the comparison.
+template<int DIM>
+void launch_cg_init_pick(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
+                         const float * xb, float * rb, const int * mlp_err, bool keep_prediction, CgState * cg,
+                         double * partials, double tol, int max_iterations, const int * nv, int rgrid, int ugrid,
+                         cudaStream_t st);
 template<int DIM>
 void launch_cg_iteration(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
                          CgState * cg, double * partials, int sgrid, int ugrid, cudaStream_t st);
