@@ -346,36 +346,46 @@ __global__ void __launch_bounds__(256) k_boundary_density(float4 * __restrict__ 
     }
 }
 
-// Mark every brick that holds a node within h of a real particle (only those
-// nodes can have a positive weight, VirtualParticle.cpp:50-56).
-// `pflag` (optional) marks the brick of the particle's own cell: the bricks the
-// brick-tiled particle kernels visit.
+// Bricks holding a node within reach of a particle (bflag: only nodes within h of
+// a real particle can have a positive weight, VirtualParticle.cpp:50-56) and
+// bricks holding a particle's own cell (pflag: the bricks the brick-tiled
+// particle kernels visit), from the sorted cell ranges.  A particle in cell c
+// reaches nodes c - ceil(h/dx) .. c + ceil(h/dx) along each axis; `reach` adds one
+// for FP32 rounding, so a brick is flagged when a particle lies in its cells
+// dilated by `reach` (particles outside the lattice sit in the border cells, so
+// the dilation still covers the nodes they reach).  One warp per brick, lanes
+// over the dilated cell rows; every brick's flag is written.
 template<int DIM>
-__global__ void k_mark_bricks(const float4 * __restrict__ pos, long long n, Lattice L, Phys P,
-                              unsigned char * __restrict__ bflag, unsigned char * __restrict__ pflag) {
-    using G = BrickGeom<DIM>;
-    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
-        const float4 p = pos[i];
-        if (pflag) {
-            const int3 c = cell_of<DIM>(L, p.x, p.y, p.z);
-            pflag[c.x / G::BX + L.bnx * (c.y / G::BY + L.bny * (c.z / G::BZ))] = 1;
+__global__ void __launch_bounds__(256) k_mark_bricks(Lattice L, const int * __restrict__ cellStart, int reach,
+                                                     unsigned char * __restrict__ bflag,
+                                                     unsigned char * __restrict__ pflag) {
+    using G               = BrickGeom<DIM>;
+    const int lane        = threadIdx.x & 31;
+    const long long warp  = (blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5;
+    const long long warps = (gridDim.x * (long long) blockDim.x) >> 5;
+    for (long long b = warp; b < L.nbricks; b += warps) {
+        const int bx = int(b % L.bnx), by = int((b / L.bnx) % L.bny), bz = int(b / ((long long) L.bnx * L.bny));
+        const int ox0 = bx * G::BX, ox1 = min(ox0 + G::BX - 1, L.nx - 1);
+        const int oy0 = by * G::BY, oy1 = min(oy0 + G::BY - 1, L.ny - 1);
+        const int oz0 = DIM == 3 ? bz * G::BZ : 0, oz1 = DIM == 3 ? min(oz0 + G::BZ - 1, L.nz - 1) : 0;
+        const int x0 = max(ox0 - reach, 0), x1 = min(ox1 + reach, L.nx - 1);
+        const int y0 = max(oy0 - reach, 0), y1 = min(oy1 + reach, L.ny - 1);
+        const int z0 = DIM == 3 ? max(oz0 - reach, 0) : 0, z1 = DIM == 3 ? min(oz1 + reach, L.nz - 1) : 0;
+        const int nyr = y1 - y0 + 1, rows = nyr * (z1 - z0 + 1);
+        bool any = false, own = false;
+        for (int r = lane; r < rows; r += 32) {
+            const int y = y0 + r % nyr, z = z0 + r / nyr;
+            const long long row = (long long) L.nx * (y + (long long) L.ny * z);
+            any = any || cellStart[row + x1 + 1] > cellStart[row + x0];
+            if (pflag && y >= oy0 && y <= oy1 && z >= oz0 && z <= oz1)
+                own = own || cellStart[row + ox1 + 1] > cellStart[row + ox0];
         }
-        const int x0 = clampi(__float2int_ru((p.x - P.h - L.ox) * L.inv_dx), 0, L.nx - 1);
-        const int x1 = clampi(__float2int_rd((p.x + P.h - L.ox) * L.inv_dx), 0, L.nx - 1);
-        const int y0 = clampi(__float2int_ru((p.y - P.h - L.oy) * L.inv_dx), 0, L.ny - 1);
-        const int y1 = clampi(__float2int_rd((p.y + P.h - L.oy) * L.inv_dx), 0, L.ny - 1);
-        int z0 = 0, z1 = 0;
-        if (DIM == 3) {
-            z0 = clampi(__float2int_ru((p.z - P.h - L.oz) * L.inv_dx), 0, L.nz - 1);
-            z1 = clampi(__float2int_rd((p.z + P.h - L.oz) * L.inv_dx), 0, L.nz - 1);
+        any = __any_sync(0xffffffffu, any);
+        own = __any_sync(0xffffffffu, own);
+        if (lane == 0) {
+            bflag[b] = any ? 1 : 0;
+            if (pflag) pflag[b] = own ? 1 : 0;
         }
-        // widen by one node to stay safe against FP32 rounding at the support edge
-        const int bx0 = max(x0 - 1, 0) / G::BX, bx1 = min(x1 + 1, L.nx - 1) / G::BX;
-        const int by0 = max(y0 - 1, 0) / G::BY, by1 = min(y1 + 1, L.ny - 1) / G::BY;
-        const int bz0 = DIM == 3 ? max(z0 - 1, 0) / G::BZ : 0, bz1 = DIM == 3 ? min(z1 + 1, L.nz - 1) / G::BZ : 0;
-        for (int bz = bz0; bz <= bz1; bz++)
-            for (int by = by0; by <= by1; by++)
-                for (int bx = bx0; bx <= bx1; bx++) bflag[bx + L.bnx * (by + L.bny * bz)] = 1;
     }
 }
 
@@ -651,8 +661,8 @@ void launch_scan(const int * in, long long n, int * out, int * tile_buf, cudaStr
 long long scan_tile_count(long long n) { return (n + kScanTile - 1) / kScanTile + 1; }
 
 template<int DIM>
-void launch_bin(const Lattice & L, long long n, float4 * pos, float4 * vel, float4 * aux, int * id, SortScratch & S,
-                int * cellStart, cudaStream_t st) {
+void launch_bin(const Lattice & L, long long n, float4 *& pos, float4 *& vel, float4 *& aux, int *& id,
+                SortScratch & S, int * cellStart, cudaStream_t st) {
     cudaMemsetAsync(S.count, 0, sizeof(int) * L.ncells, st);
     if (n > 0) k_cell_count<DIM><<<grid_for(n, 256), 256, 0, st>>>(pos, n, L, S.key, S.rank, S.count);
     launch_scan(S.count, L.ncells, cellStart, S.tiles, st);
@@ -660,10 +670,11 @@ void launch_bin(const Lattice & L, long long n, float4 * pos, float4 * vel, floa
     k_cell_scatter<<<grid_for(n, 256), 256, 0, st>>>(S.key, S.rank, cellStart, n, S.perm);
     k_cell_sort_segments<<<grid_for(L.ncells, 256), 256, 0, st>>>(cellStart, L.ncells, id, S.perm);
     k_permute<<<grid_for(n, 256), 256, 0, st>>>(S.perm, n, pos, vel, aux, id, S.pos2, S.vel2, S.aux2, S.id2);
-    cudaMemcpyAsync(pos, S.pos2, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(vel, S.vel2, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
-    if (aux) cudaMemcpyAsync(aux, S.aux2, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(id, S.id2, sizeof(int) * n, cudaMemcpyDeviceToDevice, st);
+    // the sorted arrays become the state; the previous ones the next sort's targets
+    std::swap(pos, S.pos2);
+    std::swap(vel, S.vel2);
+    if (aux) std::swap(aux, S.aux2);
+    std::swap(id, S.id2);
 }
 
 template<int DIM>
@@ -692,11 +703,16 @@ void launch_boundary_density(float4 * bpos, float4 * bvel, float * rho, long lon
         k_boundary_density<DIM><<<grid_for(nb, 256, 1 << 20), 256, 0, st>>>(bpos, bvel, rho, nb, L, P, bcellStart);
 }
 template<int DIM>
-void launch_mark_bricks(const float4 * pos, long long n, const Lattice & L, const Phys & P, unsigned char * bflag,
+void launch_mark_bricks(const int * cellStart, long long n, const Lattice & L, const Phys & P, unsigned char * bflag,
                         unsigned char * pflag, cudaStream_t st) {
-    cudaMemsetAsync(bflag, 0, L.nbricks, st);
-    if (pflag) cudaMemsetAsync(pflag, 0, L.nbricks, st);
-    if (n > 0) k_mark_bricks<DIM><<<grid_for(n, 256), 256, 0, st>>>(pos, n, L, P, bflag, pflag);
+    if (n <= 0 || L.nbricks <= 0) {
+        cudaMemsetAsync(bflag, 0, L.nbricks, st);
+        if (pflag) cudaMemsetAsync(pflag, 0, L.nbricks, st);
+        return;
+    }
+    const int reach   = int(std::ceil(double(P.h) / double(L.dx))) + 1;
+    const long long b = (L.nbricks + 7) / 8;  // eight warps per block, one warp per brick
+    k_mark_bricks<DIM><<<int(std::min<long long>(b, 152LL * 64)), 256, 0, st>>>(L, cellStart, reach, bflag, pflag);
 }
 void launch_rotate_boundary(float4 * bpos, float4 * bvel, float4 * bnrm, long long nb, float cx, float cz,
                             float omega, float dt, cudaStream_t st) {
@@ -732,15 +748,15 @@ void launch_debug_neighbors(int which, long long nq, const double * q, const Lat
 }
 
 #define SWC_INST(D)                                                                                                    \
-    template void launch_bin<D>(const Lattice &, long long, float4 *, float4 *, float4 *, int *, SortScratch &, int *, \
-                                cudaStream_t);                                                                         \
+    template void launch_bin<D>(const Lattice &, long long, float4 *&, float4 *&, float4 *&, int *&, SortScratch &,   \
+                                int *, cudaStream_t);                                                                  \
     template void launch_density<D>(const float4 *, float4 *, float *, long long, const Lattice &, const Phys &,       \
                                     const int *, int *, cudaStream_t);                                                 \
     template void launch_forces<D>(const float4 *, const float4 *, float4 *, long long, const Lattice &, const Phys &,  \
                                    const int *, float, int *, cudaStream_t);                                           \
     template void launch_boundary_density<D>(float4 *, float4 *, float *, long long, const Lattice &, const Phys &,    \
                                              const int *, cudaStream_t);                                               \
-    template void launch_mark_bricks<D>(const float4 *, long long, const Lattice &, const Phys &, unsigned char *,     \
+    template void launch_mark_bricks<D>(const int *, long long, const Lattice &, const Phys &, unsigned char *,        \
                                         unsigned char *,                                                               \
                                         cudaStream_t);                                                                 \
     template void launch_debug_neighbors<D>(int, long long, const double *, const Lattice &, const Phys &,            \

@@ -271,12 +271,13 @@ void setup_phys(swc_ctx * c) {
 }
 
 template<int DIM> int run_bin_real(swc_ctx * c) {
-    launch_bin<DIM>(c->L, c->n, c->pos, c->vel, nullptr, c->id, c->sortR, c->cellStart, c->stream);
+    float4 * no_aux = nullptr;
+    launch_bin<DIM>(c->L, c->n, c->pos, c->vel, no_aux, c->id, c->sortR, c->cellStart, c->stream);
     return SWC_OK;
 }
 template<int DIM> int run_bin_boundary(swc_ctx * c) {
     launch_bin<DIM>(c->L, c->nb, c->bpos, c->bvel, c->bnrm, c->bid, c->sortB, c->bcellStart, c->stream);
-    launch_mark_bricks<DIM>(c->bpos, c->nb, c->L, c->P, c->bnear, nullptr, c->stream);
+    launch_mark_bricks<DIM>(c->bcellStart, c->nb, c->L, c->P, c->bnear, nullptr, c->stream);
     return SWC_OK;
 }
 
@@ -287,7 +288,7 @@ inline void mark(swc_ctx * c, int k) {
 // Virtual generation: active bricks, fused gather, reference-order compaction,
 // alpha_hat (VirtualParticle::generateParticles + calculateCoef diagonal).
 template<int DIM> void run_generate(swc_ctx * c, bool with_ahat) {
-    launch_mark_bricks<DIM>(c->pos, c->n, c->L, c->P, c->B.flag, c->pflag, c->stream);
+    launch_mark_bricks<DIM>(c->cellStart, c->n, c->L, c->P, c->B.flag, c->pflag, c->stream);
     launch_brick_list(c->B.flag, c->L.nbricks, c->B.list, c->B.count, c->stream);
     launch_brick_list(c->pflag, c->L.nbricks, c->plist, c->pcount, c->stream);
     launch_node_gather<DIM>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel, c->bcellStart,

@@ -78,8 +78,10 @@ void launch_set_boundary_info(float4 * bpos, float4 * bvel, float * brho, const 
                               const int * bid, long long nb, float bmass, cudaStream_t st);
 void launch_set_moving(float4 * bnrm, const unsigned char * moving, const int * bid, long long nb, cudaStream_t st);
 void launch_max_positive(const float * a, long long n, int * out_bits, cudaStream_t st);
+// counting sort into cells; the sorted arrays are swapped in (pos, vel, aux, id
+// then point at what were the scratch targets)
 template<int DIM>
-void launch_bin(const Lattice & L, long long n, float4 * pos, float4 * vel, float4 * aux, int * id, SortScratch & S,
+void launch_bin(const Lattice & L, long long n, float4 *& pos, float4 *& vel, float4 *& aux, int *& id, SortScratch & S,
                 int * cellStart, cudaStream_t st);
 // Density and forces run one thread per pair of consecutive sorted particles;
 // `left` (n/2 + 3 ints, zeroed once at allocation) collects the pairs that are
@@ -94,7 +96,9 @@ template<int DIM>
 void launch_boundary_density(float4 * bpos, float4 * bvel, float * rho, long long nb, const Lattice & L,
                              const Phys & P, const int * bcellStart, cudaStream_t st);
 template<int DIM>
-void launch_mark_bricks(const float4 * pos, long long n, const Lattice & L, const Phys & P, unsigned char * bflag,
+// bricks within reach of the particles binned in cellStart (and, with pflag, the
+// bricks holding their cells); n = 0 clears the flags
+void launch_mark_bricks(const int * cellStart, long long n, const Lattice & L, const Phys & P, unsigned char * bflag,
                         unsigned char * pflag, cudaStream_t st);
 template<int DIM>
 void launch_debug_neighbors(int which, long long nq, const double * q, const Lattice & L, const Phys & P,
