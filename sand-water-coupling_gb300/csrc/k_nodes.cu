@@ -536,8 +536,10 @@ __device__ float3 gradient_virtual_global(const Lattice & L, const Phys & P, con
     return f;
 }
 
+constexpr int kGradNT = 256;  // threads per block of the pressure gradient (one particle brick per block)
+
 template<int DIM>
-__global__ void __launch_bounds__(kNT) k_pressure_gradient(Lattice L, Phys P, const unsigned char * __restrict__ bflag,
+__global__ void __launch_bounds__(kGradNT) k_pressure_gradient(Lattice L, Phys P, const unsigned char * __restrict__ bflag,
                                                            NodeArrays N, const int * __restrict__ plist,
                                                            const int * __restrict__ pcount,
                                                            const unsigned char * __restrict__ bnear,
@@ -562,7 +564,7 @@ __global__ void __launch_bounds__(kNT) k_pressure_gradient(Lattice L, Phys P, co
         const int b   = plist[bi];
         const int3 bc = brick_coords(L, b);
         const int x0 = bc.x * G::BX, x1 = min(x0 + G::BX, L.nx);
-        load_tile4<DIM, kNT, PX>(L, bflag, bc, tile, [&](long long s) {
+        load_tile4<DIM, kGradNT, PX>(L, bflag, bc, tile, [&](long long s) {
             const float4 v = *reinterpret_cast<const float4 *>(N.V + s), x = *reinterpret_cast<const float4 *>(N.x + s);
             return make_float4(v.x * x.x, v.y * x.y, v.z * x.z, v.w * x.w);
         });
@@ -601,7 +603,7 @@ __global__ void __launch_bounds__(kNT) k_pressure_gradient(Lattice L, Phys P, co
         // tile origin (node coordinates of tile index 0)
         const float tox = float(x0 - G::HALO), toy = float(bc.y * G::BY - G::HALO);
         const float toz = DIM == 3 ? float(bc.z * G::BZ - G::HALO) : 0.f;
-        for (int p = t; p < total; p += kNT) {
+        for (int p = t; p < total; p += kGradNT) {
             int lo = 0, hi = ROWS - 1;
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
@@ -670,12 +672,12 @@ void launch_pressure_gradient(const Lattice & L, const Phys & P, const BrickArra
                               const int * plist, const int * pcount, const unsigned char * bnear, const float4 * pos,
                               float4 * vel, const int * cellStart, const float4 * bpos, const float4 * bvel,
                               const float4 * bnrm, const int * bcellStart, int grid, int * queue, cudaStream_t st) {
-    k_pressure_gradient<DIM><<<grid, kNT, 0, st>>>(L, P, B.flag, N, plist, pcount, bnear, pos, vel, cellStart, bpos,
+    k_pressure_gradient<DIM><<<grid, kGradNT, 0, st>>>(L, P, B.flag, N, plist, pcount, bnear, pos, vel, cellStart, bpos,
                                                    bvel, bnrm, bcellStart, queue);
 }
 template<int DIM> int pressure_gradient_blocks_per_sm() {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pressure_gradient<DIM>, kNT, 0) != cudaSuccess) n = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pressure_gradient<DIM>, kGradNT, 0) != cudaSuccess) n = 1;
     return n > 0 ? n : 1;
 }
 template<int DIM> int node_gather_blocks_per_sm() {
