@@ -93,8 +93,9 @@ struct swc_ctx {
     // (N.xm1, flags two steps back) is valid, and whether this step shifted the flags
     int     extrap_steps   = 0;
     bool    extrap_shifted = false;
-    float *     pcomp = nullptr;
+    float *     pcomp = nullptr;    // last solution in reference order (prefix warm start)
     int *       nv_prev = nullptr;
+    bool        pcomp_stale = false;  // the last projection did not export pcomp (other warm-start modes)
     int *       scan_tiles = nullptr;
     CgState *   cg = nullptr;
     double *    partials = nullptr;
@@ -383,6 +384,16 @@ template<int DIM> int run_cg(swc_ctx * c, swc_stats * st, int init_mode) {
     return status;
 }
 
+// p in reference order into pcomp and N_v into nv_prev (the prefix warm start's
+// previous pressure vector, ParticlesBasedData.h:25-29).
+template<int DIM> int export_prefix(swc_ctx * c) {
+    launch_compact_export<DIM>(c->L, c->B, c->N, c->pcomp, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                               nullptr, nullptr, c->grid, c->stream);
+    CK(cudaMemcpyAsync(c->nv_prev, c->B.seg_off + c->B.nseg, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+    c->pcomp_stale = false;
+    return SWC_OK;
+}
+
 // The projection keeps a pressure history (extrapolated or learned warm start,
 // training-data logging).
 bool history_on(const swc_ctx * c) {
@@ -475,6 +486,7 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
         // report, leave the velocities unprojected and drop the poisoned warm start
         launch_zero_active<DIM>(c->L, c->B, c->N.x, c->grid, c->stream);
         CK(cudaMemsetAsync(c->nv_prev, 0, sizeof(int), c->stream));
+        c->pcomp_stale = false;
         for (int k = 6; k <= 8; k++) mark(c, k);
         return cg_status;
     }
@@ -482,10 +494,11 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     launch_pressure_gradient<DIM>(c->L, c->P, c->B, c->N, c->plist, c->pcount, c->bnear, c->pos, c->vel,
                                   c->cellStart, c->bpos, c->bvel, c->bnrm, c->bcellStart, c->pgrid, c->queues + 2, c->stream);
     mark(c, 7);
-    // p in reference order (next step's prefix warm start) and N_v for it
-    launch_compact_export<DIM>(c->L, c->B, c->N, c->pcomp, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-                               nullptr, nullptr, c->grid, c->stream);
-    CK(cudaMemcpyAsync(c->nv_prev, c->B.seg_off + c->B.nseg, sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+    // p in reference order (the next step's prefix warm start) and N_v for it;
+    // other modes skip it (a switch to the prefix mode exports the last solution)
+    if (mode == SWC_WARM_PREFIX) {
+        if ((rc = export_prefix<DIM>(c))) return rc;
+    } else c->pcomp_stale = true;
     mark(c, 8);
     if (st) {
         st->n_particles     = c->n;
@@ -602,6 +615,7 @@ template<int DIM> int do_initialize(swc_ctx * c) {
     setup_phys(c);
     // no previous pressure: empty prefix, no extrapolation history
     c->extrap_steps = 0;
+    c->pcomp_stale  = false;
     CK(cudaMemsetAsync(c->nv_prev, 0, sizeof(int), c->stream));
     CK(cudaMemsetAsync(c->N.x, 0, sizeof(float) * size_t(c->L.nbricks) * (DIM == 3 ? 512 : 256), c->stream));
     CK(cudaMemsetAsync(c->N.flag, 0, size_t(c->L.nbricks) * (DIM == 3 ? 512 : 256), c->stream));
@@ -844,6 +858,11 @@ int swc_set_stream(swc_ctx * c, void * stream) {
 int swc_set_solver_opts(swc_ctx * c, const swc_solver_opts * o) {
     if (!valid_ctx(c) || !o || o->warm_start < SWC_WARM_PREFIX || o->warm_start > SWC_WARM_EXTRAPOLATE)
         return SWC_BAD_ARG;
+    if (o->warm_start == SWC_WARM_PREFIX && c->pcomp_stale) {
+        // the last solution (still in the lattice slots) as the next prefix start
+        const int rc0 = c->dim == 2 ? export_prefix<2>(c) : export_prefix<3>(c);
+        if (rc0) return rc0;
+    }
     const bool need_vbar = o->keep_virtual_velocity && !c->N.vbar;
     const bool need_feat = o->keep_features && !c->N.nreal;
     c->opts = *o;
@@ -1105,6 +1124,7 @@ int swc_set_pressure(swc_ctx * c, const double * p, int64_t n) {
     if (n > 0) CK(cudaMemcpy(c->pcomp, f.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
     int ni = int(n);
     CK(cudaMemcpy(c->nv_prev, &ni, sizeof(int), cudaMemcpyHostToDevice));
+    c->pcomp_stale = false;
     return SWC_OK;
 }
 

@@ -207,6 +207,28 @@ def test_warm_start_modes_agree(swc_mod, oracle_mod):
     assert results["node"][1] <= results["zero"][1]
 
 
+def test_switch_to_prefix_warm_start(swc_mod):
+    """Modes other than the stale prefix skip the per-step export of the solution in
+    reference order; switching to the prefix mode exports the last solution, so
+    the next solve starts from it as if the prefix mode had run all along."""
+    base = SCENES["block_3d_n24"]().rounded_to_float32()
+    out = {}
+    for first in ("prefix", "node"):
+        liq = swc_mod.DualParticleSphLiquid(base, warm_start=first)
+        liq.initialize()
+        for _ in range(3):
+            assert liq.advance(base.dt)["status"] == 0
+        liq.setSolverOptions(warm_start="prefix")
+        st = liq.advance(base.dt)
+        assert st["status"] == 0
+        out[first] = (liq.getParticles()[1], st["cg_iterations"], st["initial_rel_residual"])
+        liq.close()
+    assert rel(out["node"][0], out["prefix"][0]) < 1e-4
+    assert abs(out["node"][1] - out["prefix"][1]) <= 2, (out["node"][1], out["prefix"][1])
+    # an empty prefix (no export) would start from zero: initial residual 1
+    assert out["node"][2] < 0.9 and abs(out["node"][2] - out["prefix"][2]) < 0.1 * out["prefix"][2] + 1e-3
+
+
 def test_extrapolated_warm_start(swc_mod):
     """Warm start extrapolated in time per lattice node (quadratic, 3 p1 - 3 p2 + p3): the
     same solution as the node-mapped start to the CG tolerance; the node-mapped
