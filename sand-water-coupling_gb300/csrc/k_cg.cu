@@ -512,19 +512,23 @@ void launch_cg_init(const Lattice & L, const BrickArrays & B, const NodeArrays &
                                                                  N.r, N.d, cg->sums, partials, &cg->ticket[0]);
     k_cg_start<<<1, 32, 0, st>>>(cg, cg->sums, nullptr, nullptr, 0, tol, max_iterations, nv);
 }
-// Both candidates' residuals (prediction in N.x -> N.r, N.d; base xb -> rb), the
-// start state keeping the better one, and the base copied in when it wins.
+// Residual of one candidate start x: r = b - A x into r (and d when non-null),
+// |r|^2 and |b|^2 into sums[0..1] (u = V x staged in N.u).
 template<int DIM>
-void launch_cg_init_pick(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
-                         const float * xb, float * rb, const int * mlp_err, bool keep_prediction, CgState * cg,
-                         double * partials, double tol, int max_iterations, const int * nv, int sgrid, int ugrid,
-                         cudaStream_t st) {
-    k_vmul<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N.V, N.x, N.u);
-    k_rows_tiled<DIM, kRowsResid><<<sgrid, KG<DIM>::BT, 0, st>>>(L, Phys{}, B.list, B.count, B.flag, N, S, N.u, N.x,
-                                                                 N.r, N.d, cg->sums, partials, &cg->ticket[0]);
-    k_vmul<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N.V, xb, N.u);
-    k_rows_tiled<DIM, kRowsResid><<<sgrid, KG<DIM>::BT, 0, st>>>(L, Phys{}, B.list, B.count, B.flag, N, S, N.u, xb, rb,
-                                                                 nullptr, cg->sums + 2, partials, &cg->ticket[0]);
+void launch_cg_residual(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
+                        const float * x, float * r, float * d, double * sums, CgState * cg, double * partials,
+                        int sgrid, int ugrid, cudaStream_t st) {
+    k_vmul<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N.V, x, N.u);
+    k_rows_tiled<DIM, kRowsResid><<<sgrid, KG<DIM>::BT, 0, st>>>(L, Phys{}, B.list, B.count, B.flag, N, S, N.u, x, r, d,
+                                                                 sums, partials, &cg->ticket[0]);
+}
+// Start state keeping the better of the prediction (residual in cg->sums[0..1],
+// already in N.x / N.r / N.d) and the base start xb (cg->sums[2..3], residual rb),
+// and the base copied in when it wins.
+template<int DIM>
+void launch_cg_pick(const BrickArrays & B, const NodeArrays & N, const float * xb, const float * rb,
+                    const int * mlp_err, bool keep_prediction, CgState * cg, double tol, int max_iterations,
+                    const int * nv, int ugrid, cudaStream_t st) {
     k_cg_start<<<1, 32, 0, st>>>(cg, cg->sums, cg->sums + 2, mlp_err, keep_prediction ? 1 : 0, tol, max_iterations, nv);
     k_cg_pick_base<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N, xb, rb, cg);
 }
@@ -594,9 +598,11 @@ void launch_rhs_norm(const BrickArrays & B, const NodeArrays & N, CgState * cg, 
                                            const float *, float *, int, cudaStream_t);                                 \
     template void launch_cg_init<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,         \
                                     CgState *, double *, double, int, const int *, int, int, cudaStream_t);            \
-    template void launch_cg_init_pick<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,    \
-                                         const float *, float *, const int *, bool, CgState *, double *, double, int,  \
-                                         const int *, int, int, cudaStream_t);                                         \
+    template void launch_cg_residual<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,     \
+                                        const float *, float *, float *, double *, CgState *, double *, int, int,      \
+                                        cudaStream_t);                                                                 \
+    template void launch_cg_pick<D>(const BrickArrays &, const NodeArrays &, const float *, const float *, const int *, \
+                                    bool, CgState *, double, int, const int *, int, cudaStream_t);                     \
     template void launch_cg_spmv<D>(const Lattice &, const BrickArrays &, const NodeArrays &, const Stencil &,         \
                                     CgState *, double *, int, cudaStream_t);                                           \
     template void launch_cg_update<D>(const BrickArrays &, const NodeArrays &, CgState *, double *, int, cudaStream_t); \

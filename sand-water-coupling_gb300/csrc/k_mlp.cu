@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
                   const float * __restrict__ feat, float * __restrict__ out, float * __restrict__ z1s,
                   float * __restrict__ h1s, float * __restrict__ z2s, NodeArrays N, const int * __restrict__ blist,
                   const int * __restrict__ bcount, int bn_log2, const int * __restrict__ nv,
-                  const CgState * __restrict__ cg, FeatScale F0, int * __restrict__ err) {
+                  const double * __restrict__ bb, FeatScale F0, int * __restrict__ err) {
     __shared__ __align__(1024) uint8_t sw1[kMlpH * 16 * 2];   // W1/2 [64 x 16] bf16 (K padded to 16)
     __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpH * 2];  // W2/2 [64 x 64]
     __shared__ __align__(1024) uint8_t sh[kMlpNT * kMlpH * 2];  // H1 [128 x 64]; X [128 x 16] in its first 4 KB
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
         rows = (long long) *bcount << bn_log2;
         // sD = RMS of the right-hand side over active nodes
         const int na    = *nv;
-        const double sD = na > 0 ? sqrt(cg->bb / double(na)) : 1.0;
+        const double sD = na > 0 ? sqrt(*bb / double(na)) : 1.0;
         F.inv_sD        = sD > 0 ? float(1.0 / sD) : 0.f;
     }
     uint32_t phase = 0;
@@ -643,13 +643,13 @@ static int num_sms_cached() {
 template<int MODE, bool SAVE>
 static void launch_forward(long long rows_max, const float * params, const float * norm, const float * feat,
                            float * out, float * z1s, float * h1s, float * z2s, const NodeArrays & N,
-                           const int * blist, const int * bcount, int bn_log2, const int * nv, const CgState * cg,
+                           const int * blist, const int * bcount, int bn_log2, const int * nv, const double * bb,
                            const FeatScale & F, int * err, cudaStream_t st) {
     const MlpLaunch s     = mlp_launch_shape<MODE, SAVE>();
     const long long tiles = std::max<long long>(1, (rows_max + kMlpNT - 1) / kMlpNT);
     const int grid        = int(std::min<long long>(tiles, (long long) s.per_sm * num_sms_cached()));
     k_mlp_forward<MODE, SAVE><<<grid, kMlpNT, s.dyn, st>>>(rows_max, params, norm, feat, out, z1s, h1s, z2s, N,
-                                                           blist, bcount, bn_log2, nv, cg, F, err);
+                                                           blist, bcount, bn_log2, nv, bb, F, err);
 }
 void launch_mlp_forward_array(long long n, const float * params, const float * norm, const float * feat, float * out,
                               float * z1s, float * h1s, float * z2s, int * err, cudaStream_t st) {
@@ -662,11 +662,11 @@ void launch_mlp_forward_array(long long n, const float * params, const float * n
                                              nullptr, nullptr, 0, nullptr, nullptr, FeatScale{}, err, st);
 }
 void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const BrickArrays & B,
-                              int bn_log2, long long slots_max, const CgState * cg, float inv_alpha0, float inv_rho0,
+                              int bn_log2, long long slots_max, const double * bb, float inv_alpha0, float inv_rho0,
                               float inv_nreal, int * err, cudaStream_t st) {
     FeatScale F{0.f, inv_alpha0, inv_rho0, inv_nreal};
     launch_forward<kMlpFromNodes, false>(slots_max, params, norm, nullptr, nullptr, nullptr, nullptr, nullptr, N, B.list,
-                                         B.count, bn_log2, B.seg_off + B.nseg, cg, F, err, st);
+                                         B.count, bn_log2, B.seg_off + B.nseg, bb, F, err, st);
 }
 void launch_mlp_backward(long long n, const float * params, const float * norm, const float * feat,
                          const float * pred, const float * target, const float * z1s, const float * h1s,

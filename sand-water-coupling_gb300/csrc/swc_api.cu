@@ -428,26 +428,37 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
         launch_warm_start<DIM>(c->L, c->B, c->N, kWarmExtrap, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream,
                                history);
         const bool no_fallback = learned && c->opts.learned_no_fallback && !logging;
+        const bool pick        = learned && !no_fallback;
         if (!no_fallback)
             CK(cudaMemcpyAsync(c->xprev, c->N.x, sizeof(float) * slots, cudaMemcpyDeviceToDevice, c->stream));
         if (logging) launch_slot_of<DIM>(c->L, c->B, c->N, c->slot_of, c->grid, c->stream);
-        launch_rhs_norm<DIM>(c->B, c->N, c->cg, c->partials, c->grid, c->stream);  // |b|^2 for sD
+        // |b|^2 for sD: from the base start's residual pass when the residual test
+        // needs that pass anyway, else a reduction of its own
+        const double * bb = &c->cg->bb;
+        if (pick) {
+            launch_cg_residual<DIM>(c->L, c->B, c->N, c->S, c->N.x, c->N.q, nullptr, c->cg->sums + 2, c->cg, c->partials,
+                                    c->sgrid, c->grid, c->stream);
+            bb = c->cg->sums + 3;
+        }
+        if (!pick || logging) launch_rhs_norm<DIM>(c->B, c->N, c->cg, c->partials, c->grid, c->stream);
         const float inv_a0 = float(1.0 / c->alpha0), inv_r0 = float(1.0 / c->rho0), inv_nr = 1.f / 32.f;
         if (logging)
             launch_node_features(c->N, c->slot_of, nv, c->L.ncells, c->cg, inv_a0, inv_r0, inv_nr, c->feat_buf,
                                  c->stream);
         if (learned) {
-            launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->B, DIM == 3 ? 9 : 8, (long long) slots, c->cg,
+            launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->B, DIM == 3 ? 9 : 8, (long long) slots, bb,
                                      inv_a0, inv_r0, inv_nr, c->mlp_err, c->stream);
             CK(cudaMemcpyAsync(&c->hcg->mlp_err, c->mlp_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
             mlp_checked = true;  // the error flag is read with CG's first check
             if (no_fallback) {
                 used = SWC_WARM_LEARNED;  // CG initialises from the prediction
             } else {
-                // residual test on the device: both starts' residuals, the smaller kept
-                launch_cg_init_pick<DIM>(c->L, c->B, c->N, c->S, c->xprev, c->N.q, c->mlp_err, false, c->cg,
-                                         c->partials, c->opts.tolerance, c->opts.max_iterations, nv, c->sgrid,
-                                         c->grid, c->stream);
+                // residual test on the device: the prediction's residual against the
+                // base start's (computed above), the smaller kept
+                launch_cg_residual<DIM>(c->L, c->B, c->N, c->S, c->N.x, c->N.r, c->N.d, c->cg->sums, c->cg,
+                                        c->partials, c->sgrid, c->grid, c->stream);
+                launch_cg_pick<DIM>(c->B, c->N, c->xprev, c->N.q, c->mlp_err, false, c->cg, c->opts.tolerance,
+                                    c->opts.max_iterations, nv, c->grid, c->stream);
                 init_mode = kInitDevice;
                 picked    = true;
             }
@@ -1276,7 +1287,7 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
     auto launch = [&]() {
         if (which == 7) {
             launch_mlp_forward_nodes(c->mlp_params, c->mlp_norm, c->N, c->B, c->dim == 3 ? 9 : 8, (long long) slots,
-                                     c->cg, float(1.0 / c->alpha0), float(1.0 / c->rho0), 1.f / 32.f, c->mlp_err,
+                                     &c->cg->bb, float(1.0 / c->alpha0), float(1.0 / c->rho0), 1.f / 32.f, c->mlp_err,
                                      c->stream);
             return;
         }

@@ -150,14 +150,19 @@ template<int DIM>
 void launch_cg_init(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
                     double * partials, double tol, int max_iterations, const int * nv, int sgrid, int ugrid,
                     cudaStream_t st);
-// CG start from the better of two candidates (x: prediction, xb: base start) by
-// their residuals, decided on the device (cg->start: 0 prediction, 1 base); rb is
-// scratch for the base's residual.  keep_prediction skips the comparison.
+// Residual r = b - A x of one candidate CG start (r, and d when non-null;
+// |r|^2, |b|^2 into sums[0..1]).
 template<int DIM>
-void launch_cg_init_pick(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
-                         const float * xb, float * rb, const int * mlp_err, bool keep_prediction, CgState * cg,
-                         double * partials, double tol, int max_iterations, const int * nv, int rgrid, int ugrid,
-                         cudaStream_t st);
+void launch_cg_residual(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
+                        const float * x, float * r, float * d, double * sums, CgState * cg, double * partials,
+                        int sgrid, int ugrid, cudaStream_t st);
+// CG start from the better of the prediction (N.x, residual sums in cg->sums[0..1])
+// and the base start xb (cg->sums[2..3], residual rb), decided on the device
+// (cg->start: 0 prediction, 1 base); keep_prediction skips the comparison.
+template<int DIM>
+void launch_cg_pick(const BrickArrays & B, const NodeArrays & N, const float * xb, const float * rb,
+                    const int * mlp_err, bool keep_prediction, CgState * cg, double tol, int max_iterations,
+                    const int * nv, int ugrid, cudaStream_t st);
 template<int DIM>
 void launch_cg_iteration(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
                          CgState * cg, double * partials, int sgrid, int ugrid, cudaStream_t st);
@@ -190,7 +195,7 @@ void launch_mlp_forward_array(long long n, const float * params, const float * n
 // node mode: every slot of the active bricks (inactive slots are skipped), the
 // active-node count at B.seg_off[B.nseg]
 void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const BrickArrays & B,
-                              int bn_log2, long long slots_max, const CgState * cg, float inv_alpha0, float inv_rho0,
+                              int bn_log2, long long slots_max, const double * bb, float inv_alpha0, float inv_rho0,
                               float inv_nreal, int * err, cudaStream_t st);
 void launch_node_features(const NodeArrays & N, const int * slot_of, const int * nv, long long rows_max,
                           const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal, float * feat_out,
