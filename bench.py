@@ -62,8 +62,10 @@ def peaks():
 SM_MAX_MHZ = 2070.0
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 128^3 block,
 # per active node of the captured launch: k_cg_spmv 32,769,792 B at 2,246,535 nodes,
-# k_node_gather 88,687,616 + 14,859,776 B at 2,246,538 nodes (profiles/)
-DRAM_BYTES_PER_NODE = {"cg_spmv": 32769792 / 2246535, "virtual_gather": (88687616 + 14859776) / 2246538}
+# k_node_gather 88,687,616 + 14,859,776 B and k_pressure_gradient 111,554,816 + 10,510,336 B
+# at 2,246,538 nodes (profiles/)
+DRAM_BYTES_PER_NODE = {"cg_spmv": 32769792 / 2246535, "virtual_gather": (88687616 + 14859776) / 2246538,
+                       "pressure_gradient": (111554816 + 10510336) / 2246538}
 
 
 class ClockSampler:

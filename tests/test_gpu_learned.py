@@ -172,3 +172,30 @@ def test_committed_model_without_fallback(swc_mod):
     v_node, v_learn = out["node"][0], out["learned"][0]
     assert np.linalg.norm(v_learn - v_node) / np.linalg.norm(v_node) < 1e-4
     print(f"\nCG iterations  node-mapped: {out['node'][1]}  learned (kept): {out['learned'][1]}")
+
+
+def test_learned_start_with_feature_logging(swc_mod):
+    """Learned start and training-data logging together (the residual test's base
+    pass and the logging reduction both run): same solution as the node-mapped
+    start, features logged every step."""
+    import os
+
+    from swc import learn
+
+    path = os.path.join(os.path.dirname(learn.__file__), "models", "warm_start.npz")
+    sc = scenes.projection_block_3d(n=20, seed=21).rounded_to_float32()
+    vel = {}
+    for mode in ("node", "learned"):
+        liq = swc_mod.DualParticleSphLiquid(sc, warm_start=mode, keep_features=(mode == "learned"))
+        if mode == "learned":
+            liq.setMlp(*learn.load_model(path))
+        liq.initialize()
+        for _ in range(5):
+            st = liq.advance(sc.dt)
+            assert st["status"] == 0
+            if mode == "learned":
+                f, t = liq.features()
+                assert f.shape == (liq.numVirtual(), learn.N_IN) and np.all(np.isfinite(f)) and np.all(np.isfinite(t))
+        vel[mode] = liq.getParticles()[1]
+        liq.close()
+    assert np.linalg.norm(vel["learned"] - vel["node"]) / np.linalg.norm(vel["node"]) < 1e-4
