@@ -13,10 +13,11 @@ host->device copy of each step's particle state and the device->host read of
 its result inside the timed region.  The headline form is the learned warm
 start (the trained model in swc/models/: a per-node correction of the
 pressure extrapolated in time, kept when it starts CG from a smaller residual
-than the extrapolation itself); ``forms`` reports plain CG from the
-node-mapped previous pressure, from the reference's stale prefix and from
-zero, the extrapolated start alone and the learned start without the
-residual test, all on the same scene and steps.
+than the extrapolation itself, the network skipped for 8 steps after 2
+consecutive rejections); ``forms`` reports plain CG from the node-mapped
+previous pressure, from the reference's stale prefix and from zero, the
+extrapolated start alone, the learned start evaluated every step and the
+learned start without the residual test, all on the same scene and steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl swc|reference]
 
@@ -48,6 +49,9 @@ UNIT = "steps/s"
 # learned warm start trained by swc/train_warm_start.py (dam-break variants + blocks, seeds
 # disjoint from the benchmark block's)
 MODEL = os.path.join(ROOT, "sand-water-coupling_gb300", "swc", "models", "warm_start.npz")
+# the headline learned form skips the network for 8 steps after 2 consecutive
+# rejections by the residual test (learned_always evaluates it every step)
+LEARNED_GATE = 2
 
 
 def peaks():
@@ -217,8 +221,10 @@ def run_gpu_arm(args):
 
     def make(warm):
         no_fallback = warm == "learned_no_fallback"
-        mode = "learned" if no_fallback else warm
-        liq = swc.DualParticleSphLiquid(scene, warm_start=mode, tolerance=1e-5, learned_no_fallback=no_fallback)
+        mode = "learned" if warm.startswith("learned") else warm
+        gate = LEARNED_GATE if warm == "learned" else 0
+        liq = swc.DualParticleSphLiquid(scene, warm_start=mode, tolerance=1e-5, learned_no_fallback=no_fallback,
+                                        learned_gate=gate)
         if mode == "learned":
             liq.setMlp(*learn.load_model(MODEL))
         liq.setStream(stream.cuda_stream)
@@ -348,7 +354,7 @@ def run_gpu_arm(args):
     # plain-CG comparison forms (same scene, same steps)
     forms = {}
     if args.compare_forms:
-        cands = ["prefix", "node", "zero", "extrapolate"] + (["learned", "learned_no_fallback"]
+        cands = ["prefix", "node", "zero", "extrapolate"] + (["learned", "learned_always", "learned_no_fallback"]
                                                              if os.path.exists(MODEL) else [])
         for warm in cands:
             if warm == args.warm_start:
@@ -403,9 +409,10 @@ def main():
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--warm-start", dest="warm_start", default="auto",
-                    choices=["auto", "prefix", "node", "zero", "extrapolate", "learned", "learned_no_fallback"],
-                    help="auto: the learned start (prediction always kept) when the trained model is "
-                         "present, else the node-mapped previous pressure")
+                    choices=["auto", "prefix", "node", "zero", "extrapolate", "learned", "learned_always",
+                             "learned_no_fallback"],
+                    help="auto: the learned start (residual test, gated) when the trained model is present, "
+                         "else the node-mapped previous pressure")
     ap.add_argument("--cpu-sample", dest="cpu_sample", type=int, default=48)
     ap.add_argument("--cpu-steps", dest="cpu_steps", type=int, default=3)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")

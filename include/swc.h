@@ -79,8 +79,11 @@ typedef struct swc_solver_opts {
     int32_t compute_true_residual; /* evaluate |b - A x| / |b| after each solve */
     int32_t keep_features;         /* keep per-node neighbour counts (learned warm start) */
     int32_t learned_no_fallback;   /* learned start: keep the prediction even when its initial
-                                      residual exceeds the node-mapped start's (evaluation) */
-    int32_t reserved[1];
+                                      residual exceeds the base start's (evaluation) */
+    int32_t learned_gate;          /* learned start with the residual test: after this many
+                                      consecutive rejections of the prediction, skip the network
+                                      (base start) for 4 * learned_gate advance steps, then test
+                                      it again; 0: evaluate the network every step */
 } swc_solver_opts;
 
 typedef struct swc_stats {

@@ -93,6 +93,9 @@ struct swc_ctx {
     // (N.xm1, flags two steps back) is valid, and whether this step shifted the flags
     int     extrap_steps   = 0;
     bool    extrap_shifted = false;
+    // learned-start gate: consecutive rejections by the residual test, steps left to skip
+    int     gate_rejects = 0;
+    int     gate_skip    = 0;
     float *     pcomp = nullptr;    // last solution in reference order (prefix warm start)
     int *       nv_prev = nullptr;
     bool        pcomp_stale = false;  // the last projection did not export pcomp (other warm-start modes)
@@ -408,7 +411,11 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     run_generate<DIM>(c, true);
     mark(c, 4);
     const int mode     = c->opts.warm_start;
-    const bool learned = mode == SWC_WARM_LEARNED && c->mlp_ready;
+    // the gate skips the network (base start) while it keeps losing the residual test
+    const bool gated   = mode == SWC_WARM_LEARNED && c->mlp_ready && c->opts.learned_gate > 0 &&
+                       !c->opts.learned_no_fallback && c->gate_skip > 0;
+    if (gated) c->gate_skip--;
+    const bool learned = mode == SWC_WARM_LEARNED && c->mlp_ready && !gated;
     const bool logging = c->opts.keep_features != 0 && c->feat_buf;
     const int * nv     = c->B.seg_off + c->B.nseg;
     const size_t slots = size_t(c->L.nbricks) * BrickGeom<DIM>::BN;
@@ -477,7 +484,16 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     }
     mark(c, 5);
     int rc = run_cg<DIM>(c, st, init_mode);
-    if (picked) used = c->hcg->st.start == 0 ? SWC_WARM_LEARNED : base_used;
+    if (picked) {
+        used = c->hcg->st.start == 0 ? SWC_WARM_LEARNED : base_used;
+        if (c->opts.learned_gate > 0) {
+            c->gate_rejects = used == SWC_WARM_LEARNED ? 0 : c->gate_rejects + 1;
+            if (c->gate_rejects >= c->opts.learned_gate) {
+                c->gate_skip    = 4 * c->opts.learned_gate;
+                c->gate_rejects = 0;
+            }
+        }
+    }
     if (mlp_checked && c->hcg->mlp_err) {
         c->err = picked ? "learned warm start: the tensor-core pass timed out; CG ran from the base start"
                         : "learned warm start: the tensor-core pass timed out; CG ran from its output";
@@ -627,6 +643,7 @@ template<int DIM> int do_initialize(swc_ctx * c) {
     // no previous pressure: empty prefix, no extrapolation history
     c->extrap_steps = 0;
     c->pcomp_stale  = false;
+    c->gate_rejects = c->gate_skip = 0;
     CK(cudaMemsetAsync(c->nv_prev, 0, sizeof(int), c->stream));
     CK(cudaMemsetAsync(c->N.x, 0, sizeof(float) * size_t(c->L.nbricks) * (DIM == 3 ? 512 : 256), c->stream));
     CK(cudaMemsetAsync(c->N.flag, 0, size_t(c->L.nbricks) * (DIM == 3 ? 512 : 256), c->stream));
@@ -876,7 +893,8 @@ int swc_set_solver_opts(swc_ctx * c, const swc_solver_opts * o) {
     }
     const bool need_vbar = o->keep_virtual_velocity && !c->N.vbar;
     const bool need_feat = o->keep_features && !c->N.nreal;
-    c->opts = *o;
+    c->opts         = *o;
+    c->gate_rejects = c->gate_skip = 0;
     const size_t slots = size_t(c->L.nbricks) * (c->dim == 3 ? 512 : 256);
     int rc;
     if (need_vbar || need_feat) {

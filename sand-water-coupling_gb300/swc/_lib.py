@@ -58,7 +58,7 @@ class SolverOpts(C.Structure):
         ("compute_true_residual", C.c_int32),
         ("keep_features", C.c_int32),
         ("learned_no_fallback", C.c_int32),
-        ("reserved", C.c_int32 * 1),
+        ("learned_gate", C.c_int32),
     ]
 
 

@@ -42,7 +42,7 @@ def _f64(a, shape=None):
 class DualParticleSphLiquid:
     def __init__(self, scene, tolerance=None, max_iterations=-1, warm_start="prefix", keep_virtual_velocity=False,
                  compute_true_residual=False, keep_features=False, check_interval=0, raise_on_nonconvergence=False,
-                 learned_no_fallback=False):
+                 learned_no_fallback=False, learned_gate=0):
         self.L = _lib.load()
         self.scene = scene
         self.dim = scene.dim
@@ -70,6 +70,7 @@ class DualParticleSphLiquid:
         o.compute_true_residual = 1 if compute_true_residual else 0
         o.keep_features = 1 if keep_features else 0
         o.learned_no_fallback = 1 if learned_no_fallback else 0
+        o.learned_gate = int(learned_gate)
         self._opts = o
         self._scene_c = s
         h = C.c_void_p()

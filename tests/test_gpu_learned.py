@@ -199,3 +199,42 @@ def test_learned_start_with_feature_logging(swc_mod):
         vel[mode] = liq.getParticles()[1]
         liq.close()
     assert np.linalg.norm(vel["learned"] - vel["node"]) / np.linalg.norm(vel["node"]) < 1e-4
+
+
+def test_learned_gate(swc_mod):
+    """learned_gate: after that many consecutive rejections by the residual test the
+    network is skipped (base start) for 4 x gate steps; the solution stays the
+    extrapolated start's to the CG tolerance and skipped steps report the base."""
+    import os
+
+    from swc import learn
+
+    path = os.path.join(os.path.dirname(learn.__file__), "models", "warm_start.npz")
+    sc = scenes.projection_block_3d(n=20, seed=8).rounded_to_float32()
+    out = {}
+    for mode, gate in (("extrapolate", 0), ("learned", 1)):
+        liq = swc_mod.DualParticleSphLiquid(sc, warm_start=mode, learned_gate=gate)
+        if mode == "learned":
+            liq.setMlp(*learn.load_model(path))
+        liq.initialize()
+        used = []
+        for _ in range(16):
+            st = liq.advance(sc.dt)
+            assert st["status"] == 0
+            used.append(st["warm_start_used"])
+        out[mode] = (liq.getParticles()[1], used)
+        liq.close()
+    used = out["learned"][1]
+    assert np.linalg.norm(out["learned"][0] - out["extrapolate"][0]) / np.linalg.norm(out["extrapolate"][0]) < 1e-4
+    # replay the gate on the reported starts: no learned start inside a skip window
+    skip = rejects = windows = 0
+    for u in used:
+        if skip > 0:
+            assert u != 3, used
+            skip -= 1
+            continue
+        rejects = 0 if u == 3 else rejects + 1
+        if rejects >= 1:
+            skip, rejects, windows = 4, 0, windows + 1
+    assert windows >= 1 and 3 in used, used
+    print(f"\nwarm start used with learned_gate=1: {used}")
