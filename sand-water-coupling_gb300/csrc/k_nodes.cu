@@ -348,19 +348,47 @@ __global__ void __launch_bounds__(kNT) k_warm_start(Lattice L, const int * __res
                     v = given[s];
                 }
             }
-            if (mode == kWarmExtrap) {
-                const bool a1  = B.flag_prev[b] && N.flag_prev[s];
-                const bool a2  = a1 && history >= 1 && B.flag_m2[b] && N.flag_m2[s];
-                const bool a3  = a2 && history >= 2 && B.flag_m3[b] && N.flag_m3[s];
-                const float p1 = a1 ? N.x[s] : 0.f, p2 = a2 ? N.xm1[s] : 0.f, p3 = a3 ? N.xm2[s] : 0.f;
-                const float d1 = a2 ? p1 - p2 : 0.f, d2 = a3 ? (p1 - 2.f * p2) + p3 : 0.f;
-                if (N.flag[s]) v = (p1 + d1) + d2;
-                if (N.d2p) N.d2p[s] = d2;
-                N.xm2[s] = p2;
-                N.xm1[s] = p1;
-            }
             N.x[s] = v;
         }
+    }
+}
+
+// History mode (extrap above) as a 16-byte streaming pass over the slots of the
+// active bricks.
+template<int DIM>
+__global__ void __launch_bounds__(kNT) k_warm_history(const int * __restrict__ blist, const int * __restrict__ bcount,
+                                                      BrickArrays B, NodeArrays N, int history) {
+    using G = BrickGeom<DIM>;
+    constexpr int Q = G::BN / 4;
+    const long long total = (long long) (*bcount) * Q;
+    for (long long e = blockIdx.x * (long long) kNT + threadIdx.x; e < total; e += (long long) gridDim.x * kNT) {
+        const int b       = blist[e / Q];
+        const long long s = (long long) b * G::BN + 4 * (e % Q);
+        const bool b1 = B.flag_prev[b] != 0, b2 = history >= 1 && B.flag_m2[b], b3 = history >= 2 && B.flag_m3[b];
+        const uchar4 f = *reinterpret_cast<const uchar4 *>(N.flag + s);
+        const uchar4 f1 = *reinterpret_cast<const uchar4 *>(N.flag_prev + s);
+        const uchar4 f2 = *reinterpret_cast<const uchar4 *>(N.flag_m2 + s);
+        const uchar4 f3 = *reinterpret_cast<const uchar4 *>(N.flag_m3 + s);
+        const float4 x = *reinterpret_cast<const float4 *>(N.x + s), x1 = *reinterpret_cast<const float4 *>(N.xm1 + s),
+                     x2 = *reinterpret_cast<const float4 *>(N.xm2 + s);
+        float v[4], p1[4], p2[4], d2[4];
+        const unsigned char fa[4] = {f.x, f.y, f.z, f.w}, fb[4] = {f1.x, f1.y, f1.z, f1.w},
+                            fc[4] = {f2.x, f2.y, f2.z, f2.w}, fd[4] = {f3.x, f3.y, f3.z, f3.w};
+        const float xa[4] = {x.x, x.y, x.z, x.w}, xb[4] = {x1.x, x1.y, x1.z, x1.w}, xc[4] = {x2.x, x2.y, x2.z, x2.w};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const bool a1 = b1 && fb[k], a2 = a1 && b2 && fc[k], a3 = a2 && b3 && fd[k];
+            p1[k] = a1 ? xa[k] : 0.f;
+            p2[k] = a2 ? xb[k] : 0.f;
+            const float p3 = a3 ? xc[k] : 0.f;
+            const float d1 = a2 ? p1[k] - p2[k] : 0.f;
+            d2[k] = a3 ? (p1[k] - 2.f * p2[k]) + p3 : 0.f;
+            v[k]  = fa[k] ? (p1[k] + d1) + d2[k] : 0.f;
+        }
+        *reinterpret_cast<float4 *>(N.x + s)   = make_float4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<float4 *>(N.xm1 + s) = make_float4(p1[0], p1[1], p1[2], p1[3]);
+        *reinterpret_cast<float4 *>(N.xm2 + s) = make_float4(p2[0], p2[1], p2[2], p2[3]);
+        if (N.d2p) *reinterpret_cast<float4 *>(N.d2p + s) = make_float4(d2[0], d2[1], d2[2], d2[3]);
     }
 }
 
@@ -725,6 +753,13 @@ void launch_diag_max_f64(const Lattice & L, const BrickArrays & B, const NodeArr
 template<int DIM>
 void launch_warm_start(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int mode, const float * pcomp,
                        const int * nv_prev, const float * given, int grid, cudaStream_t st, int history) {
+    if (mode == kWarmExtrap) {
+        // streaming grid: the slots of the active bricks, 4 per thread
+        const long long q = (long long) L.nbricks * (BrickGeom<DIM>::BN / 4);
+        k_warm_history<DIM><<<int(std::min<long long>((q + kNT - 1) / kNT, 152LL * 8)), kNT, 0, st>>>(B.list, B.count, B,
+                                                                                                    N, history);
+        return;
+    }
     k_warm_start<DIM><<<grid, kNT, 0, st>>>(L, B.list, B.count, B.seg_off, B, N, mode, history, pcomp, nv_prev,
                                             given);
 }
