@@ -61,27 +61,25 @@ __global__ void k_export_ratio(const float * __restrict__ a, int stride, int com
         out[id[s]] = double(num) / double(a[s * stride + comp]);
 }
 
-// x += v dt  (SmthParticleHydrodLiquid::moveParticles, Cores/Physics/SmthParticleHydrodLiquid.cpp:72-76).
-__global__ void k_advect(float4 * __restrict__ pos, const float4 * __restrict__ vel, long long n, float dt) {
-    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
-        float4 p = pos[i];
-        const float4 u = vel[i];
-        p.x = fmaf(u.x, dt, p.x);
-        p.y = fmaf(u.y, dt, p.y);
-        p.z = fmaf(u.z, dt, p.z);
-        pos[i] = p;
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Counting sort into cells.  Order within a cell is made deterministic by an
 // insertion sort on the original id, so the final order is (cell, id).
 // ---------------------------------------------------------------------------
+// With vel non-null the particles are first moved, x += v dt
+// (SmthParticleHydrodLiquid::moveParticles, Cores/Physics/SmthParticleHydrodLiquid.cpp:72-76,
+// fused into the pass that reads them anyway).
 template<int DIM>
-__global__ void k_cell_count(const float4 * __restrict__ pos, long long n, Lattice L, int * __restrict__ key,
-                             int * __restrict__ rank, int * __restrict__ count) {
+__global__ void k_cell_count(float4 * __restrict__ pos, const float4 * __restrict__ vel, float dt, long long n,
+                             Lattice L, int * __restrict__ key, int * __restrict__ rank, int * __restrict__ count) {
     for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
-        const float4 p = pos[i];
+        float4 p = pos[i];
+        if (vel) {
+            const float4 u = vel[i];
+            p.x    = fmaf(u.x, dt, p.x);
+            p.y    = fmaf(u.y, dt, p.y);
+            p.z    = fmaf(u.z, dt, p.z);
+            pos[i] = p;
+        }
         const int3 c   = cell_of<DIM>(L, p.x, p.y, p.z);
         const int k    = int(cell_linear(L, c));
         key[i]         = k;
@@ -644,9 +642,6 @@ void launch_export_ratio(const float * a, int stride, int comp, float num, const
                          cudaStream_t st) {
     if (n > 0) k_export_ratio<<<grid_for(n, 256), 256, 0, st>>>(a, stride, comp, num, id, n, out);
 }
-void launch_advect(float4 * pos, const float4 * vel, long long n, float dt, cudaStream_t st) {
-    if (n > 0) k_advect<<<grid_for(n, 256), 256, 0, st>>>(pos, vel, n, dt);
-}
 
 void launch_scan(const int * in, long long n, int * out, int * tile_buf, cudaStream_t st) {
     const long long ntiles = (n + kScanTile - 1) / kScanTile;
@@ -662,9 +657,11 @@ long long scan_tile_count(long long n) { return (n + kScanTile - 1) / kScanTile 
 
 template<int DIM>
 void launch_bin(const Lattice & L, long long n, float4 *& pos, float4 *& vel, float4 *& aux, int *& id,
-                SortScratch & S, int * cellStart, cudaStream_t st) {
+                SortScratch & S, int * cellStart, float advect_dt, cudaStream_t st) {
     cudaMemsetAsync(S.count, 0, sizeof(int) * L.ncells, st);
-    if (n > 0) k_cell_count<DIM><<<grid_for(n, 256), 256, 0, st>>>(pos, n, L, S.key, S.rank, S.count);
+    if (n > 0)
+        k_cell_count<DIM><<<grid_for(n, 256), 256, 0, st>>>(pos, advect_dt != 0.f ? vel : nullptr, advect_dt, n, L,
+                                                            S.key, S.rank, S.count);
     launch_scan(S.count, L.ncells, cellStart, S.tiles, st);
     if (n == 0) return;
     k_cell_scatter<<<grid_for(n, 256), 256, 0, st>>>(S.key, S.rank, cellStart, n, S.perm);
@@ -749,7 +746,7 @@ void launch_debug_neighbors(int which, long long nq, const double * q, const Lat
 
 #define SWC_INST(D)                                                                                                    \
     template void launch_bin<D>(const Lattice &, long long, float4 *&, float4 *&, float4 *&, int *&, SortScratch &,   \
-                                int *, cudaStream_t);                                                                  \
+                                int *, float, cudaStream_t);                                                           \
     template void launch_density<D>(const float4 *, float4 *, float *, long long, const Lattice &, const Phys &,       \
                                     const int *, int *, cudaStream_t);                                                 \
     template void launch_forces<D>(const float4 *, const float4 *, float4 *, long long, const Lattice &, const Phys &,  \

@@ -274,13 +274,14 @@ void setup_phys(swc_ctx * c) {
     }
 }
 
-template<int DIM> int run_bin_real(swc_ctx * c) {
+// advect_dt != 0: the particles move by v dt first (advection fused into the count pass)
+template<int DIM> int run_bin_real(swc_ctx * c, float advect_dt = 0.f) {
     float4 * no_aux = nullptr;
-    launch_bin<DIM>(c->L, c->n, c->pos, c->vel, no_aux, c->id, c->sortR, c->cellStart, c->stream);
+    launch_bin<DIM>(c->L, c->n, c->pos, c->vel, no_aux, c->id, c->sortR, c->cellStart, advect_dt, c->stream);
     return SWC_OK;
 }
 template<int DIM> int run_bin_boundary(swc_ctx * c) {
-    launch_bin<DIM>(c->L, c->nb, c->bpos, c->bvel, c->bnrm, c->bid, c->sortB, c->bcellStart, c->stream);
+    launch_bin<DIM>(c->L, c->nb, c->bpos, c->bvel, c->bnrm, c->bid, c->sortB, c->bcellStart, 0.f, c->stream);
     launch_mark_bricks<DIM>(c->bcellStart, c->nb, c->L, c->P, c->bnear, nullptr, c->stream);
     return SWC_OK;
 }
@@ -344,7 +345,9 @@ template<int DIM> int run_cg(swc_ctx * c, swc_stats * st, int init_mode) {
         c->hcg->st.iter     = 0;
         c->hcg->st.max_iter = c->opts.max_iterations >= 0 ? c->opts.max_iterations : std::numeric_limits<int>::max();
     }
-    int first   = c->opts.check_interval > 0 ? c->opts.check_interval : std::max(4, c->last_iters);
+    // first batch: the last solve's count and one more (one convergence check in
+    // the common case; the iteration kernels are no-ops past convergence)
+    int first   = c->opts.check_interval > 0 ? c->opts.check_interval : std::max(4, c->last_iters + 1);
     bool counts = init_mode == kInitHost;
     while (!c->hcg->st.done) {
         const int room = c->hcg->st.max_iter - c->hcg->st.iter;
@@ -558,7 +561,6 @@ template<int DIM> int do_advance(swc_ctx * c, double dt, swc_stats * st, bool mo
     mark(c, 0);
     save_prev_flags(c, move);
     if (move) {
-        launch_advect(c->pos, c->vel, c->n, float(dt), c->stream);
         if (c->has_motion && c->nb > 0) {
             launch_rotate_boundary(c->bpos, c->bvel, c->bnrm, c->nb, float(c->motion_c[0]), float(c->motion_c[2]),
                                    float(c->motion_omega), float(dt), c->stream);
@@ -568,7 +570,7 @@ template<int DIM> int do_advance(swc_ctx * c, double dt, swc_stats * st, bool mo
         // moving solids: rebin the boundary (the motion flag travels in bnrm.w)
         run_bin_boundary<DIM>(c);
     }
-    run_bin_real<DIM>(c);
+    run_bin_real<DIM>(c, move ? float(dt) : 0.f);
     mark(c, 1);
     launch_density<DIM>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->pleft, c->stream);
     mark(c, 2);

@@ -66,7 +66,6 @@ void launch_export_scalar(const float * a, int stride, int comp, const int * id,
                           cudaStream_t st);
 void launch_export_ratio(const float * a, int stride, int comp, float num, const int * id, long long n, double * out,
                          cudaStream_t st);
-void launch_advect(float4 * pos, const float4 * vel, long long n, float dt, cudaStream_t st);
 void launch_scan(const int * in, long long n, int * out, int * tile_buf, cudaStream_t st);
 long long scan_tile_count(long long n);
 void launch_set_volume(float4 * pos, const float * rho, long long n, float mass, cudaStream_t st);
@@ -79,10 +78,11 @@ void launch_set_boundary_info(float4 * bpos, float4 * bvel, float * brho, const 
 void launch_set_moving(float4 * bnrm, const unsigned char * moving, const int * bid, long long nb, cudaStream_t st);
 void launch_max_positive(const float * a, long long n, int * out_bits, cudaStream_t st);
 // counting sort into cells; the sorted arrays are swapped in (pos, vel, aux, id
-// then point at what were the scratch targets)
+// then point at what were the scratch targets); advect_dt != 0 first moves the
+// particles by vel * advect_dt
 template<int DIM>
 void launch_bin(const Lattice & L, long long n, float4 *& pos, float4 *& vel, float4 *& aux, int *& id, SortScratch & S,
-                int * cellStart, cudaStream_t st);
+                int * cellStart, float advect_dt, cudaStream_t st);
 // Density and forces run one thread per pair of consecutive sorted particles;
 // `left` (n/2 + 3 ints, zeroed once at allocation) collects the pairs that are
 // not in one cell row for a second, single-particle pass.
