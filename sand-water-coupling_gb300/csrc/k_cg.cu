@@ -90,6 +90,7 @@ template<int DIM>
 __global__ void __launch_bounds__(kUT) k_cg_pick_base(const int * __restrict__ blist, const int * __restrict__ bcount,
                                                       NodeArrays N, const float * __restrict__ xb,
                                                       const float * __restrict__ rb, const CgState * __restrict__ cg) {
+    pdl_wait_and_release();
     using G = BrickGeom<DIM>;
     constexpr int Q = G::BN / 4;
     if (cg->start != 1) return;
@@ -258,6 +259,7 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_rows_tiled(Lattice L, Phys P, c
                                                             float * __restrict__ d_out, double * __restrict__ sums,
                                                             double * __restrict__ partials,
                                                             unsigned int * __restrict__ ticket) {
+    pdl_wait_and_release();
     using G = BrickGeom<DIM>;
     using T = SpmvTile<DIM>;
     constexpr int BT = KG<DIM>::BT;
@@ -332,6 +334,7 @@ template<int DIM>
 __global__ void __launch_bounds__(kUT) k_vmul(const int * __restrict__ blist, const int * __restrict__ bcount,
                                               const float * __restrict__ V, const float * __restrict__ x,
                                               float * __restrict__ u) {
+    pdl_wait_and_release();
     using G = BrickGeom<DIM>;
     constexpr int Q = G::BN / 4;
     const long long total = (long long) (*bcount) * Q;
@@ -350,6 +353,7 @@ __global__ void __launch_bounds__(kUT) k_vmul(const int * __restrict__ blist, co
 __global__ void k_cg_start(CgState * cg, const double * __restrict__ sums_l, const double * __restrict__ sums_b,
                            const int * __restrict__ mlp_err, int keep_prediction, double tol, int max_iterations,
                            const int * __restrict__ nv) {
+    pdl_wait_and_release();
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double srr_l = sums_l[0], sbb = sums_l[1];
     bool keep = true;
@@ -426,6 +430,7 @@ __global__ void __launch_bounds__(kUT) k_cg_update(const int * __restrict__ blis
 template<int DIM>
 __global__ void __launch_bounds__(kUT) k_rhs_norm(const int * __restrict__ blist, const int * __restrict__ bcount,
                                                   NodeArrays N, CgState * cg, double * __restrict__ partials) {
+    pdl_wait_and_release();
     using G = BrickGeom<DIM>;
     constexpr int Q = G::BN / 4;
     __shared__ double red[kUT / 32 + 1];
@@ -493,7 +498,7 @@ __global__ void __launch_bounds__(KG<DIM>::BT) k_true_residual(Lattice L, const 
 template<int DIM>
 void launch_ahat(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
                  int sgrid, cudaStream_t st) {
-    k_rows_tiled<DIM, kRowsAhat><<<sgrid, KG<DIM>::BT, 0, st>>>(L, P, B.list, B.count, B.flag, N, S, N.V, nullptr, nullptr,
+    launch_pdl(k_rows_tiled<DIM, kRowsAhat>, sgrid, KG<DIM>::BT, 0, st, L, P, B.list, B.count, B.flag, N, S, N.V, nullptr, nullptr,
                                                                 nullptr, nullptr, nullptr, nullptr);
 }
 template<int DIM>
@@ -507,10 +512,10 @@ template<int DIM>
 void launch_cg_init(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
                     double * partials, double tol, int max_iterations, const int * nv, int sgrid, int ugrid,
                     cudaStream_t st) {
-    k_vmul<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N.V, N.x, N.u);
-    k_rows_tiled<DIM, kRowsResid><<<sgrid, KG<DIM>::BT, 0, st>>>(L, Phys{}, B.list, B.count, B.flag, N, S, N.u, N.x,
+    launch_pdl(k_vmul<DIM>, ugrid, kUT, 0, st, B.list, B.count, N.V, N.x, N.u);
+    launch_pdl(k_rows_tiled<DIM, kRowsResid>, sgrid, KG<DIM>::BT, 0, st, L, Phys{}, B.list, B.count, B.flag, N, S, N.u, N.x,
                                                                  N.r, N.d, cg->sums, partials, &cg->ticket[0]);
-    k_cg_start<<<1, 32, 0, st>>>(cg, cg->sums, nullptr, nullptr, 0, tol, max_iterations, nv);
+    launch_pdl(k_cg_start, 1, 32, 0, st, cg, cg->sums, nullptr, nullptr, 0, tol, max_iterations, nv);
 }
 // Residual of one candidate start x: r = b - A x into r (and d when non-null),
 // |r|^2 and |b|^2 into sums[0..1] (u = V x staged in N.u).
@@ -518,8 +523,8 @@ template<int DIM>
 void launch_cg_residual(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
                         const float * x, float * r, float * d, double * sums, CgState * cg, double * partials,
                         int sgrid, int ugrid, cudaStream_t st) {
-    k_vmul<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N.V, x, N.u);
-    k_rows_tiled<DIM, kRowsResid><<<sgrid, KG<DIM>::BT, 0, st>>>(L, Phys{}, B.list, B.count, B.flag, N, S, N.u, x, r, d,
+    launch_pdl(k_vmul<DIM>, ugrid, kUT, 0, st, B.list, B.count, N.V, x, N.u);
+    launch_pdl(k_rows_tiled<DIM, kRowsResid>, sgrid, KG<DIM>::BT, 0, st, L, Phys{}, B.list, B.count, B.flag, N, S, N.u, x, r, d,
                                                                  sums, partials, &cg->ticket[0]);
 }
 // Start state keeping the better of the prediction (residual in cg->sums[0..1],
@@ -529,31 +534,13 @@ template<int DIM>
 void launch_cg_pick(const BrickArrays & B, const NodeArrays & N, const float * xb, const float * rb,
                     const int * mlp_err, bool keep_prediction, CgState * cg, double tol, int max_iterations,
                     const int * nv, int ugrid, cudaStream_t st) {
-    k_cg_start<<<1, 32, 0, st>>>(cg, cg->sums, cg->sums + 2, mlp_err, keep_prediction ? 1 : 0, tol, max_iterations, nv);
-    k_cg_pick_base<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N, xb, rb, cg);
+    launch_pdl(k_cg_start, 1, 32, 0, st, cg, cg->sums, cg->sums + 2, mlp_err, keep_prediction ? 1 : 0, tol, max_iterations, nv);
+    launch_pdl(k_cg_pick_base<DIM>, ugrid, kUT, 0, st, B.list, B.count, N, xb, rb, cg);
 }
-// Launch with programmatic stream serialization: the kernel's blocks may be
-// dispatched while the previous kernel on the stream drains; the kernel itself
-// waits (pdl_wait_and_release) before touching its inputs.
-template<class Kern, class... Args>
-static void launch_pdl(Kern kernel, int grid, int block, cudaStream_t st, Args... args) {
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim          = dim3(unsigned(grid));
-    cfg.blockDim         = dim3(unsigned(block));
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream           = st;
-    cudaLaunchAttribute at[1];
-    at[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs    = at;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kernel, args...);
-}
-
 template<int DIM>
 void launch_cg_spmv(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S, CgState * cg,
                     double * partials, int sgrid, cudaStream_t st) {
-    launch_pdl(k_cg_spmv<DIM>, sgrid, KG<DIM>::BT, st, L, (const int *) B.list, (const int *) B.count,
+    launch_pdl(k_cg_spmv<DIM>, sgrid, KG<DIM>::BT, 0, st, L, (const int *) B.list, (const int *) B.count,
                (const unsigned char *) B.flag, N, S, cg, partials);
 }
 template<int DIM> int cg_spmv_blocks_per_sm() {
@@ -567,11 +554,11 @@ template<int DIM> int cg_spmv_blocks_per_sm() {
 template<int DIM>
 void launch_cg_update(const BrickArrays & B, const NodeArrays & N, CgState * cg, double * partials, int ugrid,
                       cudaStream_t st) {
-    launch_pdl(k_cg_update<DIM>, ugrid, kUT, st, (const int *) B.list, (const int *) B.count, N, cg, partials);
+    launch_pdl(k_cg_update<DIM>, ugrid, kUT, 0, st, (const int *) B.list, (const int *) B.count, N, cg, partials);
 }
 template<int DIM>
 void launch_cg_direction(const BrickArrays & B, const NodeArrays & N, const CgState * cg, int ugrid, cudaStream_t st) {
-    launch_pdl(k_cg_direction<DIM>, ugrid, kUT, st, (const int *) B.list, (const int *) B.count, N, cg);
+    launch_pdl(k_cg_direction<DIM>, ugrid, kUT, 0, st, (const int *) B.list, (const int *) B.count, N, cg);
 }
 template<int DIM>
 void launch_cg_iteration(const Lattice & L, const BrickArrays & B, const NodeArrays & N, const Stencil & S,
@@ -588,7 +575,7 @@ void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeAr
 template<int DIM>
 void launch_rhs_norm(const BrickArrays & B, const NodeArrays & N, CgState * cg, double * partials, int ugrid,
                      cudaStream_t st) {
-    k_rhs_norm<DIM><<<ugrid, kUT, 0, st>>>(B.list, B.count, N, cg, partials);
+    launch_pdl(k_rhs_norm<DIM>, ugrid, kUT, 0, st, B.list, B.count, N, cg, partials);
 }
 
 #define SWC_INST(D)                                                                                                    \

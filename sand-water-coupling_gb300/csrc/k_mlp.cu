@@ -199,6 +199,7 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
                   float * __restrict__ h1s, float * __restrict__ z2s, NodeArrays N, const int * __restrict__ blist,
                   const int * __restrict__ bcount, int bn_log2, const int * __restrict__ nv,
                   const double * __restrict__ bb, FeatScale F0, int * __restrict__ err) {
+    pdl_wait_and_release();
     __shared__ __align__(1024) uint8_t sw1[kMlpH * 16 * 2];   // W1/2 [64 x 16] bf16 (K padded to 16)
     __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpH * 2];  // W2/2 [64 x 64]
     __shared__ __align__(1024) uint8_t sh[kMlpNT * kMlpH * 2];  // H1 [128 x 64]; X [128 x 16] in its first 4 KB
@@ -648,7 +649,7 @@ static void launch_forward(long long rows_max, const float * params, const float
     const MlpLaunch s     = mlp_launch_shape<MODE, SAVE>();
     const long long tiles = std::max<long long>(1, (rows_max + kMlpNT - 1) / kMlpNT);
     const int grid        = int(std::min<long long>(tiles, (long long) s.per_sm * num_sms_cached()));
-    k_mlp_forward<MODE, SAVE><<<grid, kMlpNT, s.dyn, st>>>(rows_max, params, norm, feat, out, z1s, h1s, z2s, N,
+    launch_pdl(k_mlp_forward<MODE, SAVE>, grid, kMlpNT, s.dyn, st, rows_max, params, norm, feat, out, z1s, h1s, z2s, N,
                                                            blist, bcount, bn_log2, nv, bb, F, err);
 }
 void launch_mlp_forward_array(long long n, const float * params, const float * norm, const float * feat, float * out,

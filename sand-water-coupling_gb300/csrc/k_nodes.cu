@@ -15,6 +15,7 @@ namespace swc {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_brick_list(const unsigned char * __restrict__ bflag, int nbricks,
                                                      int * __restrict__ list, int * __restrict__ count) {
+    pdl_wait_and_release();
     __shared__ int sm[32];
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
@@ -132,6 +133,7 @@ __global__ void __launch_bounds__(128, 5) k_node_gather(Lattice L, Phys P, const
                                                     const float4 * __restrict__ bvel,
                                                     const int * __restrict__ bcellStart,
                                                     const unsigned char * __restrict__ bnear, int * queue) {
+    pdl_wait_and_release();
     using G          = BrickGeom<DIM>;
     constexpr int NX = 2;
     constexpr int XS = G::BX / NX;  // thread columns per brick row
@@ -256,6 +258,7 @@ template<int DIM>
 __global__ void __launch_bounds__(kNT) k_segment_count(Lattice L, const int * __restrict__ blist,
                                                        const int * __restrict__ bcount,
                                                        const unsigned char * __restrict__ flag, int * __restrict__ seg) {
+    pdl_wait_and_release();
     using G      = BrickGeom<DIM>;
     const int nb = *bcount;
     constexpr int ROWS = G::BY * G::BZ;
@@ -358,6 +361,7 @@ __global__ void __launch_bounds__(kNT) k_warm_start(Lattice L, const int * __res
 template<int DIM>
 __global__ void __launch_bounds__(kNT) k_warm_history(const int * __restrict__ blist, const int * __restrict__ bcount,
                                                       BrickArrays B, NodeArrays N, int history) {
+    pdl_wait_and_release();
     using G = BrickGeom<DIM>;
     constexpr int Q = G::BN / 4;
     const long long total = (long long) (*bcount) * Q;
@@ -577,6 +581,7 @@ __global__ void __launch_bounds__(kGradNT) k_pressure_gradient(Lattice L, Phys P
                                                            const float4 * __restrict__ bvel,
                                                            const float4 * __restrict__ bnrm,
                                                            const int * __restrict__ bcellStart, int * queue) {
+    pdl_wait_and_release();
     using G = BrickGeom<DIM>;
     // Row pitch 24 in 3D: a warp's particles span about four consecutive cell
     // rows of one z-plane, whose 8-node windows then fall in disjoint banks
@@ -700,7 +705,7 @@ void launch_pressure_gradient(const Lattice & L, const Phys & P, const BrickArra
                               const int * plist, const int * pcount, const unsigned char * bnear, const float4 * pos,
                               float4 * vel, const int * cellStart, const float4 * bpos, const float4 * bvel,
                               const float4 * bnrm, const int * bcellStart, int grid, int * queue, cudaStream_t st) {
-    k_pressure_gradient<DIM><<<grid, kGradNT, 0, st>>>(L, P, B.flag, N, plist, pcount, bnear, pos, vel, cellStart, bpos,
+    launch_pdl(k_pressure_gradient<DIM>, grid, kGradNT, 0, st, L, P, B.flag, N, plist, pcount, bnear, pos, vel, cellStart, bpos,
                                                    bvel, bnrm, bcellStart, queue);
 }
 template<int DIM> int pressure_gradient_blocks_per_sm() {
@@ -717,7 +722,7 @@ template<int DIM> int node_gather_blocks_per_sm() {
     return n > 0 ? n : 1;
 }
 void launch_brick_list(const unsigned char * bflag, int nbricks, int * list, int * count, cudaStream_t st) {
-    k_brick_list<<<1, 1024, 0, st>>>(bflag, nbricks, list, count);
+    launch_pdl(k_brick_list, 1, 1024, 0, st, bflag, nbricks, list, count);
 }
 
 template<int DIM>
@@ -727,10 +732,10 @@ void launch_node_gather(const Lattice & L, const Phys & P, const BrickArrays & B
                         int * queue, cudaStream_t st) {
     // H >= 2h: particles within h only reach the inner branch of W_H
     if (double(P.H) >= 2.0 * double(P.h) * (1.0 - 1e-6))
-        k_node_gather<DIM, true><<<grid, 128, 0, st>>>(L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel,
+        launch_pdl(k_node_gather<DIM, true>, grid, 128, 0, st, L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel,
                                                        bcellStart, bnear, queue);
     else
-        k_node_gather<DIM, false><<<grid, 128, 0, st>>>(L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel,
+        launch_pdl(k_node_gather<DIM, false>, grid, 128, 0, st, L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel,
                                                         bcellStart, bnear, queue);
 }
 
@@ -738,7 +743,7 @@ template<int DIM>
 void launch_segments(const Lattice & L, const BrickArrays & B, const NodeArrays & N, int * tiles, int grid,
                      cudaStream_t st) {
     cudaMemsetAsync(B.seg, 0, sizeof(int) * B.nseg, st);
-    k_segment_count<DIM><<<grid, kNT, 0, st>>>(L, B.list, B.count, N.flag, B.seg);
+    launch_pdl(k_segment_count<DIM>, grid, kNT, 0, st, L, B.list, B.count, N.flag, B.seg);
     launch_scan(B.seg, B.nseg, B.seg_off, tiles, st);
 }
 
@@ -756,7 +761,7 @@ void launch_warm_start(const Lattice & L, const BrickArrays & B, const NodeArray
     if (mode == kWarmExtrap) {
         // streaming grid: the slots of the active bricks, 4 per thread
         const long long q = (long long) L.nbricks * (BrickGeom<DIM>::BN / 4);
-        k_warm_history<DIM><<<int(std::min<long long>((q + kNT - 1) / kNT, 152LL * 8)), kNT, 0, st>>>(B.list, B.count, B,
+        launch_pdl(k_warm_history<DIM>, int(std::min<long long>((q + kNT - 1) / kNT, 152LL * 8)), kNT, 0, st, B.list, B.count, B,
                                                                                                     N, history);
         return;
     }

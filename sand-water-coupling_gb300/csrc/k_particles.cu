@@ -71,6 +71,7 @@ __global__ void k_export_ratio(const float * __restrict__ a, int stride, int com
 template<int DIM>
 __global__ void k_cell_count(float4 * __restrict__ pos, const float4 * __restrict__ vel, float dt, long long n,
                              Lattice L, int * __restrict__ key, int * __restrict__ rank, int * __restrict__ count) {
+    pdl_wait_and_release();
     for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
         float4 p = pos[i];
         if (vel) {
@@ -89,12 +90,14 @@ __global__ void k_cell_count(float4 * __restrict__ pos, const float4 * __restric
 
 __global__ void k_cell_scatter(const int * __restrict__ key, const int * __restrict__ rank,
                                const int * __restrict__ start, long long n, int * __restrict__ perm) {
+    pdl_wait_and_release();
     for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
         perm[start[key[i]] + rank[i]] = int(i);
 }
 
 __global__ void k_cell_sort_segments(const int * __restrict__ start, long long ncells, const int * __restrict__ id,
                                      int * __restrict__ perm) {
+    pdl_wait_and_release();
     for (long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x; c < ncells; c += (long long) gridDim.x * blockDim.x) {
         const int b = start[c], e = start[c + 1];
         if (e - b < 2) continue;
@@ -115,6 +118,7 @@ __global__ void k_permute(const int * __restrict__ perm, long long n, const floa
                           const float4 * __restrict__ a1, const float4 * __restrict__ a2, const int * __restrict__ i0,
                           float4 * __restrict__ b0, float4 * __restrict__ b1, float4 * __restrict__ b2,
                           int * __restrict__ j0) {
+    pdl_wait_and_release();
     for (long long s = blockIdx.x * (long long) blockDim.x + threadIdx.x; s < n; s += (long long) gridDim.x * blockDim.x) {
         const int src = perm[s];
         b0[s]         = a0[src];
@@ -155,6 +159,7 @@ template<int DIM>
 __global__ void __launch_bounds__(256) k_density(const float4 * __restrict__ pos, float4 * __restrict__ vel,
                                                  float * __restrict__ rho_out, long long n, Lattice L, Phys P,
                                                  const int * __restrict__ cellStart, float mass, int * __restrict__ left) {
+    pdl_wait_and_release();
     const long long npair = (n + 1) / 2;
     const float c         = 2.f * P.c0h * mass;
     for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < npair;
@@ -179,6 +184,7 @@ template<int DIM>
 __global__ void __launch_bounds__(256) k_density_left(const float4 * __restrict__ pos, float4 * __restrict__ vel,
                                                       float * __restrict__ rho_out, long long n, Lattice L, Phys P,
                                                       const int * __restrict__ cellStart, float mass, int * left) {
+    pdl_wait_and_release();
     // one warp per left-over particle, its neighbour rows spread over the lanes
     const long long cnt = 2LL * left[0];
     const float c       = 2.f * P.c0h * mass;
@@ -265,6 +271,7 @@ template<int DIM>
 __global__ void __launch_bounds__(256) k_forces(const float4 * __restrict__ pos, const float4 * __restrict__ vel,
                                                 float4 * __restrict__ vel_out, long long n, Lattice L, Phys P,
                                                 const int * __restrict__ cellStart, float dt, int * __restrict__ left) {
+    pdl_wait_and_release();
     const float visc      = P.viscosity * 2.f * (DIM + 2.f) * P.mass * dt * P.c1h;
     const float gx = P.gravity_on ? P.gx * dt : 0.f, gy = P.gravity_on ? P.gy * dt : 0.f;
     const float gz = P.gravity_on && DIM == 3 ? P.gz * dt : 0.f;
@@ -289,6 +296,7 @@ template<int DIM>
 __global__ void __launch_bounds__(256) k_forces_left(const float4 * __restrict__ pos, const float4 * __restrict__ vel,
                                                      float4 * __restrict__ vel_out, long long n, Lattice L, Phys P,
                                                      const int * __restrict__ cellStart, float dt, int * left) {
+    pdl_wait_and_release();
     const float visc = P.viscosity * 2.f * (DIM + 2.f) * P.mass * dt * P.c1h;
     const float gx = P.gravity_on ? P.gx * dt : 0.f, gy = P.gravity_on ? P.gy * dt : 0.f;
     const float gz = P.gravity_on && DIM == 3 ? P.gz * dt : 0.f;
@@ -357,6 +365,7 @@ template<int DIM>
 __global__ void __launch_bounds__(256) k_mark_bricks(Lattice L, const int * __restrict__ cellStart, int reach,
                                                      unsigned char * __restrict__ bflag,
                                                      unsigned char * __restrict__ pflag) {
+    pdl_wait_and_release();
     using G               = BrickGeom<DIM>;
     const int lane        = threadIdx.x & 31;
     const long long warp  = (blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5;
@@ -521,6 +530,7 @@ constexpr int kScanThreads = 256, kScanItems = 8, kScanTile = kScanThreads * kSc
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int * __restrict__ in, long long n,
                                                               int * __restrict__ tile_sum) {
+    pdl_wait_and_release();
     __shared__ int sm[kScanThreads / 32];
     const long long base = (long long) blockIdx.x * kScanTile;
     int s = 0;
@@ -541,6 +551,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int * __restr
 }
 
 __global__ void __launch_bounds__(1024) k_scan_top(int * __restrict__ tile_sum, int ntiles) {
+    pdl_wait_and_release();
     __shared__ int sm[32];
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
@@ -577,6 +588,7 @@ __global__ void __launch_bounds__(1024) k_scan_top(int * __restrict__ tile_sum, 
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int * __restrict__ in, long long n,
                                                               const int * __restrict__ tile_off, int * __restrict__ out) {
+    pdl_wait_and_release();
     __shared__ int sm[kScanThreads / 32];
     const long long base = (long long) blockIdx.x * kScanTile + (long long) threadIdx.x * kScanItems;
     int v[kScanItems];
@@ -649,9 +661,9 @@ void launch_scan(const int * in, long long n, int * out, int * tile_buf, cudaStr
         cudaMemsetAsync(out, 0, sizeof(int), st);
         return;
     }
-    k_scan_tiles<<<int(ntiles), kScanThreads, 0, st>>>(in, n, tile_buf);
-    k_scan_top<<<1, 1024, 0, st>>>(tile_buf, int(ntiles));
-    k_scan_apply<<<int(ntiles), kScanThreads, 0, st>>>(in, n, tile_buf, out);
+    launch_pdl(k_scan_tiles, int(ntiles), kScanThreads, 0, st, in, n, tile_buf);
+    launch_pdl(k_scan_top, 1, 1024, 0, st, tile_buf, int(ntiles));
+    launch_pdl(k_scan_apply, int(ntiles), kScanThreads, 0, st, in, n, tile_buf, out);
 }
 long long scan_tile_count(long long n) { return (n + kScanTile - 1) / kScanTile + 1; }
 
@@ -660,13 +672,13 @@ void launch_bin(const Lattice & L, long long n, float4 *& pos, float4 *& vel, fl
                 SortScratch & S, int * cellStart, float advect_dt, cudaStream_t st) {
     cudaMemsetAsync(S.count, 0, sizeof(int) * L.ncells, st);
     if (n > 0)
-        k_cell_count<DIM><<<grid_for(n, 256), 256, 0, st>>>(pos, advect_dt != 0.f ? vel : nullptr, advect_dt, n, L,
+        launch_pdl(k_cell_count<DIM>, grid_for(n, 256), 256, 0, st, pos, advect_dt != 0.f ? vel : nullptr, advect_dt, n, L,
                                                             S.key, S.rank, S.count);
     launch_scan(S.count, L.ncells, cellStart, S.tiles, st);
     if (n == 0) return;
-    k_cell_scatter<<<grid_for(n, 256), 256, 0, st>>>(S.key, S.rank, cellStart, n, S.perm);
-    k_cell_sort_segments<<<grid_for(L.ncells, 256), 256, 0, st>>>(cellStart, L.ncells, id, S.perm);
-    k_permute<<<grid_for(n, 256), 256, 0, st>>>(S.perm, n, pos, vel, aux, id, S.pos2, S.vel2, S.aux2, S.id2);
+    launch_pdl(k_cell_scatter, grid_for(n, 256), 256, 0, st, S.key, S.rank, cellStart, n, S.perm);
+    launch_pdl(k_cell_sort_segments, grid_for(L.ncells, 256), 256, 0, st, cellStart, L.ncells, id, S.perm);
+    launch_pdl(k_permute, grid_for(n, 256), 256, 0, st, S.perm, n, pos, vel, aux, id, S.pos2, S.vel2, S.aux2, S.id2);
     // the sorted arrays become the state; the previous ones the next sort's targets
     std::swap(pos, S.pos2);
     std::swap(vel, S.vel2);
@@ -678,9 +690,9 @@ template<int DIM>
 void launch_density(const float4 * pos, float4 * vel, float * rho, long long n, const Lattice & L, const Phys & P,
                     const int * cellStart, int * left, cudaStream_t st) {
     if (n <= 0) return;
-    k_density<DIM><<<grid_for((n + 1) / 2, 256, 1 << 20), 256, 0, st>>>(pos, vel, rho, n, L, P, cellStart, P.mass,
+    launch_pdl(k_density<DIM>, grid_for((n + 1) / 2, 256, 1 << 20), 256, 0, st, pos, vel, rho, n, L, P, cellStart, P.mass,
                                                                          left);
-    k_density_left<DIM><<<kLeftBlocks, 256, 0, st>>>(pos, vel, rho, n, L, P, cellStart, P.mass, left);
+    launch_pdl(k_density_left<DIM>, kLeftBlocks, 256, 0, st, pos, vel, rho, n, L, P, cellStart, P.mass, left);
 }
 void launch_set_volume(float4 * pos, const float * rho, long long n, float mass, cudaStream_t st) {
     if (n > 0) k_set_volume<<<grid_for(n, 256), 256, 0, st>>>(pos, rho, n, mass);
@@ -689,9 +701,9 @@ template<int DIM>
 void launch_forces(const float4 * pos, const float4 * vel, float4 * vel_out, long long n, const Lattice & L,
                    const Phys & P, const int * cellStart, float dt, int * left, cudaStream_t st) {
     if (n <= 0) return;
-    k_forces<DIM><<<grid_for((n + 1) / 2, 256, 1 << 20), 256, 0, st>>>(pos, vel, vel_out, n, L, P, cellStart, dt,
+    launch_pdl(k_forces<DIM>, grid_for((n + 1) / 2, 256, 1 << 20), 256, 0, st, pos, vel, vel_out, n, L, P, cellStart, dt,
                                                                        left);
-    k_forces_left<DIM><<<kLeftBlocks, 256, 0, st>>>(pos, vel, vel_out, n, L, P, cellStart, dt, left);
+    launch_pdl(k_forces_left<DIM>, kLeftBlocks, 256, 0, st, pos, vel, vel_out, n, L, P, cellStart, dt, left);
 }
 template<int DIM>
 void launch_boundary_density(float4 * bpos, float4 * bvel, float * rho, long long nb, const Lattice & L,
@@ -709,7 +721,7 @@ void launch_mark_bricks(const int * cellStart, long long n, const Lattice & L, c
     }
     const int reach   = int(std::ceil(double(P.h) / double(L.dx))) + 1;
     const long long b = (L.nbricks + 7) / 8;  // eight warps per block, one warp per brick
-    k_mark_bricks<DIM><<<int(std::min<long long>(b, 152LL * 64)), 256, 0, st>>>(L, cellStart, reach, bflag, pflag);
+    launch_pdl(k_mark_bricks<DIM>, int(std::min<long long>(b, 152LL * 64)), 256, 0, st, L, cellStart, reach, bflag, pflag);
 }
 void launch_rotate_boundary(float4 * bpos, float4 * bvel, float4 * bnrm, long long nb, float cx, float cz,
                             float omega, float dt, cudaStream_t st) {

@@ -72,6 +72,24 @@ __device__ __forceinline__ void pdl_wait_and_release() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Launch with programmatic stream serialization: the kernel's blocks may be
+// dispatched while the previous kernel on the stream drains; every kernel
+// launched this way calls pdl_wait_and_release() before it touches memory.
+template<class Kern, class... Args>
+inline void launch_pdl(Kern kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim          = grid;
+    cfg.blockDim         = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream           = st;
+    cudaLaunchAttribute at[1];
+    at[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs    = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // 1/sqrt(x) for normal x (every caller clamps x >= 1e-30): the hardware
 // approximation without the rescaling of denormal inputs that rsqrtf adds.
 __device__ __forceinline__ float rsqrt_n(float x) {
