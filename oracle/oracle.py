@@ -36,10 +36,22 @@ class Params(C.Structure):
     ]
 
 
+class DemParams(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32),
+        ("enable_gravity", C.c_int32),
+        ("radius", C.c_double),
+        ("mass", C.c_double),
+        ("young", C.c_double),
+        ("poisson", C.c_double),
+        ("fric_angle", C.c_double),
+    ]
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle with make (g++ -fopenmp)."""
-    src = os.path.join(HERE, "swc_oracle.cpp")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("swc_oracle.cpp", "dem_oracle.cpp", "orc_core.h", "Makefile")]
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(map(os.path.getmtime, srcs)):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
@@ -83,6 +95,22 @@ def lib():
         L.orc_kernel.argtypes = [C.c_int, C.c_double, C.c_int, C.c_double]
         L.orc_packed_kernel_sum.restype = C.c_double
         L.orc_packed_kernel_sum.argtypes = [C.c_int, C.c_double]
+        # DEM sand step (dem_oracle.cpp)
+        DP = C.POINTER(DemParams)
+        L.dem_create.restype = P
+        L.dem_create.argtypes = [DP]
+        L.dem_destroy.argtypes = [P]
+        L.dem_set_particles.argtypes = [P, C.c_longlong, D, D]
+        L.dem_get_particles.argtypes = [P, D, D]
+        L.dem_set_boundary.argtypes = [P, C.c_longlong, D, D, D]
+        L.dem_initialize.argtypes = [P]
+        L.dem_advance.argtypes = [P, C.c_double]
+        L.dem_get_boundary_info.argtypes = [P, D, D]
+        L.dem_time_step.restype = C.c_double
+        L.dem_time_step.argtypes = [P, C.c_double]
+        L.dem_model.argtypes = [DP, D]
+        L.dem_pair_force.argtypes = [DP, D, D, D, D]
+        L.dem_boundary_term.argtypes = [DP, D, D, C.c_double, C.c_double, D]
         _lib = L
     return _lib
 
@@ -264,3 +292,86 @@ class Oracle:
         ids = np.zeros(max(1, offsets[-1]), dtype=np.int64)
         lib().orc_neighbors(self.h, w, nq, _dp(q), _ip(counts), _ip(offsets), _ip(ids))
         return counts, offsets, ids[: offsets[-1]]
+
+
+def dem_params(dim, radius, mass=1.0, young=1e9, poisson=0.3, fric_angle=0.5, enable_gravity=True):
+    p = DemParams()
+    p.dim, p.enable_gravity, p.radius, p.mass = int(dim), 1 if enable_gravity else 0, float(radius), float(mass)
+    p.young, p.poisson, p.fric_angle = float(young), float(poisson), float(fric_angle)
+    return p
+
+
+def dem_model(p):
+    """K_norm, K_tang, tan(friction angle), d_rupture, capillary coefficient, liquid-bridge volume."""
+    o = np.zeros(6)
+    lib().dem_model(C.byref(p), _dp(o))
+    return dict(zip(("K_norm", "K_tang", "tan_fric", "d_rupture", "coeff_c", "v_bridge"), o))
+
+
+def dem_pair_force(p, d, w):
+    """(contact, capillary) force of one pair, d = x_j - x_i, w = v_j - v_i (3 components)."""
+    d = np.ascontiguousarray(np.resize(np.asarray(d, dtype=np.float64), 3))
+    w = np.ascontiguousarray(np.resize(np.asarray(w, dtype=np.float64), 3))
+    if p.dim == 2:
+        d[2] = w[2] = 0.0
+    f0, f1 = np.zeros(3), np.zeros(3)
+    lib().dem_pair_force(C.byref(p), _dp(d), _dp(w), _dp(f0), _dp(f1))
+    return f0[: p.dim], f1[: p.dim]
+
+
+def dem_boundary_term(p, dv, nb, vol, w):
+    dv = np.zeros(3) + np.pad(np.asarray(dv, dtype=np.float64), (0, 3 - len(dv)))
+    nb = np.zeros(3) + np.pad(np.asarray(nb, dtype=np.float64), (0, 3 - len(nb)))
+    out = np.zeros(3)
+    lib().dem_boundary_term(C.byref(p), _dp(dv), _dp(nb), float(vol), float(w), _dp(out))
+    return out[: p.dim]
+
+
+class DemOracle:
+    """FP64 CPU restatement of DEMParticleSand (initialize / advance / getTimeStep)."""
+
+    def __init__(self, dim, radius, mass=1.0, young=1e9, poisson=0.3, fric_angle=0.5, enable_gravity=True):
+        self.dim = int(dim)
+        self._p = dem_params(dim, radius, mass, young, poisson, fric_angle, enable_gravity)
+        self.h = lib().dem_create(C.byref(self._p))
+        if not self.h:
+            raise ValueError("dem oracle: bad parameters")
+        self.n = self.nb = 0
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().dem_destroy(self.h)
+            self.h = None
+
+    def set_particles(self, x, v):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, self.dim)
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1, self.dim)
+        self.n = x.shape[0]
+        lib().dem_set_particles(self.h, self.n, _dp(x), _dp(v))
+
+    def set_boundary(self, x, nrm, v=None):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, self.dim)
+        nrm = np.ascontiguousarray(nrm, dtype=np.float64).reshape(-1, self.dim)
+        v = None if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(-1, self.dim)
+        self.nb = x.shape[0]
+        lib().dem_set_boundary(self.h, self.nb, _dp(x), _dp(nrm), _dp(v))
+
+    def initialize(self):
+        lib().dem_initialize(self.h)
+
+    def advance(self, dt):
+        lib().dem_advance(self.h, float(dt))
+
+    def particles(self):
+        x = np.zeros((self.n, self.dim))
+        v = np.zeros((self.n, self.dim))
+        lib().dem_get_particles(self.h, _dp(x), _dp(v))
+        return x, v
+
+    def boundary_info(self):
+        rho, vol = np.zeros(self.nb), np.zeros(self.nb)
+        lib().dem_get_boundary_info(self.h, _dp(rho), _dp(vol))
+        return rho, vol
+
+    def time_step(self, step_rate):
+        return lib().dem_time_step(self.h, float(step_rate))

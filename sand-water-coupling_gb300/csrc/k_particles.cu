@@ -67,18 +67,33 @@ __global__ void k_export_ratio(const float * __restrict__ a, int stride, int com
 // ---------------------------------------------------------------------------
 // With vel non-null the particles are first moved, x += v dt
 // (SmthParticleHydrodLiquid::moveParticles, Cores/Physics/SmthParticleHydrodLiquid.cpp:72-76,
-// fused into the pass that reads them anyway).
+// DEMParticleSand::moveParticles, Cores/Physics/DEMParticleSand.cpp:98-99), fused into
+// the pass that reads them anyway.  With lo non-null the position is the
+// float-float pair (pos, lo) and dt = dt + dt_lo: the move is done in
+// float-float arithmetic.  With Ld non-null the lattice is read from device
+// memory (written by an earlier kernel of the stream); L then only sizes the
+// cell arrays.
 template<int DIM>
 __global__ void k_cell_count(float4 * __restrict__ pos, const float4 * __restrict__ vel, float dt, long long n,
-                             Lattice L, int * __restrict__ key, int * __restrict__ rank, int * __restrict__ count) {
+                             Lattice L, int * __restrict__ key, int * __restrict__ rank, int * __restrict__ count,
+                             float4 * __restrict__ lo, float dt_lo, const Lattice * __restrict__ Ld) {
     pdl_wait_and_release();
+    if (Ld) L = *Ld;
     for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
         float4 p = pos[i];
         if (vel) {
             const float4 u = vel[i];
-            p.x    = fmaf(u.x, dt, p.x);
-            p.y    = fmaf(u.y, dt, p.y);
-            p.z    = fmaf(u.z, dt, p.z);
+            if (lo) {
+                float4 l = lo[i];
+                ff_add_product(p.x, l.x, u.x, dt, dt_lo);
+                ff_add_product(p.y, l.y, u.y, dt, dt_lo);
+                if (DIM == 3) ff_add_product(p.z, l.z, u.z, dt, dt_lo);
+                lo[i] = l;
+            } else {
+                p.x = fmaf(u.x, dt, p.x);
+                p.y = fmaf(u.y, dt, p.y);
+                p.z = fmaf(u.z, dt, p.z);
+            }
             pos[i] = p;
         }
         const int3 c   = cell_of<DIM>(L, p.x, p.y, p.z);
@@ -669,11 +684,12 @@ long long scan_tile_count(long long n) { return (n + kScanTile - 1) / kScanTile 
 
 template<int DIM>
 void launch_bin(const Lattice & L, long long n, float4 *& pos, float4 *& vel, float4 *& aux, int *& id,
-                SortScratch & S, int * cellStart, float advect_dt, cudaStream_t st) {
+                SortScratch & S, int * cellStart, float advect_dt, cudaStream_t st, float advect_dt_lo, bool aux_lo,
+                const Lattice * Ld) {
     cudaMemsetAsync(S.count, 0, sizeof(int) * L.ncells, st);
     if (n > 0)
         launch_pdl(k_cell_count<DIM>, grid_for(n, 256), 256, 0, st, pos, advect_dt != 0.f ? vel : nullptr, advect_dt, n, L,
-                                                            S.key, S.rank, S.count);
+                   S.key, S.rank, S.count, aux_lo ? aux : nullptr, advect_dt_lo, Ld);
     launch_scan(S.count, L.ncells, cellStart, S.tiles, st);
     if (n == 0) return;
     launch_pdl(k_cell_scatter, grid_for(n, 256), 256, 0, st, S.key, S.rank, cellStart, n, S.perm);
@@ -758,7 +774,7 @@ void launch_debug_neighbors(int which, long long nq, const double * q, const Lat
 
 #define SWC_INST(D)                                                                                                    \
     template void launch_bin<D>(const Lattice &, long long, float4 *&, float4 *&, float4 *&, int *&, SortScratch &,   \
-                                int *, float, cudaStream_t);                                                           \
+                                int *, float, cudaStream_t, float, bool, const Lattice *);                             \
     template void launch_density<D>(const float4 *, float4 *, float *, long long, const Lattice &, const Phys &,       \
                                     const int *, int *, cudaStream_t);                                                 \
     template void launch_forces<D>(const float4 *, const float4 *, float4 *, long long, const Lattice &, const Phys &,  \

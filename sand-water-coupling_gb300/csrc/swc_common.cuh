@@ -63,6 +63,50 @@ struct Phys {
     int   gravity_on;
 };
 
+// ---------------------------------------------------------------------------
+// Float-float ("double-single") arithmetic: a value is the unevaluated sum
+// hi + lo of two floats with |lo| <= ulp(hi) / 2 (about 48 significant bits)
+// on the FP32 pipe, where GB300's FP64 rate is a small fraction of it.  The
+// error-free steps are Knuth's two-sum and the FMA form of the exact product
+// (Ogita, Rump and Oishi, "Accurate sum and dot product", 2005); the explicit
+// _rn intrinsics keep the compiler from contracting or reassociating them.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(float a, float b, float & s, float & e) {
+    s              = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e              = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// s + e = a + b exactly when |a| >= |b| (or a == 0)
+__device__ __forceinline__ void fast_two_sum(float a, float b, float & s, float & e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+// (hi, lo) += v * (dt + dt_lo)
+__device__ __forceinline__ void ff_add_product(float & hi, float & lo, float v, float dt, float dt_lo) {
+    const float p  = __fmul_rn(v, dt);
+    const float pe = __fmaf_rn(v, dt_lo, __fmaf_rn(v, dt, -p));
+    float s, e;
+    two_sum(hi, p, s, e);
+    e = __fadd_rn(e, __fadd_rn(lo, pe));
+    fast_two_sum(s, e, hi, lo);
+}
+// (h, l) = (ah + al) - (bh + bl)
+__device__ __forceinline__ void ff_diff(float ah, float al, float bh, float bl, float & h, float & l) {
+    float s, e;
+    two_sum(ah, -bh, s, e);
+    e = __fadd_rn(e, __fsub_rn(al, bl));
+    fast_two_sum(s, e, h, l);
+}
+// (sh, sl) += (h + l)^2
+__device__ __forceinline__ void ff_sqr_add(float h, float l, float & sh, float & sl) {
+    const float p  = __fmul_rn(h, h);
+    const float c  = __fmaf_rn(__fmul_rn(2.f, h), l, __fmaf_rn(h, h, -p));
+    float s, e;
+    two_sum(sh, p, s, e);
+    e = __fadd_rn(e, __fadd_rn(sl, c));
+    fast_two_sum(s, e, sh, sl);
+}
+
 // Programmatic dependent launch: a kernel launched with programmatic stream
 // serialization waits here until the preceding kernel's memory is visible
 // (a no-op for an ordinary launch), then lets the next kernel's blocks be

@@ -79,10 +79,14 @@ void launch_set_moving(float4 * bnrm, const unsigned char * moving, const int * 
 void launch_max_positive(const float * a, long long n, int * out_bits, cudaStream_t st);
 // counting sort into cells; the sorted arrays are swapped in (pos, vel, aux, id
 // then point at what were the scratch targets); advect_dt != 0 first moves the
-// particles by vel * advect_dt
+// particles by vel * advect_dt; with aux_lo, aux holds the low parts of
+// float-float positions (pos + aux) and the move uses dt = advect_dt + advect_dt_lo;
+// with Ld (device memory) the cell keys come from that lattice and L.ncells only
+// gives the length of the cell arrays (at least Ld->ncells)
 template<int DIM>
 void launch_bin(const Lattice & L, long long n, float4 *& pos, float4 *& vel, float4 *& aux, int *& id, SortScratch & S,
-                int * cellStart, float advect_dt, cudaStream_t st);
+                int * cellStart, float advect_dt, cudaStream_t st, float advect_dt_lo = 0.f, bool aux_lo = false,
+                const Lattice * Ld = nullptr);
 // Density and forces run one thread per pair of consecutive sorted particles;
 // `left` (n/2 + 3 ints, zeroed once at allocation) collects the pairs that are
 // not in one cell row for a second, single-particle pass.

@@ -1,10 +1,12 @@
 """GB300-native dual-particle SPH pressure projection (skytang0205/sand-water-coupling).
 
 ``DualParticleSphLiquid`` mirrors the reference's Simulation API over the C ABI
-in include/swc.h; ``scenes`` builds the seeded synthetic workloads.
+in include/swc.h, ``DEMParticleSand`` the DEM sand solver over include/swc_sand.h;
+``scenes`` builds the seeded synthetic workloads.
 """
 from . import scenes  # noqa: F401
 from ._lib import SwcError, load  # noqa: F401
 from .liquid import DualParticleSphLiquid  # noqa: F401
+from .sand import DEMParticleSand  # noqa: F401
 
-__all__ = ["DualParticleSphLiquid", "SwcError", "load", "scenes"]
+__all__ = ["DEMParticleSand", "DualParticleSphLiquid", "SwcError", "load", "scenes"]

@@ -1,4 +1,4 @@
-"""ctypes binding of the C ABI in include/swc.h (libswc_gb300.so).
+"""ctypes binding of the C ABI in include/swc.h and include/swc_sand.h (libswc_gb300.so).
 
 Loading fails loudly when the library is missing: there is no CPU fallback.
 """
@@ -82,7 +82,19 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
-# Every symbol declared in include/swc.h, with its ctypes signature.
+class SandParams(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32),
+        ("enable_gravity", C.c_int32),
+        ("radius", C.c_double),
+        ("mass", C.c_double),
+        ("young", C.c_double),
+        ("poisson", C.c_double),
+        ("fric_angle", C.c_double),
+    ]
+
+
+# Every symbol declared in include/swc.h and include/swc_sand.h, with its ctypes signature.
 _P, _D, _I64, _U8 = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_uint8)
 SIGNATURES = {
     "swc_default_solver_opts": (None, [C.POINTER(SolverOpts)]),
@@ -130,6 +142,20 @@ SIGNATURES = {
                                            C.c_void_p, C.c_void_p]),
     "swc_host_alloc": (C.c_void_p, [C.c_size_t]),
     "swc_host_free": (None, [C.c_void_p]),
+    # DEM sand step (include/swc_sand.h)
+    "swc_sand_default_params": (None, [C.POINTER(SandParams)]),
+    "swc_sand_last_error": (C.c_char_p, [_P]),
+    "swc_sand_create": (C.c_int, [C.POINTER(SandParams), C.POINTER(_P)]),
+    "swc_sand_destroy": (None, [_P]),
+    "swc_sand_set_stream": (C.c_int, [_P, _P]),
+    "swc_sand_set_particles": (C.c_int, [_P, _D, _D, C.c_int64]),
+    "swc_sand_get_particles": (C.c_int, [_P, _D, _D, C.c_int64]),
+    "swc_sand_set_boundary": (C.c_int, [_P, _D, _D, C.c_int64]),
+    "swc_sand_initialize": (C.c_int, [_P]),
+    "swc_sand_advance": (C.c_int, [_P, C.c_double]),
+    "swc_sand_get_time_step": (C.c_int, [_P, C.c_double, _D]),
+    "swc_sand_get_boundary_info": (C.c_int, [_P, _D, _D, C.c_int64]),
+    "swc_sand_time_kernel": (C.c_int, [_P, C.c_int, C.c_int, _D]),
 }
 
 _lib = None

@@ -288,3 +288,182 @@ CONFIGS = {
     "projection_block_3d": projection_block_3d,
     "paddle_tank_3d": paddle_tank_3d,
 }
+
+
+# ---------------------------------------------------------------------------
+# DEM sand scenes
+# ---------------------------------------------------------------------------
+def _round_half_away(x):
+    """std::round / Eigen round: halves away from zero (numpy rounds them to even)."""
+    x = np.asarray(x, dtype=np.float64)
+    return np.sign(x) * np.floor(np.abs(x) + 0.5)
+
+
+def packed_box(dim: int, radius: float, center, half_lengths) -> np.ndarray:
+    """Shapes::generateBox without Poisson sampling (Cores/Utilities/Shapes.h:32-58), the
+    same packing as BoundaryParticles::addSurface (Cores/Structures/SmoothedParticles.cpp:111-155):
+    2D rows of a hexagonal lattice at spacing 2r; 3D the faces and nodes of a
+    StaggeredGrid of spacing 2 sqrt(2) r (faces of axis 0, 1, 2, then nodes; x fastest)."""
+    center = np.asarray(center, dtype=np.float64)[:dim]
+    half = np.asarray(half_lengths, dtype=np.float64)[:dim] * np.ones(dim)
+    if dim == 2:
+        spacing = radius * 2
+        xs = int(_round_half_away(half[0] * 2 / spacing))
+        ys = int(_round_half_away((half[1] * 2 / spacing - 1) * 2 / np.sqrt(3.0) + 1))
+        origin = center - np.array([xs - 1, (ys - 1.0) * np.sqrt(3.0) / 2]) * spacing / 2
+        rows = []
+        for j in range(ys):
+            y0 = origin + np.array([0.5 if j & 1 else 0.0, j * np.sqrt(3.0) / 2]) * spacing
+            i = np.arange(xs - (j & 1), dtype=np.float64)
+            rows.append(np.stack([y0[0] + i * spacing, np.full(i.shape, y0[1])], axis=1))
+        return np.concatenate(rows, axis=0) if rows else np.zeros((0, 2))
+    spacing = 2 * np.sqrt(2.0) * radius
+    res = _round_half_away((half - radius) * 2 / spacing).astype(np.int64)
+    origin = center - res.astype(np.float64) * spacing / 2
+    parts = []
+    for axis in range(3):
+        size = res + np.eye(3, dtype=np.int64)[axis]
+        parts.append(_grid_points(size, origin + (1 - np.eye(3)[axis]) * spacing / 2, spacing))
+    parts.append(_grid_points(res + 1, origin, spacing))
+    return np.concatenate(parts, axis=0)
+
+
+def _grid_points(size, off, spacing):
+    """Grid::dataPosition = origin + index * spacing over the grid, x fastest
+    (Cores/Structures/Grid.h:51, Grid.cpp:231-243)."""
+    kz, ky, kx = np.meshgrid(np.arange(size[2]), np.arange(size[1]), np.arange(size[0]), indexing="ij")
+    idx = np.stack([kx.ravel(), ky.ravel(), kz.ravel()], axis=1)
+    return off + idx * spacing
+
+
+def complement_box_boundary(dim: int, radius: float, box_lo, box_hi, center, half_lengths, depth=None):
+    """BoundaryParticles::addSurface(ComplementarySurface(ImplicitBox(box_lo, box_hi - box_lo)),
+    center, half_lengths): the packed points outside (or on) the box with its inward
+    normals.  `depth` keeps only the points within that distance of the box (the
+    reference keeps the whole shell; every boundary particle within 4r of the box
+    has the same neighbours whenever depth >= 8r)."""
+    lo = np.asarray(box_lo, dtype=np.float64)[:dim]
+    hi = np.asarray(box_hi, dtype=np.float64)[:dim]
+    if dim == 3 and depth is not None:
+        pts = _packed_box_3d_shell(radius, center, half_lengths, lo, hi, depth)
+    else:
+        pts = packed_box(dim, radius, center, half_lengths)
+    c, h = (lo + hi) / 2, (hi - lo) / 2
+    phi = np.abs(pts - c) - h
+    sd = np.where(np.all(phi <= 0, axis=1), phi.max(axis=1), np.linalg.norm(np.maximum(phi, 0), axis=1))
+    keep = sd >= 0  # ComplementarySurface::isInside: -sd <= 0 (Cores/Geometries/Surface.h:68)
+    if depth is not None:
+        keep &= sd <= depth
+    pts = pts[keep]
+    return pts, box_inward_normals(pts, lo, hi)
+
+
+def _packed_box_3d_shell(radius, center, half_lengths, lo, hi, depth):
+    """The points of packed_box(3, ...) within `depth` outside the faces of [lo, hi],
+    in the same order, without generating the interior (one slab per face and
+    side, merged per sub-grid by linear index)."""
+    center = np.asarray(center, dtype=np.float64)[:3]
+    half = np.asarray(half_lengths, dtype=np.float64)[:3] * np.ones(3)
+    spacing = 2 * np.sqrt(2.0) * radius
+    res = _round_half_away((half - radius) * 2 / spacing).astype(np.int64)
+    origin = center - res.astype(np.float64) * spacing / 2
+    grids = [(res + np.eye(3, dtype=np.int64)[a], origin + (1 - np.eye(3)[a]) * spacing / 2) for a in range(3)]
+    grids.append((res + 1, origin))
+    out = []
+    eps = 1e-9 * spacing
+    for size, off in grids:
+        keys = []
+        for b in range(3):
+            for side in (0, 1):
+                rlo, rhi = lo - depth, hi + depth
+                rlo, rhi = rlo.copy(), rhi.copy()
+                if side == 0:
+                    rhi[b] = lo[b]
+                else:
+                    rlo[b] = hi[b]
+                i0 = np.maximum(np.ceil((rlo - off) / spacing - eps), 0).astype(np.int64)
+                i1 = np.minimum(np.floor((rhi - off) / spacing + eps), size - 1).astype(np.int64)
+                if np.any(i1 < i0):
+                    continue
+                ax = [np.arange(i0[a], i1[a] + 1) for a in range(3)]
+                kz, ky, kx = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+                keys.append((kx + size[0] * (ky + size[1] * kz)).ravel())
+        if not keys:
+            continue
+        k = np.unique(np.concatenate(keys))
+        idx = np.stack([k % size[0], (k // size[0]) % size[1], k // (size[0] * size[1])], axis=1)
+        out.append(off + idx * spacing)
+    return np.concatenate(out, axis=0) if out else np.zeros((0, 3))
+
+
+@dataclass
+class SandScene:
+    name: str
+    dim: int
+    radius: float
+    mass: float
+    positions: np.ndarray
+    velocities: np.ndarray
+    boundary_positions: np.ndarray
+    boundary_normals: np.ndarray
+    enable_gravity: bool = True
+    young: float = 1e9
+    poisson: float = 0.3
+    fric_angle: float = 0.5
+    dt: float = 1e-4
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n_particles(self) -> int:
+        return int(self.positions.shape[0])
+
+    @property
+    def n_boundary(self) -> int:
+        return int(self.boundary_positions.shape[0])
+
+
+def rotate_velocities(pos: np.ndarray, omega: float, center=None) -> np.ndarray:
+    """Shapes::generateRotate (Cores/Utilities/Shapes.h:95-101): v = omega (y - c_y) e_x - omega (x - c_x) e_y."""
+    c = np.zeros(pos.shape[1]) if center is None else np.asarray(center, dtype=np.float64)[: pos.shape[1]]
+    v = np.zeros_like(pos)
+    v[:, 0] = omega * (pos[:, 1] - c[1])
+    v[:, 1] = -omega * (pos[:, 0] - c[0])
+    return v
+
+
+def sand_rotating_box(dim: int = 2, scale: int = 30, omega: float = 2.0, length: float = 1.0, wall_depth=None,
+                      density: float = 1000.0) -> SandScene:
+    """DEMParticleSandBuilder case 0 (Demos/DEMParticleSandTest/DEMParticleSandBuilder.h:25-57):
+    r = length / 2 / scale / 2, a packed box of half-length length / 8 at the origin
+    rotating at omega, mass density / N, the boundary shell of the box
+    [-length/2, length/2]^dim sampled over half-length 1.2 length (`wall_depth`
+    trims it to the layers within that distance of the box)."""
+    r = length / 2 / scale / 2
+    pos = packed_box(dim, r, np.zeros(dim), np.ones(dim) * length / 8)
+    vel = rotate_velocities(pos, omega)
+    bpos, bnrm = complement_box_boundary(dim, r, -length / 2 * np.ones(dim), length / 2 * np.ones(dim), np.zeros(dim),
+                                         np.ones(dim) * length * 1.2, depth=wall_depth)
+    return SandScene(name=f"sand_rotating_box_{dim}d_s{scale}", dim=dim, radius=r, mass=density / pos.shape[0],
+                     positions=pos, velocities=vel, boundary_positions=bpos, boundary_normals=bnrm,
+                     meta={"scale": scale, "omega": omega, "wall_depth": wall_depth})
+
+
+def sand_contact_block(dim: int = 2, scale: int = 30, seed: int = 0, squeeze: float = 0.99, jitter: float = 0.05,
+                       sigma: float = 0.05, length: float = 1.0, wall_depth=None) -> SandScene:
+    """The builder's packed block squeezed by `squeeze` (every touching pair then
+    overlaps by (1 - squeeze) 2r), jittered by U(+-jitter r), with N(0, sigma) velocities,
+    set down in the corner of the container 1.5 r from the floor and the x = -length/2
+    wall: contacts, Coulomb caps and boundary friction act from the first step."""
+    base = sand_rotating_box(dim, scale, omega=0.0, length=length, wall_depth=wall_depth)
+    r = base.radius
+    rng = np.random.default_rng(seed)
+    pos = base.positions * squeeze + rng.uniform(-jitter * r, jitter * r, base.positions.shape)
+    lo = pos.min(axis=0)
+    shift = np.zeros(dim)
+    shift[0] = -length / 2 + 1.5 * r - lo[0]
+    shift[1] = -length / 2 + 1.5 * r - lo[1]
+    pos = pos + shift
+    vel = rng.normal(0.0, sigma, pos.shape)
+    return SandScene(name=f"sand_contact_block_{dim}d_s{scale}", dim=dim, radius=r, mass=base.mass, positions=pos,
+                     velocities=vel, boundary_positions=base.boundary_positions, boundary_normals=base.boundary_normals,
+                     meta={"scale": scale, "seed": seed, "squeeze": squeeze, "wall_depth": wall_depth})

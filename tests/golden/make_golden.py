@@ -3,8 +3,10 @@
 The reference publishes no golden vectors and cannot be built here, so these
 fixtures pin the oracle (itself cross-checked against an independent
 brute-force restatement in tests/bruteforce.py) on small seeded scenes:
-initialize + a few advance steps, every intermediate of the projection.
-Inputs are rounded through float32 so the GPU path sees identical values.
+initialize + a few advance steps, every intermediate of the projection, and
+the DEM sand step (boundary volumes, states after each advance).  Liquid inputs
+are rounded through float32, sand velocities too, so the GPU path sees
+identical values.
 
     python tests/golden/make_golden.py
 """
@@ -25,6 +27,29 @@ CASES = {
     "dam_break_2d_small": (lambda: scenes.dam_break_2d(seed=11, height_cells=16, width_cells=12), 3),
     "projection_block_3d_n8": (lambda: scenes.projection_block_3d(n=8, seed=12), 2),
 }
+
+
+# DEM sand: the oracle's boundary volumes and states after each advance.
+SAND_CASES = {
+    "sand_contact_block_2d": (lambda: scenes.sand_contact_block(2, scale=30, seed=5), 4),
+}
+
+
+def make_sand(name):
+    build, steps = SAND_CASES[name]
+    s = build()
+    s.velocities = s.velocities.astype(np.float32).astype(np.float64)  # the GPU keeps FP32 velocities
+    o = orc.DemOracle(s.dim, s.radius, s.mass)
+    o.set_particles(s.positions, s.velocities)
+    o.set_boundary(s.boundary_positions, s.boundary_normals)
+    o.initialize()
+    rho, vol = o.boundary_info()
+    out = {"positions": s.positions, "velocities": s.velocities, "steps": steps, "dt": s.dt, "brho": rho, "bvol": vol}
+    for k in range(steps):
+        o.advance(s.dt)
+        out[f"s{k}_x"], out[f"s{k}_v"] = o.particles()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    return out
 
 
 def make(name):
@@ -56,4 +81,7 @@ def make(name):
 if __name__ == "__main__":
     for n in CASES:
         make(n)
+        print("wrote", n)
+    for n in SAND_CASES:
+        make_sand(n)
         print("wrote", n)
