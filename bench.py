@@ -18,6 +18,8 @@ consecutive rejections); ``forms`` reports plain CG from the node-mapped
 previous pressure, from the reference's stale prefix and from zero, the
 extrapolated start alone, the learned start evaluated every step and the
 learned start without the residual test, all on the same scene and steps.
+``sand`` measures the DEM sand step (DEMParticleSand::advance) on a 2,009,840
+particle block the same way (device steps/s, e2e, roofline, CPU port).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl swc|reference]
 
@@ -197,6 +199,126 @@ def run_reference_arm(args):
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# DEM sand leg: DEMParticleSandBuilder's layout (packed block of half-length 1/8 in the
+# container [-1/2, 1/2]^3) at scale 225, r = 1/900: 2,009,840 particles, the block
+# squeezed by 1e-4 (every touching pair overlaps by 2e-4 r) and set down in the
+# container's corner on the floor, N(0, 0.01^2) velocities, walls 8r deep,
+# dt = 1e-4 (the demo's frame rate 10000).
+SAND_SCALE = 225
+SAND_METRIC = "DEM sand advance steps/s at 2,009,840 particles"
+
+
+def sand_scene(scale=SAND_SCALE, seed=0):
+    from swc import scenes
+
+    r = 1.0 / (4 * scale)
+    return scenes.sand_contact_block(3, scale=scale, seed=seed, squeeze=0.9999, jitter=0.0, sigma=0.01,
+                                     wall_depth=8 * r)
+
+
+def sand_cpu_reference(scale=120, steps=5):
+    """The DEM step's CPU restatement (oracle, all host threads) on the same layout at a
+    smaller scale; steps/s scaled by the particle count to the benchmark's."""
+    from oracle import oracle as orc
+
+    orc.build()
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    s = sand_scene(scale)
+    o = orc.DemOracle(3, s.radius, s.mass)
+    o.set_particles(s.positions, s.velocities)
+    o.set_boundary(s.boundary_positions, s.boundary_normals)
+    o.initialize()
+    o.advance(s.dt)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.advance(s.dt)
+    dt = time.perf_counter() - t0
+    n_full = 2009840
+    sps = steps / dt
+    return {"value": sps * s.n_particles / n_full, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} advance steps at scale {scale} ({s.n_particles} particles, {sps:.3f} steps/s), "
+                      f"scaled by {s.n_particles}/{n_full} particles"}
+
+
+def run_sand_leg(args, torch, stream, hbm, peak_kind, with_cpu):
+    """Device-resident steps/s, e2e through the public C ABI with pinned host FP64
+    buffers, the contact pass against the HBM roof, and the CPU port beside it."""
+    from swc import _lib
+    from swc.sand import DEMParticleSand
+
+    s = sand_scene(args.sand_scale)
+    n = s.n_particles
+    g = DEMParticleSand.from_scene(s)
+    g.setStream(stream.cuda_stream)
+    g.initialize()
+    for _ in range(args.warmup):
+        g.advance(s.dt)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        g.advance(s.dt)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    kern = {"contacts": g.timeKernel(0, 20), "binning": g.timeKernel(1, 20)}
+    # algorithmic bytes: the contact pass reads pos, pos_lo, vel and writes vel (16 B each);
+    # the binning moves them (48 B in, 32 B out), writes key / rank, scatters, permutes
+    # pos, pos_lo, vel, id (52 B in and out)
+    alg = {"contacts": 64 * n, "binning": (48 + 32 + 8) * n + (8 + 4) * n + (4 + 52 + 52) * n}
+    dom = max(kern, key=kern.get)
+    ach = alg[dom] / (kern[dom] / 1e3) / 1e9
+    roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+            "peak_source": peak_kind, "traffic": None, "per_kernel_ms": kern,
+            "per_kernel_GBps": {k: alg[k] / (kern[k] / 1e3) / 1e9 for k in kern}}
+    # e2e: host FP64 state in, one advance, host FP64 state out, every step
+    L = _lib.load()
+    nbytes = n * 3 * 8
+    hx_p, hv_p = L.swc_host_alloc(nbytes), L.swc_host_alloc(nbytes)
+    hx = np.frombuffer((C.c_double * (n * 3)).from_address(hx_p), dtype=np.float64).reshape(n, 3)
+    hv = np.frombuffer((C.c_double * (n * 3)).from_address(hv_p), dtype=np.float64).reshape(n, 3)
+    x0, v0 = g.getParticles()
+    hx[:], hv[:] = x0, v0
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+
+    def e2e_step():
+        rc = L.swc_sand_set_particles(g.h, dp(hx), dp(hv), n)
+        rc |= L.swc_sand_advance(g.h, s.dt)
+        rc |= L.swc_sand_get_particles(g.h, dp(hx), dp(hv), n)
+        if rc:
+            raise RuntimeError("sand e2e step failed")
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    f1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = f0.elapsed_time(f1)
+    L.swc_host_free(hx_p)
+    L.swc_host_free(hv_p)
+    g.close()
+    out = {"metric": SAND_METRIC if n == 2009840 else f"DEM sand advance steps/s at {n} particles", "value": args.steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / args.steps,
+           "steps": args.steps, "warmup": args.warmup, "dtype": "f32 (float-float positions)",
+           "config": {"workload": f"DEM sand block (DEMParticleSandBuilder layout, scale {args.sand_scale}, "
+                                  f"r = 1/{4 * args.sand_scale}): "
+                                  f"{n} particles squeezed by 1e-4 on the container floor, {s.n_boundary} wall "
+                                  f"particles 8r deep, dt 1e-4", "particles": n, "boundary": s.n_boundary,
+                      "l2": "inputs larger than L2 (particle state 128 MB + sort scratch per step)"},
+           "e2e": {"value": args.steps / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
+                   "d2h_bytes_per_step": 2 * nbytes},
+           "roofline": roof, "gpu_launches_per_step": 10}
+    if with_cpu:
+        out["cpu_baseline"] = sand_cpu_reference()
+    return out
 
 
 def workload_config(args):
@@ -379,6 +501,9 @@ def run_gpu_arm(args):
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_reference(args, n, sample_n=args.cpu_sample, steps=args.cpu_steps, warmup=1)
         cpu.pop("seconds", None)
+    sand = None
+    if args.sand:
+        sand = run_sand_leg(args, torch, stream, hbm, peak_kind, with_cpu=rank == 0 and ws == 1 and not args.no_cpu)
 
     # kernels launched per step: binning 8, density 1, forces 1, generation 6, warm start 1,
     # CG init 1 + 2 per iteration, gradient 1, export 1
@@ -391,7 +516,7 @@ def run_gpu_arm(args):
                 "wall_s_timed": wall, "cg_iterations_mean": float(np.mean(iters)), "n_virtual": nv,
                 "phases_ms": phases, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk.summary(), "gpu_launches": int(round(launches_per_step * args.steps)),
-                "forms": forms}
+                "forms": forms, "sand": sand}
         print(json.dumps(line), flush=True)
     liq.close()
     if dist is not None:
@@ -417,6 +542,11 @@ def main():
     ap.add_argument("--cpu-steps", dest="cpu_steps", type=int, default=3)
     ap.add_argument("--no-cpu", dest="no_cpu", action="store_true")
     ap.add_argument("--compare-forms", dest="compare_forms", type=int, default=1)
+    ap.add_argument("--sand", type=int, default=1, help="also measure the DEM sand step (the 'sand' object)")
+    ap.add_argument("--sand-scale", dest="sand_scale", type=int, default=SAND_SCALE,
+                    help="builder scale of the sand block (225: 2,009,840 particles)")
+    ap.add_argument("--sand-only", dest="sand_only", action="store_true",
+                    help="only the DEM sand leg (for profiler captures); prints the sand object")
     ap.add_argument("--profile-run", dest="profile_run", action="store_true",
                     help="only the timed steps (for profiler captures); prints a reduced line")
     args = ap.parse_args()
@@ -426,6 +556,13 @@ def main():
         if args.steps > 10:
             args.steps = 10  # each reference step is seconds of CPU work
         run_reference_arm(args)
+    elif args.sand_only:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        hbm, peak_kind = peaks()
+        print(json.dumps(run_sand_leg(args, torch, torch.cuda.Stream(), hbm, peak_kind, with_cpu=not args.no_cpu)),
+              flush=True)
     else:
         run_gpu_arm(args)
 

@@ -40,7 +40,8 @@ struct SandPhys {
 
 namespace {
 
-constexpr int kSandNT = 256;
+constexpr int kSandNT   = 256;
+constexpr int kSandList = 16;  // candidates per thread gathered before their pair terms run
 
 inline int sand_grid(long long n, int threads, int cap = 152 * 16) {
     const long long g = (n + threads - 1) / threads;
@@ -250,7 +251,7 @@ __global__ void k_sand_lattice(unsigned * __restrict__ box, float3 home_lo, floa
 // The contact pass.  d = x_j - x_i, w = v_j - v_i as in DEMParticle::getForce
 // (DEMParticle.cpp:176-181).
 template<int DIM>
-__global__ void __launch_bounds__(kSandNT, 3) k_sand_forces(const Lattice * __restrict__ Ld, Lattice Lb, SandPhys P,
+__global__ void __launch_bounds__(kSandNT, 4) k_sand_forces(const Lattice * __restrict__ Ld, Lattice Lb, SandPhys P,
                                                         const int * __restrict__ cellStart,
                                                         const float4 * __restrict__ pos, const float4 * __restrict__ plo,
                                                         const float4 * __restrict__ vel, float4 * __restrict__ vel_out,
@@ -260,6 +261,7 @@ __global__ void __launch_bounds__(kSandNT, 3) k_sand_forces(const Lattice * __re
                                                         const float4 * __restrict__ bnrm,
                                                         const unsigned char * __restrict__ bnear) {
     pdl_wait_and_release();
+    __shared__ int clist[kSandList * kSandNT];  // per-thread candidate lists, slot-major
     const Lattice L = *Ld;
     for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
         const float4 qi = pos[i], li = plo[i], vi = vel[i];
@@ -269,11 +271,10 @@ __global__ void __launch_bounds__(kSandNT, 3) k_sand_forces(const Lattice * __re
         const float Rq  = P.R + ldexpf(ax + P.R, -21);
         const float Rq2 = Rq * Rq * 1.000001f;
         float fx = 0.f, fy = 0.f, fz = 0.f;
-        for_each_in_radius<DIM>(L, cellStart, qi.x, qi.y, qi.z, Rq, Rq2, [&](int j) {
-            if (j == int(i)) return;  // d = 0, w = 0: the reference's self term is zero
+        // the pair terms of the candidates that pass the FP32 pre-test; run from the
+        // per-thread list below so the lanes of a warp take this path together
+        auto contact = [&](int j) {
             const float4 qj = pos[j];
-            const float ex = qj.x - qi.x, ey = qj.y - qi.y, ez = DIM == 3 ? qj.z - qi.z : 0.f;
-            if (ex * ex + ey * ey + ez * ez >= Rq2) return;
             const float4 lj = plo[j];
             float hx, lx, hy, ly, hz = 0.f, lz = 0.f;
             ff_diff(qj.x, lj.x, qi.x, li.x, hx, lx);
@@ -343,7 +344,20 @@ __global__ void __launch_bounds__(kSandNT, 3) k_sand_forces(const Lattice * __re
                 fy -= __fadd_rn(hy, ly) * inv * s;
                 fz -= __fadd_rn(hz, lz) * inv * s;
             }
+        };
+        int cnt = 0;
+        for_each_in_radius<DIM>(L, cellStart, qi.x, qi.y, qi.z, Rq, Rq2, [&](int j) {
+            if (j == int(i)) return;  // d = 0, w = 0: the reference's self term is zero
+            const float4 qj = pos[j];
+            const float ex = qj.x - qi.x, ey = qj.y - qi.y, ez = DIM == 3 ? qj.z - qi.z : 0.f;
+            if (ex * ex + ey * ey + ez * ez >= Rq2) return;
+            clist[cnt * kSandNT + threadIdx.x] = j;
+            if (++cnt == kSandList) {
+                for (int k = 0; k < cnt; k++) contact(clist[k * kSandNT + threadIdx.x]);
+                cnt = 0;
+            }
         });
+        for (int k = 0; k < cnt; k++) contact(clist[k * kSandNT + threadIdx.x]);
         // force = dt * sum_j F_ij, then the boundary terms without dt (DEMParticleSand.cpp:133-150)
         float Fx = fx * P.dt, Fy = fy * P.dt, Fz = fz * P.dt;
         if (bnear[cell_linear(Lb, cell_of<DIM>(Lb, qi.x, qi.y, qi.z))]) {
