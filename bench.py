@@ -423,6 +423,18 @@ def run_gpu_arm(args):
                 "frac": ach / hbm, "peak_source": peak_kind, "traffic": traffic,
                 "per_kernel_ms": kern, "per_kernel_GBps": {k: alg[k] / (kern[k] / 1e3) / 1e9 for k in kern},
                 "cg_iteration_ms": cg_ms}
+    if dominant == "pressure_gradient":
+        # the gradient is bound by instruction issue, not HBM: its arithmetic against the
+        # FP32 roof (nominal: SMs x 128 lanes x 2 x max clock).  Per particle, the
+        # 268 lattice nodes within H = 4 spacings (4/3 pi 4^3) at 22 FLOP each: r^2 (5),
+        # 1/r (1), r (1), a = 1 - r/4 (2), b = max(a - 1/2, 0) (2), a^2 - 4 b^2 (3),
+        # w = (a^2 - 4 b^2) u / r (2), the three components w d (6)
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        fp32_peak = sms * 128 * 2 * SM_MAX_MHZ * 1e6 / 1e12
+        flops = 268 * 22 * n
+        roofline["fp32"] = {"achieved": flops / (kern["pressure_gradient"] / 1e3) / 1e12, "peak": fp32_peak,
+                            "unit": "TFLOP/s", "peak_source": "nominal",
+                            "frac": flops / (kern["pressure_gradient"] / 1e3) / 1e12 / fp32_peak}
     if dominant == "cg_spmv":
         # the stencil's arithmetic against the FP32 FMA roof (nominal: SMs x 128 lanes x 2 x max clock)
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
