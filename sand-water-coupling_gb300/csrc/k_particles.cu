@@ -111,8 +111,9 @@ __global__ void k_cell_scatter(const int * __restrict__ key, const int * __restr
 }
 
 __global__ void k_cell_sort_segments(const int * __restrict__ start, long long ncells, const int * __restrict__ id,
-                                     int * __restrict__ perm) {
+                                     int * __restrict__ perm, const Lattice * __restrict__ Ld) {
     pdl_wait_and_release();
+    if (Ld) ncells = min(ncells, Ld->ncells);
     for (long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x; c < ncells; c += (long long) gridDim.x * blockDim.x) {
         const int b = start[c], e = start[c + 1];
         if (e - b < 2) continue;
@@ -539,13 +540,15 @@ __global__ void k_max_positive(const float * __restrict__ a, long long n, int * 
 
 // ---------------------------------------------------------------------------
 // Exclusive scan of int32 counts (three phases: tile sums, scan of tile sums,
-// tile scan + offset).  out has n + 1 entries; out[n] = total.
+// tile scan + offset).  out has n + 1 entries; out[n] = total.  With Ld (a
+// lattice in device memory) only its first Ld->ncells <= n counts are scanned.
 // ---------------------------------------------------------------------------
 constexpr int kScanThreads = 256, kScanItems = 8, kScanTile = kScanThreads * kScanItems;
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int * __restrict__ in, long long n,
-                                                              int * __restrict__ tile_sum) {
+                                                              int * __restrict__ tile_sum, const Lattice * __restrict__ Ld) {
     pdl_wait_and_release();
+    if (Ld) n = min(n, Ld->ncells);
     __shared__ int sm[kScanThreads / 32];
     const long long base = (long long) blockIdx.x * kScanTile;
     int s = 0;
@@ -602,8 +605,13 @@ __global__ void __launch_bounds__(1024) k_scan_top(int * __restrict__ tile_sum, 
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int * __restrict__ in, long long n,
-                                                              const int * __restrict__ tile_off, int * __restrict__ out) {
+                                                              const int * __restrict__ tile_off, int * __restrict__ out,
+                                                              const Lattice * __restrict__ Ld) {
     pdl_wait_and_release();
+    if (Ld) {
+        n = min(n, Ld->ncells);
+        if ((long long) blockIdx.x * kScanTile > n) return;  // past the lattice's cells (and past out[n])
+    }
     __shared__ int sm[kScanThreads / 32];
     const long long base = (long long) blockIdx.x * kScanTile + (long long) threadIdx.x * kScanItems;
     int v[kScanItems];
@@ -670,15 +678,15 @@ void launch_export_ratio(const float * a, int stride, int comp, float num, const
     if (n > 0) k_export_ratio<<<grid_for(n, 256), 256, 0, st>>>(a, stride, comp, num, id, n, out);
 }
 
-void launch_scan(const int * in, long long n, int * out, int * tile_buf, cudaStream_t st) {
+void launch_scan(const int * in, long long n, int * out, int * tile_buf, cudaStream_t st, const Lattice * Ld) {
     const long long ntiles = (n + kScanTile - 1) / kScanTile;
     if (n <= 0) {
         cudaMemsetAsync(out, 0, sizeof(int), st);
         return;
     }
-    launch_pdl(k_scan_tiles, int(ntiles), kScanThreads, 0, st, in, n, tile_buf);
+    launch_pdl(k_scan_tiles, int(ntiles), kScanThreads, 0, st, in, n, tile_buf, Ld);
     launch_pdl(k_scan_top, 1, 1024, 0, st, tile_buf, int(ntiles));
-    launch_pdl(k_scan_apply, int(ntiles), kScanThreads, 0, st, in, n, tile_buf, out);
+    launch_pdl(k_scan_apply, int(ntiles), kScanThreads, 0, st, in, n, (const int *) tile_buf, out, Ld);
 }
 long long scan_tile_count(long long n) { return (n + kScanTile - 1) / kScanTile + 1; }
 
@@ -690,10 +698,11 @@ void launch_bin(const Lattice & L, long long n, float4 *& pos, float4 *& vel, fl
     if (n > 0)
         launch_pdl(k_cell_count<DIM>, grid_for(n, 256), 256, 0, st, pos, advect_dt != 0.f ? vel : nullptr, advect_dt, n, L,
                    S.key, S.rank, S.count, aux_lo ? aux : nullptr, advect_dt_lo, Ld);
-    launch_scan(S.count, L.ncells, cellStart, S.tiles, st);
+    launch_scan(S.count, L.ncells, cellStart, S.tiles, st, Ld);
     if (n == 0) return;
     launch_pdl(k_cell_scatter, grid_for(n, 256), 256, 0, st, S.key, S.rank, cellStart, n, S.perm);
-    launch_pdl(k_cell_sort_segments, grid_for(L.ncells, 256), 256, 0, st, cellStart, L.ncells, id, S.perm);
+    launch_pdl(k_cell_sort_segments, grid_for(L.ncells, 256), 256, 0, st, (const int *) cellStart, L.ncells,
+               (const int *) id, S.perm, Ld);
     launch_pdl(k_permute, grid_for(n, 256), 256, 0, st, S.perm, n, pos, vel, aux, id, S.pos2, S.vel2, S.aux2, S.id2);
     // the sorted arrays become the state; the previous ones the next sort's targets
     std::swap(pos, S.pos2);

@@ -66,7 +66,8 @@ void launch_export_scalar(const float * a, int stride, int comp, const int * id,
                           cudaStream_t st);
 void launch_export_ratio(const float * a, int stride, int comp, float num, const int * id, long long n, double * out,
                          cudaStream_t st);
-void launch_scan(const int * in, long long n, int * out, int * tile_buf, cudaStream_t st);
+void launch_scan(const int * in, long long n, int * out, int * tile_buf, cudaStream_t st,
+                 const Lattice * Ld = nullptr);
 long long scan_tile_count(long long n);
 void launch_set_volume(float4 * pos, const float * rho, long long n, float mass, cudaStream_t st);
 void launch_rotate_boundary(float4 * bpos, float4 * bvel, float4 * bnrm, long long nb, float cx, float cz,

@@ -191,15 +191,30 @@ __global__ void k_sand_bbox(const float4 * __restrict__ pos, const float4 * __re
                 hi[a] = fmaxf(hi[a], q[a]);
             }
     }
+    // warp, then block (256 threads), then one atomic per block and bound
+    __shared__ float sl[3][8], sh[3][8];
     for (int a = 0; a < DIM; a++) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
             hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
         }
-        if ((threadIdx.x & 31) == 0 && lo[a] <= hi[a]) {
-            atomicMin(box + a, f2ord(lo[a]));
-            atomicMax(box + 3 + a, f2ord(hi[a]));
+        if ((threadIdx.x & 31) == 0) {
+            sl[a][threadIdx.x >> 5] = lo[a];
+            sh[a][threadIdx.x >> 5] = hi[a];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < DIM) {
+        const int a = threadIdx.x;
+        float l = sl[a][0], h = sh[a][0];
+        for (int w = 1; w < int(blockDim.x >> 5); w++) {
+            l = fminf(l, sl[a][w]);
+            h = fmaxf(h, sh[a][w]);
+        }
+        if (l <= h) {
+            atomicMin(box + a, f2ord(l));
+            atomicMax(box + 3 + a, f2ord(h));
         }
     }
 }
