@@ -310,7 +310,8 @@ __global__ void __launch_bounds__(kSandNT, 4) k_sand_forces(const Lattice * __re
             if (pen > 0.f) {
                 // DEMParticle::ComputeDemForces (DEMParticle.cpp:188-208)
                 const float dist = __fadd_rn(s0, sl);
-                const float inv  = 1.f / (dist <= P.rclamp ? P.rclamp : dist);
+                const bool clamp = dist <= P.rclamp;
+                const float inv  = __frcp_rn(clamp ? P.rclamp : dist);
                 const float nx = __fadd_rn(hx, lx) * inv, ny = __fadd_rn(hy, ly) * inv;
                 const float nz = DIM == 3 ? __fadd_rn(hz, lz) * inv : 0.f;
                 const float4 vj = vel[j];
@@ -333,10 +334,11 @@ __global__ void __launch_bounds__(kSandNT, 4) k_sand_forces(const Lattice * __re
                 const float kp = P.Kn * pen;
                 const float Nx = kp * nx, Ny = kp * ny, Nz = kp * nz;
                 float Sx = -P.Kt * tx, Sy = -P.Kt * ty, Sz = -P.Kt * tz;
-                const float max_fs = sqrtf(Nx * Nx + Ny * Ny + Nz * Nz) * P.tanf;
-                const float sn     = sqrtf(Sx * Sx + Sy * Sy + Sz * Sz);
-                if (sn > max_fs) {
-                    const float k = max_fs / sn;
+                // |normal| = K_n pen |n|, |n| = 1 unless the distance was clamped
+                const float max_fs = kp * (clamp ? dist * inv : 1.f) * P.tanf;
+                const float sn2    = Sx * Sx + Sy * Sy + Sz * Sz;
+                if (sn2 > max_fs * max_fs) {
+                    const float k = max_fs * rsqrtf(sn2);
                     Sx *= k;
                     Sy *= k;
                     Sz *= k;
