@@ -266,7 +266,7 @@ __global__ void k_sand_lattice(unsigned * __restrict__ box, float3 home_lo, floa
 // The contact pass.  d = x_j - x_i, w = v_j - v_i as in DEMParticle::getForce
 // (DEMParticle.cpp:176-181).
 template<int DIM>
-__global__ void __launch_bounds__(kSandNT, 4) k_sand_forces(const Lattice * __restrict__ Ld, Lattice Lb, SandPhys P,
+__global__ void __launch_bounds__(kSandNT, 5) k_sand_forces(const Lattice * __restrict__ Ld, Lattice Lb, SandPhys P,
                                                         const int * __restrict__ cellStart,
                                                         const float4 * __restrict__ pos, const float4 * __restrict__ plo,
                                                         const float4 * __restrict__ vel, float4 * __restrict__ vel_out,
