@@ -113,6 +113,21 @@ def test_reference_scene_rotating_box_2d(oracle_mod, swc_mod):
     assert np.abs(vg - vo).max() < 2e-5 * np.abs(vo).max()
 
 
+def test_reference_scene_rotating_box_3d(oracle_mod, swc_mod):
+    """DEMParticleSandBuilder case 0 in 3D at its default scale 30 as built: 4,631 sand
+    particles and the full 1.2 shell of boundary particles; volumes, then 5 steps."""
+    from swc import scenes
+
+    s = scenes.sand_rotating_box(3, 30)
+    assert s.n_particles == 4631
+    g, o = _pair(s, oracle_mod, swc_mod)
+    rg, vg = g.boundaryInfo()
+    ro, vo = o.boundary_info()
+    np.testing.assert_allclose(vg, vo, rtol=2e-6)
+    for _ in range(5):
+        _check_step(g, o, s.dt)
+
+
 def test_without_boundary_and_gravity_momentum_is_kept(oracle_mod, swc_mod):
     """Pair forces are antisymmetric (F_ij = -F_ji), so with no boundary and no gravity
     a step leaves the total momentum unchanged; checked at 3D scale 120 (307,063 particles)."""
