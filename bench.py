@@ -160,7 +160,7 @@ def barrier(dist):
         dist.barrier()
 
 
-def cpu_reference(args, n_full, sample_n=48, steps=None, warmup=None):
+def cpu_reference(args, n_full, sample_n=48, steps=None, warmup=None, policy=False):
     """The reference algorithm's CPU implementation (oracle port, all host threads)
     on a bounded n^3 sample of the benchmark block; steps/s scaled to n_full particles."""
     from oracle import oracle as orc
@@ -180,10 +180,23 @@ def cpu_reference(args, n_full, sample_n=48, steps=None, warmup=None):
     dt = time.perf_counter() - t0
     sps_sample = steps / dt
     value = sps_sample * s.n_particles / n_full
-    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{steps} advance steps of the {sample_n}^3 = {s.n_particles} particle block "
-                      f"({sps_sample:.3f} steps/s), scaled by {s.n_particles}/{n_full} particles",
-            "seconds": dt}
+    out = {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{steps} advance steps of the {sample_n}^3 = {s.n_particles} particle block "
+                     f"({sps_sample:.3f} steps/s), scaled by {s.n_particles}/{n_full} particles",
+           "seconds": dt}
+    if policy:
+        # the reference demos' own thread count, max(procs / 3, 1)
+        # (Demos/SmthPartHydrodLiquidTest/SmthPartHydrodLiquidTest.cpp:28)
+        t3 = max(threads // 3, 1)
+        orc.set_threads(t3)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            o.advance(s.dt)
+        d3 = time.perf_counter() - t0
+        orc.set_threads(threads)
+        out["reference_thread_policy"] = {"threads": t3, "value": steps / d3 * s.n_particles / n_full,
+                                          "unit": UNIT}
+    return out
 
 
 def run_reference_arm(args):
@@ -511,7 +524,7 @@ def run_gpu_arm(args):
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu = cpu_reference(args, n, sample_n=args.cpu_sample, steps=args.cpu_steps, warmup=1)
+        cpu = cpu_reference(args, n, sample_n=args.cpu_sample, steps=args.cpu_steps, warmup=1, policy=True)
         cpu.pop("seconds", None)
     sand = None
     if args.sand:
