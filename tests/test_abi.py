@@ -74,3 +74,37 @@ def test_no_cpu_fallback(swc_mod):
         pytest.skip("GPU present")
     with pytest.raises(swc.SwcError):
         swc.DualParticleSphLiquid(scenes.dam_break_2d(height_cells=4, width_cells=4))
+
+
+def test_sand_params_layout_and_defaults(swc_mod):
+    """swc_sand_params as laid out in include/swc_sand.h; defaults are the reference's
+    (DEMParticle.cpp:132-136, DEMParticleSandBuilder case 0 radius at scale 30)."""
+    from swc import _lib
+
+    assert C.sizeof(_lib.SandParams) == 2 * 4 + 5 * 8
+    assert _lib.SandParams.radius.offset == 8
+    L = _lib.load()
+    p = _lib.SandParams()
+    L.swc_sand_default_params(C.byref(p))
+    assert (p.dim, p.enable_gravity, p.mass) == (2, 1, 1.0)
+    assert p.young == 1e9 and p.poisson == 0.3 and p.fric_angle == 0.5
+    assert p.radius == pytest.approx(1.0 / 120)
+    h = C.c_void_p()
+    assert L.swc_sand_create(None, C.byref(h)) == _lib.SWC_BAD_ARG
+    p.radius = -1.0
+    assert L.swc_sand_create(C.byref(p), C.byref(h)) == _lib.SWC_BAD_ARG
+
+
+def test_sand_no_cpu_fallback(swc_mod):
+    try:
+        import torch
+
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("GPU present")
+    from swc.sand import DEMParticleSand
+
+    with pytest.raises(swc_mod.SwcError):
+        DEMParticleSand(1.0 / 120, dim=2)
