@@ -134,7 +134,9 @@ int swc_advance(swc_ctx * ctx, double dt, swc_stats * stats);
  * VirtualParticle::project (VirtualParticle.cpp:76-86). */
 int swc_project(swc_ctx * ctx, swc_stats * stats);
 /* SmthParticleHydrodLiquid::getTimeStep (Cores/Physics/SmthParticleHydrodLiquid.h:39-41):
- * step_rate * 2 r / max |v|. */
+ * step_rate * 2 r / max |v| (ParticlesAttribute::normMax,
+ * Cores/Structures/ParticlesAttribute.h:61-67), the maximum reduced on the device;
+ * +inf when every particle is at rest. */
 int swc_get_time_step(swc_ctx * ctx, double step_rate, double * dt);
 
 /* Inspection and replay. */
@@ -142,6 +144,10 @@ int swc_get_real_info(swc_ctx * ctx, double * rho, double * vol, int64_t n);
 int swc_set_volumes(swc_ctx * ctx, const double * vol, int64_t n);
 int swc_get_boundary_info(swc_ctx * ctx, double * rho, double * vol, int64_t nb);
 int swc_set_boundary_info(swc_ctx * ctx, const double * rho, const double * vol, int64_t nb);
+/* Boundary particles as they stand (moving solids turn every advance): positions,
+ * inward normals and velocities in the order of swc_set_boundary; any pointer may
+ * be NULL (the reference's BoundaryParticles members, SmoothedParticles.h:118-134). */
+int swc_get_boundary(swc_ctx * ctx, double * pos, double * normals, double * vel, int64_t nb);
 int swc_get_scalars(swc_ctx * ctx, double * rho0, double * alpha0, double * kappa);
 int swc_set_scalars(swc_ctx * ctx, double rho0, double alpha0, double kappa);
 int64_t swc_num_virtual(swc_ctx * ctx);
@@ -243,6 +249,12 @@ int swc_mlp_gradient(const float * params, const float * norm, const float * fea
 #define SWC_MLP_NOALLOC_MAX_ROWS 2048
 int swc_mlp_gradient_noalloc(const float * params, const float * norm, const float * features,
                              const float * targets, int64_t n, float * grad, float * loss, void * stream);
+
+/* Test hook for the failure paths (no counterpart in the reference): the device
+ * allocation `after` allocations from now (0: the next one) made by any context of
+ * this library, liquid or sand, fails with SWC_OUT_OF_MEMORY instead of calling
+ * cudaMalloc; a negative value disarms it.  Process-wide, meant for tests. */
+int swc_debug_fail_alloc(int64_t after);
 
 /* Pinned host memory helpers for callers that stream state every step. */
 void * swc_host_alloc(size_t bytes);

@@ -5,12 +5,14 @@
 // Same method names and meaning as the reference's Simulation interface
 // (Cores/Physics/Simulation.h:25-34):
 //   initialize(), advance(dt), getTimeStep(frameRate, stepRate), dimension(),
-//   writeFrame(frameDir, staticDraw), saveFrame(frameDir), loadFrame(frameDir).
+//   writeDescription(path), writeFrame(frameDir, staticDraw), saveFrame(frameDir),
+//   loadFrame(frameDir); swc::Simulator (Simulator.hpp) drives it frame by frame.
 // Positions and velocities are exchanged as FP64 arrays of Dim components per
 // particle (the reference's VectorDr storage order).  Errors throw
 // swc::Error carrying the swc_status code instead of calling std::exit.
 #pragma once
 
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdint>
@@ -138,18 +140,64 @@ public:
     swc_ctx * handle() { return ctx_; }
 
     // SmthParticleHydrodLiquid::saveFrame / loadFrame: raw FP64 arrays
-    // (SmthParticleHydrodLiquid.cpp:34-55, Cores/Utilities/IO.h:19-26).
+    // (SmthParticleHydrodLiquid.cpp:34-55, Cores/Utilities/IO.h:19-26), plus dual_state.sav
+    // (n, N_v, rho0, alpha0, kappa, V_i[n], p[N_v]) so that a resumed run keeps the
+    // initial volumes and scalars: the reference's resume skips initialize
+    // (Simulator.cpp:43-45) and loses them.
     void saveFrame(const std::string & frameDir) {
         std::filesystem::create_directories(frameDir);
         pull();
         writeRaw(frameDir + "/particles.sav", pos_);
         writeRaw(frameDir + "/velocities.sav", vel_);
+        const int64_t n = int64_t(pos_.size() / Dim), nv = ctx_ ? swc_num_virtual(ctx_) : 0;
+        std::vector<double> vol(static_cast<size_t>(n)), p(static_cast<size_t>(std::max<int64_t>(nv, 0)));
+        double rho0 = 0, alpha0 = 0, kappa = 0;
+        if (ctx_) {
+            check(swc_get_real_info(ctx_, nullptr, vol.data(), n), "swc_get_real_info");
+            if (nv > 0)
+                check(swc_get_virtual(ctx_, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, p.data(), nv),
+                      "swc_get_virtual");
+            check(swc_get_scalars(ctx_, &rho0, &alpha0, &kappa), "swc_get_scalars");
+        }
+        std::ofstream f(frameDir + "/dual_state.sav", std::ios::binary);
+        const int64_t hdr[2] = {n, int64_t(p.size())};
+        const double  sc[3]  = {rho0, alpha0, kappa};
+        f.write(reinterpret_cast<const char *>(hdr), sizeof(hdr));
+        f.write(reinterpret_cast<const char *>(sc), sizeof(sc));
+        f.write(reinterpret_cast<const char *>(vol.data()), std::streamsize(vol.size() * sizeof(double)));
+        f.write(reinterpret_cast<const char *>(p.data()), std::streamsize(p.size() * sizeof(double)));
     }
     void loadFrame(const std::string & frameDir) {
         pos_ = readRaw(frameDir + "/particles.sav");
         vel_ = readRaw(frameDir + "/velocities.sav");
         dirty_ = true;
         ensure();
+        check(swc_initialize(ctx_), "swc_initialize");  // boundary information
+        std::ifstream f(frameDir + "/dual_state.sav", std::ios::binary);
+        if (!f) return;
+        int64_t hdr[2];
+        double  sc[3];
+        f.read(reinterpret_cast<char *>(hdr), sizeof(hdr));
+        f.read(reinterpret_cast<char *>(sc), sizeof(sc));
+        std::vector<double> vol(static_cast<size_t>(hdr[0])), p(static_cast<size_t>(hdr[1]));
+        f.read(reinterpret_cast<char *>(vol.data()), std::streamsize(vol.size() * sizeof(double)));
+        f.read(reinterpret_cast<char *>(p.data()), std::streamsize(p.size() * sizeof(double)));
+        if (!f) throw Error(SWC_BAD_ARG, "loadFrame", "truncated " + frameDir + "/dual_state.sav");
+        check(swc_set_volumes(ctx_, vol.data(), hdr[0]), "swc_set_volumes");
+        check(swc_set_scalars(ctx_, sc[0], sc[1], sc[2]), "swc_set_scalars");
+        check(swc_set_pressure(ctx_, p.data(), hdr[1]), "swc_set_pressure");
+    }
+    // description.yaml objects of DualParticleSphLiquid::writeDescription
+    // (DualParticleSphLiquid.cpp:8-40) as YAML text, with the dimension line the
+    // Simulator adds (Simulator.cpp:33-39).
+    void writeDescription(const std::string & path) const {
+        std::ofstream f(path);
+        f << "dimension: " << Dim << "\nobjects:\n";
+        const char * names[3] = {"particles", "virtual_particles", "boundary_particles"};
+        for (int k = 0; k < 3; k++)
+            f << "  - name: " << names[k] << "\n    data_mode: dynamic\n    primitive_type: point_list\n"
+              << "    material:\n      diffuse_albedo: [0.203921569, 0.423529412, 0.611764706, 1]\n"
+              << "    indexed: false\n    color_map:\n      enabled: " << (k < 2 ? "true" : "false") << "\n";
     }
     // particles.mesh of writeFrame (DualParticleSphLiquid.cpp:42-52).
     void writeFrame(const std::string & frameDir, bool staticDraw = false) {

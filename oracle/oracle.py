@@ -74,6 +74,9 @@ def lib():
         L.orc_get_particles.argtypes = [P, D, D]
         L.orc_set_boundary.argtypes = [P, C.c_int64, D, D, D]
         L.orc_set_boundary_motion.argtypes = [P, C.POINTER(C.c_uint8), D, C.c_double]
+        L.orc_set_searcher.argtypes = [P, C.c_int]
+        L.orc_hash_candidates.restype = C.c_int64
+        L.orc_hash_candidates.argtypes = [P, C.c_int, C.c_int64, D]
         for n in ("orc_initialize", "orc_project", "orc_compute_densities"):
             getattr(L, n).argtypes = [P]
         L.orc_advance.argtypes = [P, C.c_double]
@@ -142,7 +145,7 @@ def num_threads() -> int:
 class Oracle:
     """FP64 CPU restatement of DualParticleSphLiquid (initialize / advance / project)."""
 
-    def __init__(self, scene, tolerance=None, max_iterations=-1):
+    def __init__(self, scene, tolerance=None, max_iterations=-1, searcher="hash"):
         self.scene = scene
         self.dim = scene.dim
         p = Params()
@@ -167,6 +170,26 @@ class Oracle:
             raise ValueError("oracle: bad parameters")
         self.set_particles(scene.positions, scene.velocities)
         self.set_boundary(scene.boundary_positions, scene.boundary_normals, scene.boundary_velocities)
+        self.set_searcher(searcher)
+
+    def set_searcher(self, kind: str):
+        """Neighbour searcher of every query: "hash", the reference's hash grid (its
+        enumeration order), or "cells", a cell grid over the same cells (the same
+        neighbour sets in cell order; FP64 sums differ in rounding only).  The
+        reference's hash degenerates when its 2N bucket count is a power of two
+        (128^3 particles), so scenes of that size use "cells"."""
+        if kind not in ("hash", "cells"):
+            raise ValueError(f"searcher {kind!r}")
+        self.searcher = kind
+        lib().orc_set_searcher(self.h, 1 if kind == "cells" else 0)
+
+    def hash_candidates(self, which: str, queries) -> float:
+        """Mean number of candidates the reference's hash grid visits per query
+        (bucket entries before the distance test) on the current real / boundary /
+        virtual set: the reference searcher's per-query cost."""
+        w = {"real": 0, "boundary": 1, "virtual": 2}[which]
+        q = np.ascontiguousarray(queries, dtype=np.float64)
+        return lib().orc_hash_candidates(self.h, w, q.shape[0], _dp(q)) / max(q.shape[0], 1)
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -77,7 +77,7 @@ template<int D> struct Oracle {
     std::vector<int32_t> col;
     std::vector<double>  val;
 
-    HashGrid<D> sReal, sBnd, sVirt;
+    Searcher<D> sReal, sBnd, sVirt;
     double rho0 = 0, alpha0 = -1e6, kappa = 0;
     int cgIters = 0, cgEigenIters = 0, status = 0;
     double cgRelRes = 0, rhsNorm = 0;
@@ -196,40 +196,53 @@ template<int D> struct Oracle {
     }
 
     // VirtualParticle::calculateCoef (VirtualParticle.cpp:149-169), stored row-wise with
-    // duplicates merged and columns ascending (the column order Eigen's setFromTriplets gives).
+    // duplicates merged and columns ascending (the column order Eigen's setFromTriplets
+    // gives).  The only duplicate is the diagonal: the search visits J = I (distance 0,
+    // alpha_II = 0 since W'(0) = 0) and the clamped diagonal is added to it.  Two passes
+    // (count, then fill) build the CSR arrays in place.
     void calculateCoef(double a0) {
         const size_t n = xv.size();
-        std::vector<std::vector<std::pair<int, double>>> rows(n);
         alphaHat.assign(n, 0);
+        rowStart.assign(n + 1, 0);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long long I = 0; I < (long long) n; I++) {
+            int64_t c = 0;
+            sVirt.forEach(xv, xv[I], [&](int, const Vec<D> &) { c++; });
+            rowStart[I + 1] = c;
+        }
+        for (size_t I = 0; I < n; I++) rowStart[I + 1] += rowStart[I];
+        col.resize(rowStart[n]);
+        val.resize(rowStart[n]);
+        std::vector<int> bad;
 #pragma omp parallel for schedule(dynamic, 64)
         for (long long I = 0; I < (long long) n; I++) {
             double sum = 0;
-            auto & row = rows[I];
+            int64_t o = rowStart[I], self = -1;
             sVirt.forEach(xv, xv[I], [&](int J, const Vec<D> & pJ) {
                 const double r = norm<D>(sub<D>(xv[I], pJ));
                 const double a = 2. * volv[J] * KH.dW(r) / (r + 1e-6);
                 sum -= a;
-                row.push_back({J, a});
+                if (J == int(I)) self = o;
+                col[o] = J, val[o] = a, o++;
             });
             const double dg = std::max(sum, a0);
-            row.push_back({int(I), dg});
-            std::sort(row.begin(), row.end(), [](auto & l, auto & r) { return l.first < r.first; });
-            size_t o = 0;
-            for (size_t t = 0; t < row.size(); t++) {
-                if (o && row[o - 1].first == row[t].first) row[o - 1].second += row[t].second;
-                else row[o++] = row[t];
-            }
-            row.resize(o);
             alphaHat[I] = dg;
+            if (self < 0) {
+#pragma omp critical
+                bad.push_back(int(I));
+                continue;
+            }
+            val[self] += dg;
+            // sort the row by column (the search order is not the column order)
+            const int64_t b = rowStart[I], e = rowStart[I + 1];
+            std::vector<std::pair<int, double>> row(size_t(e - b));
+            for (int64_t t = b; t < e; t++) row[size_t(t - b)] = {col[t], val[t]};
+            std::sort(row.begin(), row.end(), [](auto & l, auto & r) { return l.first < r.first; });
+            for (int64_t t = b; t < e; t++) col[t] = row[size_t(t - b)].first, val[t] = row[size_t(t - b)].second;
         }
-        rowStart.assign(n + 1, 0);
-        for (size_t I = 0; I < n; I++) rowStart[I + 1] = rowStart[I] + int64_t(rows[I].size());
-        col.resize(rowStart[n]);
-        val.resize(rowStart[n]);
-#pragma omp parallel for
-        for (long long I = 0; I < (long long) n; I++) {
-            int64_t o = rowStart[I];
-            for (auto & e : rows[I]) col[o] = e.first, val[o] = e.second, o++;
+        if (!bad.empty()) {
+            std::fprintf(stderr, "oracle: virtual node %d does not find itself within H\n", bad[0]);
+            std::abort();
         }
     }
 
@@ -452,6 +465,19 @@ template<int D> void loadVecs(std::vector<Vec<D>> & dst, const double * src, int
     for (int64_t i = 0; i < n; i++)
         for (int a = 0; a < D; a++) dst[i][a] = src ? src[i * D + a] : 0.0;
 }
+template<int D> int64_t hashCandidates(const Oracle<D> & O, int which, int64_t nq, const double * q) {
+    HashGrid<D> g;
+    g.setRadius(which == 2 ? O.KH.h : O.Kh.h);
+    g.reset(which == 0 ? O.x : which == 1 ? O.xb : O.xv);
+    int64_t total = 0;
+#pragma omp parallel for reduction(+ : total) schedule(dynamic, 64)
+    for (long long t = 0; t < (long long) nq; t++) {
+        Vec<D> p;
+        for (int a = 0; a < D; a++) p[a] = q[t * D + a];
+        total += g.candidates(p);
+    }
+    return total;
+}
 template<int D> void storeVecs(const std::vector<Vec<D>> & src, double * dst) {
     for (size_t i = 0; i < src.size(); i++)
         for (int a = 0; a < D; a++) dst[i * D + a] = src[i][a];
@@ -512,7 +538,24 @@ void orc_set_boundary(Handle * h, int64_t n, const double * x, const double * nr
         orc::loadVecs<D>(O.xb, x, n);
         orc::loadVecs<D>(O.nb, nrm, n);
         orc::loadVecs<D>(O.vb, v, n);
+        O.sBnd.reset(O.xb);  // a replayed step needs no initialize
     });
+}
+// Searcher of every neighbour query: 0 = the reference's hash grid (its enumeration
+// order; default), 1 = the cell grid over the same cells (same sets, other order).
+void orc_set_searcher(Handle * h, int cells) {
+    DISPATCH(h, {
+        for (auto * s : {&O.sReal, &O.sBnd, &O.sVirt}) s->useCells = cells != 0;
+        O.sReal.reset(O.x);
+        O.sBnd.reset(O.xb);
+        O.sVirt.reset(O.xv);
+    });
+}
+// Candidates the reference's hash grid visits (bucket entries before the distance
+// test) summed over nq query points, for the real (which 0), boundary (1) or
+// virtual (2) set as it stands: the reference searcher's cost.
+int64_t orc_hash_candidates(Handle * h, int which, int64_t nq, const double * q) {
+    return h->dim == 2 ? orc::hashCandidates<2>(h->o2, which, nq, q) : orc::hashCandidates<3>(h->o3, which, nq, q);
 }
 void orc_set_boundary_motion(Handle * h, const unsigned char * moving, const double * center, double omega) {
     DISPATCH(h, {

@@ -61,6 +61,31 @@ __global__ void k_export_ratio(const float * __restrict__ a, int stride, int com
         out[id[s]] = double(num) / double(a[s * stride + comp]);
 }
 
+// max_i |v_i|^2 over the particles, squared norms in FP64 of the FP32 components
+// (ParticlesAttribute::normMax, Cores/Structures/ParticlesAttribute.h:61-67; a NaN
+// component is skipped as std::max skips it there).  Non-negative doubles order
+// like their bit patterns, so block maxima combine with an integer atomicMax.
+__global__ void k_max_speed2(const float4 * __restrict__ vel, long long n, int dim,
+                             unsigned long long * __restrict__ out) {
+    double m = 0;
+    for (long long s = blockIdx.x * (long long) blockDim.x + threadIdx.x; s < n; s += (long long) gridDim.x * blockDim.x) {
+        const float4 u = vel[s];
+        double q = double(u.x) * u.x + double(u.y) * u.y;
+        if (dim == 3) q += double(u.z) * u.z;
+        m = fmax(m, q);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ double wm[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) wm[w] = m;
+    __syncthreads();
+    if (w == 0) {
+        m = lane < (int) (blockDim.x >> 5) ? wm[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) atomicMax(out, (unsigned long long) __double_as_longlong(m));
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Counting sort into cells.  Order within a cell is made deterministic by an
 // insertion sort on the original id, so the final order is (cell, id).
@@ -668,6 +693,9 @@ void launch_import(const double * x, const double * v, int dim, long long n, flo
 void launch_export(const float4 * pos, const float4 * vel, const int * id, int dim, long long n, double * x,
                    double * v, cudaStream_t st) {
     if (n > 0) k_export<<<grid_for(n, 256), 256, 0, st>>>(pos, vel, id, dim, n, x, v);
+}
+void launch_max_speed2(const float4 * vel, long long n, int dim, unsigned long long * out, cudaStream_t st) {
+    if (n > 0) k_max_speed2<<<grid_for(n, 256), 256, 0, st>>>(vel, n, dim, out);
 }
 void launch_export_scalar(const float * a, int stride, int comp, const int * id, long long n, double * out,
                           cudaStream_t st) {

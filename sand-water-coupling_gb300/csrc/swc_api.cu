@@ -4,6 +4,7 @@
 // iterations are replayed from captured CUDA graphs between host convergence
 // checks.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <limits>
 #include <cstdio>
@@ -16,6 +17,19 @@
 #include "swc_kernels.h"
 
 using namespace swc;
+
+namespace swc {
+// allocations left before the armed failure (-1: none armed)
+std::atomic<int64_t> g_fail_alloc_after{-1};
+
+bool debug_alloc_should_fail() {
+    int64_t k = g_fail_alloc_after.load();
+    while (k >= 0) {
+        if (g_fail_alloc_after.compare_exchange_weak(k, k - 1)) return k == 0;
+    }
+    return false;
+}
+}  // namespace swc
 
 namespace {
 
@@ -104,6 +118,7 @@ struct swc_ctx {
     double *    partials = nullptr;
     HostCg *    hcg = nullptr;  // pinned
     unsigned long long * diag_bits = nullptr;
+    unsigned long long * vmax_bits = nullptr;  // max |v|^2 (swc_get_time_step)
     int *       max_bits = nullptr;
     double *    res2 = nullptr;
     cudaGraphExec_t g1 = nullptr, g8 = nullptr;
@@ -132,6 +147,10 @@ template<class T> int dalloc(swc_ctx * c, T ** p, size_t count) {
     if (*p) cudaFree(*p);
     *p = nullptr;
     if (count == 0) count = 1;
+    if (debug_alloc_should_fail()) {
+        c->err = "cudaMalloc: out of memory (injected)";
+        return SWC_OUT_OF_MEMORY;
+    }
     CK(cudaMalloc(reinterpret_cast<void **>(p), sizeof(T) * count));
     return SWC_OK;
 }
@@ -857,6 +876,7 @@ void swc_destroy(swc_ctx * c) {
     dfree(c->partials);
     dfree(c->queues);
     dfree(c->diag_bits);
+    dfree(c->vmax_bits);
     dfree(c->max_bits);
     dfree(c->res2);
     if (c->hcg) cudaFreeHost(c->hcg);
@@ -927,9 +947,11 @@ int swc_set_particles(swc_ctx * c, const double * x, const double * v, int64_t n
         if ((rc = dalloc(c, &c->pos, n)) || (rc = dalloc(c, &c->vel, n)) || (rc = dalloc(c, &c->vel2, n)) ||
             (rc = dalloc(c, &c->id, n)) || (rc = dalloc(c, &c->rho, n)) || (rc = dalloc(c, &c->vol_by_id, n)) ||
             (rc = dalloc(c, &c->stage, size_t(2) * std::max<int64_t>(n, 1) * c->dim)) ||
-            (rc = dalloc(c, &c->pleft, size_t(n) / 2 + 3)))
+            (rc = dalloc(c, &c->pleft, size_t(n) / 2 + 3)) || (rc = alloc_sort(c, c->sortR, n, false))) {
+            c->n           = 0;
+            c->initialized = false;
             return rc;
-        if ((rc = alloc_sort(c, c->sortR, n, false))) return rc;
+        }
         CK(cudaMemsetAsync(c->pleft, 0, sizeof(int) * 2, c->stream));
         c->n = n;
     }
@@ -958,11 +980,16 @@ int swc_set_boundary(swc_ctx * c, const double * x, const double * nrm, const do
     if (!valid_ctx(c) || nb < 0 || (nb > 0 && (!x || !nrm))) return SWC_BAD_ARG;
     int rc;
     CK(cudaStreamSynchronize(c->stream));
+    // a failed allocation leaves no boundary and an uninitialized context, so a later
+    // advance returns SWC_NOT_INITIALIZED instead of reaching freed buffers
     if ((rc = dalloc(c, &c->bpos, nb)) || (rc = dalloc(c, &c->bvel, nb)) || (rc = dalloc(c, &c->bnrm, nb)) ||
         (rc = dalloc(c, &c->bid, nb)) || (rc = dalloc(c, &c->brho, nb)) ||
-        (rc = dalloc(c, &c->bstage, size_t(3) * std::max<int64_t>(nb, 1) * c->dim)))
+        (rc = dalloc(c, &c->bstage, size_t(3) * std::max<int64_t>(nb, 1) * c->dim)) ||
+        (rc = alloc_sort(c, c->sortB, nb, true))) {
+        c->nb          = 0;
+        c->initialized = false;
         return rc;
-    if ((rc = alloc_sort(c, c->sortB, nb, true))) return rc;
+    }
     c->nb = nb;
     const size_t bytes = sizeof(double) * size_t(nb) * c->dim;
     double * sx = c->bstage;
@@ -1020,16 +1047,35 @@ int swc_project(swc_ctx * c, swc_stats * st) {
 
 int swc_get_time_step(swc_ctx * c, double step_rate, double * dt) {
     if (!valid_ctx(c) || !dt) return SWC_BAD_ARG;
-    std::vector<double> v(size_t(c->n) * c->dim);
-    int rc = swc_get_particles(c, nullptr, v.data(), c->n);
-    if (rc) return rc;
-    double m2 = 0;
-    for (long long i = 0; i < c->n; i++) {
-        double s = 0;
-        for (int a = 0; a < c->dim; a++) s += v[i * c->dim + a] * v[i * c->dim + a];
-        m2 = std::max(m2, s);
+    unsigned long long bits = 0;
+    if (c->n > 0) {
+        int rc;
+        if (!c->vmax_bits && (rc = dalloc(c, &c->vmax_bits, 1))) return rc;
+        CK(cudaMemsetAsync(c->vmax_bits, 0, sizeof(unsigned long long), c->stream));
+        launch_max_speed2(c->vel, c->n, c->dim, c->vmax_bits, c->stream);
+        CK(cudaMemcpyAsync(&bits, c->vmax_bits, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
     }
+    double m2;
+    std::memcpy(&m2, &bits, sizeof(m2));
+    // at rest max |v| = 0 and the step is unbounded (+inf), as in the reference
     *dt = step_rate * c->scene.particle_radius * 2 / std::sqrt(m2);
+    return SWC_OK;
+}
+
+int swc_get_boundary(swc_ctx * c, double * pos, double * normals, double * vel, int64_t nb) {
+    if (!valid_ctx(c) || nb != c->nb) return SWC_BAD_ARG;
+    if (nb == 0) return SWC_OK;
+    double * sx = c->bstage;
+    double * sn = c->bstage + size_t(nb) * c->dim;
+    double * sv = c->bstage + 2 * size_t(nb) * c->dim;
+    launch_export(c->bpos, c->bvel, c->bid, c->dim, nb, pos ? sx : nullptr, vel ? sv : nullptr, c->stream);
+    if (normals) launch_export(c->bnrm, nullptr, c->bid, c->dim, nb, sn, nullptr, c->stream);
+    const size_t bytes = sizeof(double) * size_t(nb) * c->dim;
+    if (pos) CK(cudaMemcpyAsync(pos, sx, bytes, cudaMemcpyDeviceToHost, c->stream));
+    if (normals) CK(cudaMemcpyAsync(normals, sn, bytes, cudaMemcpyDeviceToHost, c->stream));
+    if (vel) CK(cudaMemcpyAsync(vel, sv, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return SWC_OK;
 }
 
@@ -1358,6 +1404,11 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
         cudaFree(vel_save);
     }
     CK(cudaGetLastError());
+    return SWC_OK;
+}
+
+int swc_debug_fail_alloc(int64_t after) {
+    swc::g_fail_alloc_after.store(after < 0 ? -1 : after);
     return SWC_OK;
 }
 

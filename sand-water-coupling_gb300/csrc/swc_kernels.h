@@ -64,6 +64,7 @@ void launch_export(const float4 * pos, const float4 * vel, const int * id, int d
                    double * v, cudaStream_t st);
 void launch_export_scalar(const float * a, int stride, int comp, const int * id, long long n, double * out,
                           cudaStream_t st);
+void launch_max_speed2(const float4 * vel, long long n, int dim, unsigned long long * out, cudaStream_t st);
 void launch_export_ratio(const float * a, int stride, int comp, float num, const int * id, long long n, double * out,
                          cudaStream_t st);
 void launch_scan(const int * in, long long n, int * out, int * tile_buf, cudaStream_t st,
@@ -219,5 +220,10 @@ void launch_mlp_targets(long long rows_max, const int * nv, const int * slot_of,
                         cudaStream_t st);
 void launch_gather_rows(const float * src, const float * src_t, const int * idx, long long n, float * dst,
                         float * dst_t, cudaStream_t st);
+
+// ---- host-side allocation fault injection (tests of the failure paths) ----
+// True when the device allocation about to be made is the one armed by
+// swc_debug_fail_alloc; that allocation then reports out-of-memory.
+bool debug_alloc_should_fail();
 
 }  // namespace swc

@@ -472,6 +472,10 @@ template<class T> int salloc(swc_sand * s, T ** p, size_t count) {
     if (*p) cudaFree(*p);
     *p = nullptr;
     if (count == 0) count = 1;
+    if (swc::debug_alloc_should_fail()) {
+        s->err = "cudaMalloc: out of memory (injected)";
+        return SWC_OUT_OF_MEMORY;
+    }
     SK(cudaMalloc(reinterpret_cast<void **>(p), sizeof(T) * count));
     return SWC_OK;
 }
@@ -789,16 +793,24 @@ int swc_sand_set_stream(swc_sand * s, void * stream) {
 int swc_sand_set_particles(swc_sand * s, const double * x, const double * v, int64_t n) {
     if (!valid(s) || n < 0 || (n > 0 && !x) || n > (1LL << 30)) return SWC_BAD_ARG;
     int rc;
+    // a failed allocation leaves no particles and an uninitialized context, so a
+    // later advance returns SWC_NOT_INITIALIZED instead of reaching freed buffers
+    auto fail = [s](int code) {
+        s->n           = 0;
+        s->initialized = false;
+        s->sorted      = false;
+        return code;
+    };
     if (n != s->n || !s->pos) {
         SK(cudaStreamSynchronize(s->stream));
         s->n = n;
         if ((rc = salloc(s, &s->pos, n)) || (rc = salloc(s, &s->plo, n)) || (rc = salloc(s, &s->vel, n)) ||
             (rc = salloc(s, &s->vel2, n)) || (rc = salloc(s, &s->id, n)) || (rc = alloc_particle_sort(s)))
-            return rc;
+            return fail(rc);
     }
     // the box only places the home box at initialize; later states need no host pass
     if (!s->initialized) grow_box(s->dim, x, n, s->bb_lo, s->bb_hi, s->has_bb);
-    if ((rc = ensure_stage(s, size_t(2) * std::max<int64_t>(n, 1) * s->dim))) return rc;
+    if ((rc = ensure_stage(s, size_t(2) * std::max<int64_t>(n, 1) * s->dim))) return fail(rc);
     const size_t bytes = sizeof(double) * size_t(n) * s->dim;
     if (n > 0) {
         SK(cudaMemcpyAsync(s->stage, x, bytes, cudaMemcpyHostToDevice, s->stream));
@@ -808,7 +820,7 @@ int swc_sand_set_particles(swc_sand * s, const double * x, const double * v, int
     }
     SK(cudaGetLastError());
     // cell arrays for a new count; the next advance sorts the particles into them
-    if (s->initialized && (rc = ensure_sand_cells(s))) return rc;
+    if (s->initialized && (rc = ensure_sand_cells(s))) return fail(rc);
     s->sorted = false;
     return SWC_OK;
 }
@@ -833,14 +845,22 @@ int swc_sand_set_boundary(swc_sand * s, const double * x, const double * normals
     if (!valid(s) || nb < 0 || (nb > 0 && (!x || !normals)) || nb > (1LL << 30)) return SWC_BAD_ARG;
     SK(cudaStreamSynchronize(s->stream));
     int rc;
-    s->nb = nb;
+    // the boundary changes: volumes and lattice wait for the next initialize, also
+    // when an allocation below fails (no boundary is left then)
+    s->initialized = false;
+    s->nb          = nb;
     if ((rc = salloc(s, &s->bpos, nb)) || (rc = salloc(s, &s->blo, nb)) || (rc = salloc(s, &s->bnrm, nb)) ||
-        (rc = salloc(s, &s->bid, nb)) || (rc = salloc(s, &s->brho, nb)))
+        (rc = salloc(s, &s->bid, nb)) || (rc = salloc(s, &s->brho, nb))) {
+        s->nb = 0;
         return rc;
+    }
     grow_box(s->dim, x, nb, s->bb_lo, s->bb_hi, s->has_bb);
     s->has_bbb = false;
     grow_box(s->dim, x, nb, s->bbb_lo, s->bbb_hi, s->has_bbb);
-    if ((rc = ensure_stage(s, size_t(2) * std::max<int64_t>(nb, 1) * s->dim))) return rc;
+    if ((rc = ensure_stage(s, size_t(2) * std::max<int64_t>(nb, 1) * s->dim))) {
+        s->nb = 0;
+        return rc;
+    }
     if (nb > 0) {
         const size_t bytes = sizeof(double) * size_t(nb) * s->dim;
         SK(cudaMemcpyAsync(s->stage, x, bytes, cudaMemcpyHostToDevice, s->stream));
@@ -853,7 +873,6 @@ int swc_sand_set_boundary(swc_sand * s, const double * x, const double * normals
     }
     SK(cudaGetLastError());
     SK(cudaStreamSynchronize(s->stream));
-    s->initialized = false;  // boundary volumes and the lattice are rebuilt by initialize
     return SWC_OK;
 }
 

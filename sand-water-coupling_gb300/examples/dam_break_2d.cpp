@@ -2,11 +2,16 @@
 // reference-shaped class in include/swc/DualParticleSphLiquid.hpp): the 2D dam
 // break (40 x 80 particles at 0.01 in [0,1]^2, two wall layers, gravity,
 // dt 1e-3), advanced `steps` times; prints one line per step.
+//   dam_break_2d <steps> frames <F>: instead, F frames at 100 frames/s through
+//   swc::Simulator (CFL 0.5 substeps, frame files under dam_break_2d_frames/);
+//   prints one line per substep and one per frame.
 #include <cstdio>
 #include <cstdlib>
 #include <random>
+#include <string>
 
 #include "swc/DualParticleSphLiquid.hpp"
+#include "swc/Simulator.hpp"
 
 int main(int argc, char ** argv) {
     const int steps = argc > 1 ? std::atoi(argv[1]) : 10;
@@ -41,6 +46,16 @@ int main(int argc, char ** argv) {
     liquid.addParticles(pos, vel);
     liquid.setBoundary(bpos, bnrm);
     try {
+        if (argc > 3 && std::string(argv[2]) == "frames") {
+            swc::Simulator<swc::DualParticleSphLiquid<2>> sim("dam_break_2d_frames", 0, unsigned(std::atoi(argv[3])) + 1,
+                                                              100, 0.5, &liquid);
+            sim.onSubstep = [&](double dt) {
+                std::printf("substep dt %.17g  cg %d\n", dt, liquid.lastStats().cg_iterations);
+            };
+            sim.onFrame = [](unsigned f) { std::printf("frame %u\n", f); };
+            sim.Simulate();
+            return 0;
+        }
         liquid.initialize();
         for (int s = 0; s < steps; s++) {
             liquid.advance(1e-3);

@@ -9,6 +9,7 @@
 #include <cstdlib>
 
 #include "swc/DEMParticleSand.hpp"
+#include "swc/Simulator.hpp"
 
 namespace {
 
@@ -63,21 +64,11 @@ int main(int argc, char ** argv) {
         sand.initialize();
         const unsigned rate = 10000;
         const double cfl = 0.4, frame = 1.0 / rate;
+        // frames of 1 / rate substepped as Simulator::advanceTimeBySteps does
+        // (Cores/Physics/Simulator.cpp:103-128)
+        swc::Simulator<swc::DEMParticleSand<2>> driver("sand_rotating_box_2d_out", 1, 1, rate, cfl, &sand);
         for (int f = 0; f < frames; f++) {
-            // Simulator::advanceTimeBySteps (Cores/Physics/Simulator.cpp:103-128)
-            double t = 0;
-            int steps = 0;
-            for (bool done = false; !done; steps++) {
-                double dt = sand.getTimeStep(rate, cfl);
-                if (t + dt >= frame) {
-                    dt   = frame - t;
-                    done = true;
-                } else if (t + 2 * dt >= frame) {
-                    dt = (frame - t) / 2;
-                }
-                sand.advance(dt);
-                t += dt;
-            }
+            const int steps = int(driver.advanceTimeBySteps(frame).size());
             const auto & v = sand.velocities();
             double vmax = 0;
             for (size_t i = 0; i < v.size(); i += 2) vmax = std::fmax(vmax, std::hypot(v[i], v[i + 1]));

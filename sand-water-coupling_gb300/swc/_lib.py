@@ -116,6 +116,7 @@ SIGNATURES = {
     "swc_set_volumes": (C.c_int, [_P, _D, C.c_int64]),
     "swc_get_boundary_info": (C.c_int, [_P, _D, _D, C.c_int64]),
     "swc_set_boundary_info": (C.c_int, [_P, _D, _D, C.c_int64]),
+    "swc_get_boundary": (C.c_int, [_P, _D, _D, _D, C.c_int64]),
     "swc_get_scalars": (C.c_int, [_P, _D, _D, _D]),
     "swc_set_scalars": (C.c_int, [_P, C.c_double, C.c_double, C.c_double]),
     "swc_num_virtual": (C.c_int64, [_P]),
@@ -140,6 +141,7 @@ SIGNATURES = {
                                    C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "swc_mlp_gradient_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
                                            C.c_void_p, C.c_void_p]),
+    "swc_debug_fail_alloc": (C.c_int, [C.c_int64]),
     "swc_host_alloc": (C.c_void_p, [C.c_size_t]),
     "swc_host_free": (None, [C.c_void_p]),
     # DEM sand step (include/swc_sand.h)

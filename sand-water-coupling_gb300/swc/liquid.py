@@ -197,6 +197,13 @@ class DualParticleSphLiquid:
         self._check(self.L.swc_get_boundary_info(self.h, _dp(rho), _dp(vol), self.nb), "swc_get_boundary_info")
         return rho, vol
 
+    def getBoundary(self):
+        """Boundary positions, inward normals and velocities as they stand (a moving
+        paddle turns every advance), in the order of setBoundary."""
+        x, n, v = (np.empty((self.nb, self.dim)) for _ in range(3))
+        self._check(self.L.swc_get_boundary(self.h, _dp(x), _dp(n), _dp(v), self.nb), "swc_get_boundary")
+        return x, n, v
+
     def setBoundaryInfo(self, rho, vol):
         rho = _f64(rho, (self.nb,))
         vol = _f64(vol, (self.nb,))

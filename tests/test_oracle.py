@@ -159,3 +159,53 @@ def test_warm_start_prefix_quirk(oracle_mod):
     o.set_pressure(p_star)
     o.project()
     assert cold > 5 and o.stats()["iterations"] <= 1
+
+
+@pytest.mark.parametrize("build", [lambda: scenes.dam_break_2d(seed=4),
+                                   lambda: scenes.projection_block_3d(n=12, seed=4),
+                                   lambda: scenes.paddle_tank_3d(seed=4, cells=(12, 6, 12), domain=(0.24, 0.12, 0.24),
+                                                                 paddle_particles=400, paddle_half=(0.03, 0.01, 0.05))])
+def test_cell_grid_searcher_matches_hash(oracle_mod, build):
+    """The cell-grid searcher (used at full benchmark size) visits the reference
+    hash grid's neighbour sets: identical sorted sets for real, boundary and
+    virtual queries, and every field of two advance steps equal up to FP64
+    rounding of the changed summation order."""
+    s = build().rounded_to_float32()
+    out = {}
+    for kind in ("hash", "cells"):
+        o = oracle_mod.Oracle(s, searcher=kind)
+        if "paddle_omega" in s.meta:
+            moving = np.zeros(s.n_boundary, np.uint8)
+            moving[s.meta["n_walls"]:] = 1
+            o.set_boundary_motion(moving, s.meta["paddle_center"], s.meta["paddle_omega"])
+        o.initialize()
+        for _ in range(2):
+            o.advance(s.dt)
+        rng = np.random.default_rng(0)
+        x, v = o.particles()
+        q = np.concatenate([x[rng.choice(len(x), 200)] + rng.uniform(-0.03, 0.03, (200, s.dim)), x[:50]])
+        nbr = {w: o.neighbors(w, q) for w in ("real", "boundary", "virtual")}
+        out[kind] = (o.virtual(), x, v, nbr, o.stats())
+    (vh, xh, velh, nh, sh), (vc, xc, velc, nc, sc) = out["hash"], out["cells"]
+    for w in nh:
+        for a, b in zip(nh[w], nc[w]):
+            assert np.array_equal(a, b), w
+    assert np.array_equal(vh["node"], vc["node"])
+    for f in ("rho", "vol", "div", "alpha_hat"):
+        np.testing.assert_allclose(vc[f], vh[f], rtol=1e-11, atol=1e-13 * np.abs(vh[f]).max())
+    np.testing.assert_allclose(xc, xh, rtol=0, atol=1e-14)
+    assert np.linalg.norm(velc - velh) / np.linalg.norm(velh) < 1e-9
+    assert abs(sc["iterations"] - sh["iterations"]) <= 1
+
+
+def test_hash_candidates_power_of_two_buckets(oracle_mod):
+    """The reference's hash (OR of three prime products mod 2N) fills few buckets
+    when 2N is a power of two: a 32^3 block (2N = 2^16) visits far more candidates
+    per query than a 31^3 block, while the cell grid visits about 27 cells' worth."""
+    per = {}
+    for n in (31, 32):
+        s = scenes.projection_block_3d(n=n, seed=0)
+        o = oracle_mod.Oracle(s)
+        per[n] = o.hash_candidates("real", s.positions[::7])
+    # 27 cells of side h = 2 spacings hold ~27 * 8 = 216 particles
+    assert per[31] < 20 * 216 < per[32], per
