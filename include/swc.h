@@ -218,8 +218,10 @@ int swc_set_mlp(swc_ctx * ctx, const float * params, const float * norm);
  * the count in *n (<= capacity). */
 int swc_get_features(swc_ctx * ctx, float * features, float * targets, int64_t capacity, int64_t * n);
 
-/* Device-side training of the network (forward on tensor cores, FP32 backward,
- * Adam with FP32 master weights).  The dataset lives in device memory. */
+/* Device-side training of the network: every batch runs one fused tensor-core
+ * pass (forward, backward and weight gradients as BF16 tcgen05 products with
+ * FP32 accumulation; the per-CTA shares of the gradient added in a fixed order)
+ * and an Adam step with FP32 master weights.  The dataset lives in device memory. */
 typedef struct swc_trainer swc_trainer;
 int  swc_trainer_create(int64_t capacity, int32_t batch, swc_trainer ** out);
 void swc_trainer_destroy(swc_trainer * tr);
@@ -230,7 +232,7 @@ int  swc_trainer_get_params(swc_trainer * tr, float * params, float * norm);
  * error of the normalised output after epoch e. */
 int  swc_trainer_fit(swc_trainer * tr, int32_t epochs, float lr, uint64_t seed, float * epoch_loss);
 /* Stateless helpers on host arrays (run on the GPU): predictions, and the loss
- * gradient for one batch. */
+ * gradient for one batch (the mean squared error of the normalised output in *loss). */
 int swc_mlp_forward(const float * params, const float * norm, const float * features, int64_t n, float * out);
 int swc_mlp_gradient(const float * params, const float * norm, const float * features, const float * targets,
                      int64_t n, float * grad, float * loss);
@@ -241,11 +243,13 @@ int swc_mlp_gradient(const float * params, const float * norm, const float * fea
  * (params[SWC_MLP_PARAMS], norm[SWC_MLP_NORM], features[n][SWC_MLP_IN], targets[n],
  * grad[SWC_MLP_PARAMS] and loss[1] out), work is queued on `stream` (NULL: the
  * default stream) and its scratch lives in fixed device arrays for at most
- * SWC_MLP_NOALLOC_MAX_ROWS rows (about 2.7 MB per device, held until the process
+ * SWC_MLP_NOALLOC_MAX_ROWS rows (about 0.7 MB per device, held until the process
  * exits).  n above the limit returns SWC_BAD_ARG.  The first call on a device
- * resolves the arrays' device addresses, so make it before any stream capture.
- * All calls share the arrays: calls that overlap on the GPU race.  A failure of
- * the tensor-core pass shows as loss = NaN. */
+ * resolves the arrays' device addresses and sets the kernel's shared-memory
+ * attribute, so make it before any stream capture; the resolved addresses do
+ * not survive a cudaDeviceReset of that device.  All calls share the arrays:
+ * calls that overlap on the GPU race.  A failure of the tensor-core pass shows
+ * as loss = NaN. */
 #define SWC_MLP_NOALLOC_MAX_ROWS 2048
 int swc_mlp_gradient_noalloc(const float * params, const float * norm, const float * features,
                              const float * targets, int64_t n, float * grad, float * loss, void * stream);

@@ -88,11 +88,22 @@ def forward(params, norm, feats, bf16=False, cache=False):
     return t
 
 
-def loss_and_grad(params, norm, feats, target):
-    """Mean squared error on the normalised output y (target -> (t - t_mean) / t_std)."""
+def loss_and_grad(params, norm, feats, target, bf16=False):
+    """Mean squared error on the normalised output y (target -> (t - t_mean) / t_std)
+    and its gradient.  `bf16=True` rounds where the tensor-core gradient pass
+    does: x, W1, W2, h1 (operands of the forward products and of dW2 / dW1),
+    dz2 (operand of dz1 = dz2 W2 and of dW2) and dz1 (operand of dW1); the
+    rest (biases, silu, the final layer, dy, sums) stays exact."""
     W1, b1, W2, b2, w3, b3 = unpack(params)
     norm = np.asarray(norm, dtype=np.float64)
-    _, (x, z1, h1, z2, h2, y) = forward(params, norm, feats, cache=True)
+    x = (np.asarray(feats, dtype=np.float64) - norm[:N_IN]) / norm[N_IN:2 * N_IN]
+    r = bf16_round if bf16 else (lambda a: a)
+    x, W1r, W2r = r(x), r(W1), r(W2)
+    z1 = x @ W1r.T + b1
+    h1 = r(silu(z1))
+    z2 = h1 @ W2r.T + b2
+    h2 = silu(z2)
+    y = h2 @ w3 + b3
     ty = (np.asarray(target, dtype=np.float64) - norm[2 * N_IN]) / norm[2 * N_IN + 1]
     n = y.shape[0]
     e = y - ty
@@ -100,13 +111,22 @@ def loss_and_grad(params, norm, feats, target):
     dy = 2.0 * e / n
     gw3 = h2.T @ dy
     gb3 = dy.sum()
-    dz2 = np.outer(dy, w3) * dsilu(z2)
+    dz2 = r(np.outer(dy, w3) * dsilu(z2))
     gW2 = dz2.T @ h1
     gb2 = dz2.sum(0)
-    dz1 = (dz2 @ W2) * dsilu(z1)
+    dz1 = r((dz2 @ W2r) * dsilu(z1))
     gW1 = dz1.T @ x
     gb1 = dz1.sum(0)
     return loss, pack(gW1, gb1, gW2, gb2, gw3, gb3)
+
+
+def param_groups():
+    """Slices of the parameter vector: W1, b1, W2, b2, w3, b3."""
+    o, out = 0, {}
+    for name, size in (("W1", N_H * N_IN), ("b1", N_H), ("W2", N_H * N_H), ("b2", N_H), ("w3", N_H), ("b3", 1)):
+        out[name] = slice(o, o + size)
+        o += size
+    return out
 
 
 class Adam:

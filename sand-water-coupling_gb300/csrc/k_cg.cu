@@ -126,32 +126,6 @@ __global__ void __launch_bounds__(kUT) k_cg_direction(const int * __restrict__ b
     }
 }
 
-__device__ __forceinline__ void cp_async16(float * smem_dst, const float * gsrc, bool valid) {
-    const unsigned sa = unsigned(__cvta_generic_to_shared(smem_dst));
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(sa), "l"(gsrc), "r"(valid ? 16 : 0) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-
-// Neighbour-brick table of brick b: tab[(k+1)*9 + (j+1)*3 + (i+1)] = id of brick
-// (bx+i, by+j, bz+k) when it exists and is active, else -1.
-template<int DIM>
-__device__ __forceinline__ void neighbour_table(const Lattice & L, const unsigned char * __restrict__ bflag, int b,
-                                                int * tab) {
-    const int t = threadIdx.x;
-    if (t < 27) {
-        const int3 bc = brick_coords(L, b);
-        const int i = t % 3 - 1, j = (t / 3) % 3 - 1, k = t / 9 - 1;
-        const int x = bc.x + i, y = bc.y + j, z = bc.z + k;
-        int id = -1;
-        if (x >= 0 && x < L.bnx && y >= 0 && y < L.bny && z >= 0 && z < L.bnz && (DIM == 3 || k == 0)) {
-            const int nb = x + L.bnx * (y + L.bny * z);
-            if (bflag[nb]) id = nb;
-        }
-        tab[t] = id;
-    }
-}
-
 // Asynchronous copy of the u halo tile of a brick (16-byte segments, zero-filled
 // outside the active set).
 template<int DIM>

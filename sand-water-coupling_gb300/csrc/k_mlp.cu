@@ -12,122 +12,17 @@
 // (bias, SiLU, final 64-wide dot).  Every wait is bounded: on timeout the kernel
 // records an error, frees its TMEM and returns.
 //
-// Training: the same forward kernel (saving pre-activations), an FP32 backward
-// pass and Adam (FP32 master weights), all deterministic.
-#include <cuda_bf16.h>
-
+// Training: the fused tensor-core gradient pass of k_mlp_train.cu and Adam (FP32
+// master weights), all deterministic.
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 
 #include "../../include/swc.h"
 #include "swc_kernels.h"
+#include "swc_tc.cuh"
 
 namespace swc {
-
-// ---------------------------------------------------------------------------
-// PTX helpers (tcgen05 / TMEM / mbarrier).
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void * p) { return uint32_t(__cvta_generic_to_shared(p)); }
-
-__device__ __forceinline__ void tmem_alloc(uint32_t * dst, uint32_t ncols) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
-                 : "memory");
-}
-__device__ __forceinline__ void tmem_relinquish() {
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-// D (TMEM) = A * B (+ D when accumulate), A/B described in shared memory.
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
-                                         uint32_t accumulate) {
-    asm volatile(
-        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint64_t * mbar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
-                 : "memory");
-}
-__device__ __forceinline__ void mbar_init(uint64_t * mbar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t * mbar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(mbar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t * mbar, uint32_t parity) {
-    for (int i = 0; i < (1 << 22); i++)
-        if (mbar_try_wait(mbar, parity)) return true;
-    return false;
-}
-
-// 16 consecutive FP32 columns of this thread's TMEM lane (warp w reads lanes 32w..32w+31).
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
-#pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
-__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-
-// Shared-memory matrix descriptor: K-major, no swizzle; LBO = byte step between
-// core matrices along K, SBO = byte step between 8-row groups.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    return uint64_t((saddr & 0x3FFFFu) >> 4) | (uint64_t(lbo >> 4) << 16) | (uint64_t(sbo >> 4) << 32) |
-           (uint64_t(1) << 46);
-}
-// Instruction descriptor, kind::f16: BF16 A and B (K-major), FP32 accumulate, M = 128, N = 64.
-constexpr uint32_t kIdescM128N64 = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
-
-// Byte offset of element (r, k) of a K-major bf16 matrix with `kdim` columns.
-__device__ __forceinline__ uint32_t canon_off(int r, int k, int kdim) {
-    return uint32_t((r >> 3) * (kdim / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
-}
-
-// sigma(z) = (1 + tanh(z/2)) / 2 with the hardware tanh approximation (relative
-// error about 2^-11, below the bf16 rounding the activations go through);
-// silu(z) = z sigma(z), silu'(z) = sigma(z) (1 + z (1 - sigma(z))).
-__device__ __forceinline__ float sigmoid_fast(float z) {
-    float t;
-    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
-    return fmaf(0.5f, t, 0.5f);
-}
-__device__ __forceinline__ float silu(float z) { return z * sigmoid_fast(z); }
-__device__ __forceinline__ float dsilu(float z) {
-    const float s = sigmoid_fast(z);
-    return s * (1.f + z * (1.f - s));
-}
-__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
-    return *reinterpret_cast<const uint32_t *>(&v);
-}
-
-constexpr int kMlpIn = SWC_MLP_IN, kMlpH = 64;
-constexpr int kMlpParams = kMlpH * kMlpIn + kMlpH + kMlpH * kMlpH + kMlpH + kMlpH + 1;
-static_assert(kMlpParams == SWC_MLP_PARAMS && 2 * kMlpIn + 2 == SWC_MLP_NORM, "MLP layout");
-static_assert(kMlpIn <= 8, "the X row holds the features in its first 16-byte core-matrix row");
-constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kMlpH * kMlpIn, kOffW2 = kOffB1 + kMlpH, kOffB2 = kOffW2 + kMlpH * kMlpH,
-              kOffW3 = kOffB2 + kMlpH, kOffB3 = kOffW3 + kMlpH;
-constexpr int kMlpNT = 128;  // threads = rows per tile
 
 // Per-node features (the definitions of include/swc.h) from the raw node
 // values D, alpha_hat, n_real, p_base (x after the history warm start), p1
@@ -173,16 +68,8 @@ enum { kMlpFromArray = 0, kMlpFromNodes = 1 };
 constexpr uint32_t kMlpTmemCols = 64;
 constexpr int kMlpMaxCtasPerSm  = 512 / int(kMlpTmemCols);
 
-// tanh with the hardware approximation (relative error about 2^-11).
-__device__ __forceinline__ float tanh_fast(float h) {
-    float t;
-    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
-    return t;
-}
-
 // params: FP32 vector (layout above); norm: f_mean[kMlpIn], f_std[kMlpIn], t_mean, t_std.
-// kMlpFromArray: rows of feat[n][kMlpIn] -> out[n] (prediction t); with SAVE,
-//   the pre-activations z1, z2 and h1 (bf16-rounded) for training.
+// kMlpFromArray: rows of feat[n][kMlpIn] -> out[n] (prediction t).
 // kMlpFromNodes: rows = the slots of the active bricks in brick order (slot
 //   blist[r / BN] * BN + r % BN, contiguous within a brick); writes the warm
 //   start x[s] = p_base + t s sD / alpha_hat into N.x at active nodes.
@@ -192,11 +79,10 @@ __device__ __forceinline__ float tanh_fast(float h) {
 // tanh and one FMA; bias, SiLU and the final dot run as packed FP32x2 pairs.
 // The X tile aliases the first 4 KB of the H1 tile: X is dead once layer 1
 // completes, H1 once layer 2 completes.
-template<int MODE, bool SAVE>
+template<int MODE>
 __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
     k_mlp_forward(long long n, const float * __restrict__ params, const float * __restrict__ norm,
-                  const float * __restrict__ feat, float * __restrict__ out, float * __restrict__ z1s,
-                  float * __restrict__ h1s, float * __restrict__ z2s, NodeArrays N, const int * __restrict__ blist,
+                  const float * __restrict__ feat, float * __restrict__ out, NodeArrays N, const int * __restrict__ blist,
                   const int * __restrict__ bcount, int bn_log2, const int * __restrict__ nv,
                   const double * __restrict__ bb, FeatScale F0, int * __restrict__ err) {
     pdl_wait_and_release();
@@ -340,12 +226,6 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
                 const float2 h = add2(make_float2(z[2 * i], z[2 * i + 1]), sb1[c]);
                 const float2 a = fma2(h, make_float2(tanh_fast(h.x), tanh_fast(h.y)), h);
                 pk[i]          = pack_bf16(a.x, a.y);
-                if (SAVE && valid) {
-                    const __nv_bfloat162 hv = *reinterpret_cast<const __nv_bfloat162 *>(&pk[i]);
-                    *reinterpret_cast<float2 *>(z1s + row * kMlpH + 2 * c) = make_float2(2.f * h.x, 2.f * h.y);
-                    *reinterpret_cast<float2 *>(h1s + row * kMlpH + 2 * c) =
-                        make_float2(__bfloat162float(hv.x), __bfloat162float(hv.y));
-                }
             }
             *reinterpret_cast<uint4 *>(sh + canon_off(tid, cblk * 16, kMlpH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
             *reinterpret_cast<uint4 *>(sh + canon_off(tid, cblk * 16 + 8, kMlpH)) =
@@ -377,8 +257,6 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
             for (int i = 0; i < 8; i++) {
                 const int c    = cblk * 8 + i;
                 const float2 h = add2(make_float2(z[2 * i], z[2 * i + 1]), sb2[c]);
-                if (SAVE && valid)
-                    *reinterpret_cast<float2 *>(z2s + row * kMlpH + 2 * c) = make_float2(2.f * h.x, 2.f * h.y);
                 const float2 a = fma2(h, make_float2(tanh_fast(h.x), tanh_fast(h.y)), h);
                 y2             = fma2(sw3[c], a, y2);
             }
@@ -402,92 +280,8 @@ __global__ void __launch_bounds__(kMlpNT, kMlpMaxCtasPerSm)
 }
 
 // ---------------------------------------------------------------------------
-// Training: backward pass (FP32) and Adam.
-// Loss = mean over the batch of (y - (t - t_mean)/t_std)^2 on the normalised output.
+// Training (the gradient pass is in k_mlp_train.cu).
 // ---------------------------------------------------------------------------
-// Per-row part: dz2 = 2 (y - ty)/B * w3 * silu'(z2); dz1 = (W2^T dz2) * silu'(z1).
-__global__ void __launch_bounds__(128) k_mlp_backward_rows(long long n, const float * __restrict__ params,
-                                                           const float * __restrict__ norm,
-                                                           const float * __restrict__ pred,
-                                                           const float * __restrict__ target,
-                                                           const float * __restrict__ z1s,
-                                                           const float * __restrict__ z2s, float * __restrict__ dz1,
-                                                           float * __restrict__ dz2, float * __restrict__ dy_out,
-                                                           float * __restrict__ sq_err) {
-    __shared__ float w2t[kMlpH][kMlpH + 1];
-    __shared__ float w3[kMlpH];
-    for (int e = threadIdx.x; e < kMlpH * kMlpH; e += blockDim.x) w2t[e % kMlpH][e / kMlpH] = params[kOffW2 + e];
-    if (threadIdx.x < kMlpH) w3[threadIdx.x] = params[kOffW3 + threadIdx.x];
-    __syncthreads();
-    const float tm = norm[2 * kMlpIn], ts = norm[2 * kMlpIn + 1];
-    for (long long r = blockIdx.x * (long long) blockDim.x + threadIdx.x; r < n; r += (long long) gridDim.x * blockDim.x) {
-        const float y  = (pred[r] - tm) / ts;
-        const float ty = (target[r] - tm) / ts;
-        const float e  = y - ty;
-        sq_err[r]      = e * e;
-        const float dy = 2.f * e / float(n);
-        dy_out[r]      = dy;
-        float d2[kMlpH];
-#pragma unroll
-        for (int o = 0; o < kMlpH; o++) {
-            d2[o]                 = dy * w3[o] * dsilu(z2s[r * kMlpH + o]);
-            dz2[r * kMlpH + o]    = d2[o];
-        }
-#pragma unroll 4
-        for (int i = 0; i < kMlpH; i++) {
-            float a = 0.f;
-#pragma unroll
-            for (int o = 0; o < kMlpH; o++) a = fmaf(w2t[i][o], d2[o], a);  // (W2^T dz2)_i = sum_o W2[o][i] dz2[o]
-            dz1[r * kMlpH + i] = a * dsilu(z1s[r * kMlpH + i]);
-        }
-    }
-}
-
-// Weight gradients, one block per output unit o (rows summed in a fixed order):
-//   gW2[o][i] = sum_r dz2[r][o] h1[r][i]   gb2[o] = sum_r dz2[r][o]
-//   gW1[o][k] = sum_r dz1[r][o] x[r][k]    gb1[o] = sum_r dz1[r][o]
-//   gw3[o]    = sum_r dy[r] silu(z2[r][o]) gb3 = sum_r dy[r] (block 0)
-__global__ void __launch_bounds__(128) k_mlp_grad_weights(long long n, const float * __restrict__ norm,
-                                                          const float * __restrict__ feat,
-                                                          const float * __restrict__ h1s,
-                                                          const float * __restrict__ z2s,
-                                                          const float * __restrict__ dz1,
-                                                          const float * __restrict__ dz2,
-                                                          const float * __restrict__ dy, float * __restrict__ grad) {
-    const int o = blockIdx.x;
-    __shared__ float red[128][kMlpH + kMlpIn + 4];
-    float acc[kMlpH + kMlpIn + 4];
-#pragma unroll
-    for (int k = 0; k < kMlpH + kMlpIn + 4; k++) acc[k] = 0.f;
-    for (long long r = threadIdx.x; r < n; r += blockDim.x) {
-        const float g2 = dz2[r * kMlpH + o], g1 = dz1[r * kMlpH + o];
-#pragma unroll
-        for (int i = 0; i < kMlpH; i++) acc[i] = fmaf(g2, h1s[r * kMlpH + i], acc[i]);
-#pragma unroll
-        for (int k = 0; k < kMlpIn; k++) {
-            const float xk = (feat[r * kMlpIn + k] - norm[k]) / norm[kMlpIn + k];
-            acc[kMlpH + k] = fmaf(g1, __bfloat162float(__float2bfloat16_rn(xk)), acc[kMlpH + k]);
-        }
-        acc[kMlpH + kMlpIn] += g2;
-        acc[kMlpH + kMlpIn + 1] += g1;
-        acc[kMlpH + kMlpIn + 2] = fmaf(dy[r], silu(z2s[r * kMlpH + o]), acc[kMlpH + kMlpIn + 2]);
-        acc[kMlpH + kMlpIn + 3] += dy[r];
-    }
-#pragma unroll
-    for (int k = 0; k < kMlpH + kMlpIn + 4; k++) red[threadIdx.x][k] = acc[k];
-    __syncthreads();
-    for (int k = threadIdx.x; k < kMlpH + kMlpIn + 4; k += blockDim.x) {
-        float s = 0.f;
-        for (int t = 0; t < 128; t++) s += red[t][k];
-        if (k < kMlpH) grad[kOffW2 + o * kMlpH + k] = s;
-        else if (k < kMlpH + kMlpIn) grad[kOffW1 + o * kMlpIn + (k - kMlpH)] = s;
-        else if (k == kMlpH + kMlpIn) grad[kOffB2 + o] = s;
-        else if (k == kMlpH + kMlpIn + 1) grad[kOffB1 + o] = s;
-        else if (k == kMlpH + kMlpIn + 2) grad[kOffW3 + o] = s;
-        else if (o == 0) grad[kOffB3] = s;
-    }
-}
-
 // Adam (Kingma & Ba) with bias correction, FP32 master weights.
 __global__ void k_adam(float * __restrict__ p, const float * __restrict__ g, float * __restrict__ m,
                        float * __restrict__ v, int count, float lr, float b1, float b2, float eps, float bc1,
@@ -594,20 +388,30 @@ void launch_gather_rows(const float * src, const float * src_t, const int * idx,
 struct MlpLaunch {
     int per_sm = 0;
     size_t dyn = 0;
+    int sms    = 152;
 };
 // Residency is computed from the kernel's registers and shared memory and the
-// SM's limits (the occupancy calculator is only consulted as a cross-check and
-// reported on stderr when it disagrees).
-template<int MODE, bool SAVE>
+// SM's limits.  The CUDA occupancy calculator is not used: for kernels that
+// contain tcgen05.alloc it returns 1 CTA per SM for every block size and
+// dynamic shared memory size (measured on GB300 with driver 580; it answers
+// normally for the kernels without tensor-memory allocation), while the hardware
+// runs the CTAs the registers and shared memory allow (ncu: ~40% of the 64 warps
+// active at 4 warps per CTA, i.e. ~6 resident CTAs per SM).  The shape is cached
+// per device; host threads share the cache under a lock.
+template<int MODE>
 static MlpLaunch mlp_launch_shape() {
-    static MlpLaunch shape;
-    if (shape.per_sm) return shape;
-    auto kern = k_mlp_forward<MODE, SAVE>;
+    static std::mutex mu;
+    static MlpLaunch cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MlpLaunch{1, 0};
+    std::lock_guard<std::mutex> lock(mu);
+    if (cache[dev].per_sm) return cache[dev];
+    auto kern = k_mlp_forward<MODE>;
     MlpLaunch s;
     s.per_sm = 1;
-    int dev = 0, regs_sm = 65536, smem_sm = 233472, reserved = 1024, threads_sm = 2048;
+    int regs_sm = 65536, smem_sm = 233472, reserved = 1024, threads_sm = 2048, sms = 152;
     cudaFuncAttributes fa{};
-    if (cudaGetDevice(&dev) == cudaSuccess && cudaFuncGetAttributes(&fa, kern) == cudaSuccess) {
+    if (cudaFuncGetAttributes(&fa, kern) == cudaSuccess) {
         cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
         cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
         cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
@@ -621,62 +425,36 @@ static MlpLaunch mlp_launch_shape() {
         while (fit(s.dyn) > kMlpMaxCtasPerSm) s.dyn += 1024;  // pad until TMEM cannot be oversubscribed
         s.per_sm = std::max(1, fit(s.dyn));
         if (s.dyn) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(s.dyn));
-        int occ          = 0;
-        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kMlpNT, s.dyn);
-        if (e != cudaSuccess || occ != s.per_sm)
-            fprintf(stderr, "swc: k_mlp_forward residency %d CTAs/SM (occupancy calculator: %d, %s)\n", s.per_sm, occ,
-                    cudaGetErrorString(e));
     }
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 152;
+    s.sms = sms;
     cudaGetLastError();
-    shape = s;
-    return shape;
-}
-static int num_sms_cached() {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 152;
-    }
-    return sms;
+    cache[dev] = s;
+    return s;
 }
 // Persistent grid: every resident CTA slot once, never more CTAs than tiles.
-template<int MODE, bool SAVE>
+template<int MODE>
 static void launch_forward(long long rows_max, const float * params, const float * norm, const float * feat,
-                           float * out, float * z1s, float * h1s, float * z2s, const NodeArrays & N,
-                           const int * blist, const int * bcount, int bn_log2, const int * nv, const double * bb,
-                           const FeatScale & F, int * err, cudaStream_t st) {
-    const MlpLaunch s     = mlp_launch_shape<MODE, SAVE>();
+                           float * out, const NodeArrays & N, const int * blist, const int * bcount, int bn_log2,
+                           const int * nv, const double * bb, const FeatScale & F, int * err, cudaStream_t st) {
+    const MlpLaunch s     = mlp_launch_shape<MODE>();
     const long long tiles = std::max<long long>(1, (rows_max + kMlpNT - 1) / kMlpNT);
-    const int grid        = int(std::min<long long>(tiles, (long long) s.per_sm * num_sms_cached()));
-    launch_pdl(k_mlp_forward<MODE, SAVE>, grid, kMlpNT, s.dyn, st, rows_max, params, norm, feat, out, z1s, h1s, z2s, N,
-                                                           blist, bcount, bn_log2, nv, bb, F, err);
+    const int grid        = int(std::min<long long>(tiles, (long long) s.per_sm * s.sms));
+    launch_pdl(k_mlp_forward<MODE>, grid, kMlpNT, s.dyn, st, rows_max, params, norm, feat, out, N, blist, bcount,
+               bn_log2, nv, bb, F, err);
 }
 void launch_mlp_forward_array(long long n, const float * params, const float * norm, const float * feat, float * out,
-                              float * z1s, float * h1s, float * z2s, int * err, cudaStream_t st) {
+                              int * err, cudaStream_t st) {
     if (n <= 0) return;
-    if (z1s || h1s || z2s)
-        launch_forward<kMlpFromArray, true>(n, params, norm, feat, out, z1s, h1s, z2s, NodeArrays{}, nullptr, nullptr,
-                                            0, nullptr, nullptr, FeatScale{}, err, st);
-    else
-        launch_forward<kMlpFromArray, false>(n, params, norm, feat, out, nullptr, nullptr, nullptr, NodeArrays{},
-                                             nullptr, nullptr, 0, nullptr, nullptr, FeatScale{}, err, st);
+    launch_forward<kMlpFromArray>(n, params, norm, feat, out, NodeArrays{}, nullptr, nullptr, 0, nullptr, nullptr,
+                                  FeatScale{}, err, st);
 }
 void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const BrickArrays & B,
                               int bn_log2, long long slots_max, const double * bb, float inv_alpha0, float inv_rho0,
                               float inv_nreal, int * err, cudaStream_t st) {
     FeatScale F{0.f, inv_alpha0, inv_rho0, inv_nreal};
-    launch_forward<kMlpFromNodes, false>(slots_max, params, norm, nullptr, nullptr, nullptr, nullptr, nullptr, N, B.list,
-                                         B.count, bn_log2, B.seg_off + B.nseg, bb, F, err, st);
-}
-void launch_mlp_backward(long long n, const float * params, const float * norm, const float * feat,
-                         const float * pred, const float * target, const float * z1s, const float * h1s,
-                         const float * z2s, float * dz1, float * dz2, float * dy, float * sq_err, float * grad,
-                         cudaStream_t st) {
-    if (n <= 0) return;
-    const int g = int(std::min<long long>((n + 127) / 128, 152 * 8));
-    k_mlp_backward_rows<<<g, 128, 0, st>>>(n, params, norm, pred, target, z1s, z2s, dz1, dz2, dy, sq_err);
-    k_mlp_grad_weights<<<kMlpH, 128, 0, st>>>(n, norm, feat, h1s, z2s, dz1, dz2, dy, grad);
+    launch_forward<kMlpFromNodes>(slots_max, params, norm, nullptr, nullptr, N, B.list, B.count, bn_log2,
+                                  B.seg_off + B.nseg, bb, F, err, st);
 }
 void launch_adam(float * p, const float * g, float * m, float * v, int count, float lr, float b1, float b2, float eps,
                  float bc1, float bc2, cudaStream_t st) {

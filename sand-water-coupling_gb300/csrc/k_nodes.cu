@@ -132,7 +132,8 @@ __global__ void __launch_bounds__(128, 5) k_node_gather(Lattice L, Phys P, const
                                                     const float4 * __restrict__ bpos,
                                                     const float4 * __restrict__ bvel,
                                                     const int * __restrict__ bcellStart,
-                                                    const unsigned char * __restrict__ bnear, int * queue) {
+                                                    const unsigned char * __restrict__ bnear,
+                                                    const unsigned char * __restrict__ bcell, int * queue) {
     pdl_wait_and_release();
     using G          = BrickGeom<DIM>;
     constexpr int NX = 2;
@@ -143,16 +144,32 @@ __global__ void __launch_bounds__(128, 5) k_node_gather(Lattice L, Phys P, const
     for (int bi = queue_take(queue, &slot); bi < nb; bi = queue_take(queue, &slot)) {
         const int b     = blist[bi];
         const int3 bc   = brick_coords(L, b);
-        const int npass = bnear[b] ? 2 : 1;  // boundary particles only near walls
+        const bool walls = bnear[b] != 0;  // boundary particles only near walls
         for (int l4 = threadIdx.x; l4 < TPB; l4 += blockDim.x) {
             const int lx0 = (l4 % XS) * NX, ly = (l4 / XS) % G::BY, lz = l4 / (XS * G::BY);
             const int x0 = bc.x * G::BX + lx0, y = bc.y * G::BY + ly, z = bc.z * G::BZ + lz;
             const long long s0 = (long long) b * G::BN + lx0 + G::BX * (ly + G::BY * lz);
             const bool row_in = y < L.ny && (DIM == 2 || z < L.nz);
+            // and, per node pair, only when a node's cell is within reach of the boundary
+            int npass = 1;
+            if (walls && row_in && x0 < L.nx) {
+                const long long c0 = (long long) x0 + (long long) L.nx * (y + (long long) L.ny * z);
+                if (bcell[c0] || (x0 + 1 < L.nx && bcell[c0 + 1])) npass = 2;
+            }
             NodeSums2 a;
             a.wsum = a.rhoI = a.VI = a.cnt = a.ux = a.uy = a.uz = a.bw = a.dvg = a.gx = a.gy = a.gz = f2(0.f);
-            const float xn0 = L.ox + x0 * L.dx, yn = L.oy + y * L.dx, zn = DIM == 3 ? L.oz + z * L.dx : 0.f;
-            const float2 xn = make_float2(xn0, L.ox + (x0 + 1) * L.dx);
+            // node positions of the FP64 lattice (the oracle's nodes) as float-float
+            // pairs: x_I - x_j = (hi - x_j) + lo is then exact to a few ulp of the
+            // offset, where an FP32 node position would carry ~1e-7 of rounding
+            float2 xn, xl, yzn, yzl;
+            {
+                const double xd0 = L.ox_d + x0 * L.dx_d, xd1 = L.ox_d + (x0 + 1) * L.dx_d, yd = L.oy_d + y * L.dx_d,
+                             zd = DIM == 3 ? L.oz_d + z * L.dx_d : 0.0;
+                xn  = make_float2(float(xd0), float(xd1));
+                xl  = make_float2(float(xd0 - double(xn.x)), float(xd1 - double(xn.y)));
+                yzn = make_float2(float(yd), float(zd));
+                yzl = make_float2(float(yd - double(yzn.x)), float(zd - double(yzn.y)));
+            }
             const int cxa = max(x0 + P.cell_lo, 0), cxb = min(x0 + NX - 1 + P.cell_hi, L.nx - 1);
             const int cy0 = max(y + P.cell_lo, 0), cy1 = min(y + P.cell_hi, L.ny - 1);
             const int cz0 = DIM == 3 ? max(z + P.cell_lo, 0) : 0, cz1 = DIM == 3 ? min(z + P.cell_hi, L.nz - 1) : 0;
@@ -182,12 +199,27 @@ __global__ void __launch_bounds__(128, 5) k_node_gather(Lattice L, Phys P, const
                         for (int j = jb; j < je; j++) {
                             const float4 p = pn, u = un;
                             if (j + 1 < je) pn = X[j + 1], un = U[j + 1];
-                            const float dy  = yn - p.y, dz = zn - p.z;
-                            const float ryz = dy * dy + dz * dz;
-                            if (ryz >= P.h2) continue;
-                            const float2 dxx = add2(xn, f2(-p.x));
+                            const float2 dyz = add2(add2(yzn, make_float2(-p.y, -p.z)), yzl);
+                            const float dy = dyz.x, dz = DIM == 3 ? dyz.y : 0.f;
+                            const float ryz = fmaf(dz, dz, dy * dy);
+                            if (ryz >= P.h2 + P.tie2) continue;
+                            const float2 dxx = add2(add2(xn, f2(-p.x)), xl);
                             const float2 r2  = fma2(dxx, dxx, f2(ryz));
-                            const bool m0 = r2.x < P.h2, m1 = r2.y < P.h2;
+                            const float2 e2  = add2(r2, f2(-P.h2));
+                            bool m0 = e2.x < 0.f, m1 = e2.y < 0.f;
+                            if (pass == 0 && fminf(fabsf(e2.x), fabsf(e2.y)) < P.tie2) {
+                                // rho_I sums W_H cut at h, which jumps there: membership
+                                // within rounding of r = h is decided in FP64 from the
+                                // exact positions, as the oracle's strict |d|^2 < h^2
+                                // (summed x, y, z in the oracle's order)
+                                const double xd0 = L.ox_d + x0 * L.dx_d, xd1 = L.ox_d + (x0 + 1) * L.dx_d;
+                                const double yd = L.oy_d + y * L.dx_d, zd = DIM == 3 ? L.oz_d + z * L.dx_d : 0.0;
+                                const double hh = P.h_d * P.h_d, ey = double(p.y) - yd, ez = double(p.z) - zd;
+                                const double e0 = double(p.x) - xd0, e1 = double(p.x) - xd1;
+                                const double s0 = fma(ey, ey, e0 * e0), s1 = fma(ey, ey, e1 * e1);
+                                m0 = (DIM == 3 ? fma(ez, ez, s0) : s0) < hh;
+                                m1 = (DIM == 3 ? fma(ez, ez, s1) : s1) < hh;
+                            }
                             if (!(m0 || m1)) continue;
                             if (pass == 0) pair_add<true, FAST_H>(a, P, dxx, dy, dz, r2, m0, m1, p, u);
                             else pair_add<false, FAST_H>(a, P, dxx, dy, dz, r2, m0, m1, p, u);
@@ -580,7 +612,8 @@ __global__ void __launch_bounds__(kGradNT) k_pressure_gradient(Lattice L, Phys P
                                                            const float4 * __restrict__ bpos,
                                                            const float4 * __restrict__ bvel,
                                                            const float4 * __restrict__ bnrm,
-                                                           const int * __restrict__ bcellStart, int * queue) {
+                                                           const int * __restrict__ bcellStart,
+                                                           const unsigned char * __restrict__ bcell, int * queue) {
     pdl_wait_and_release();
     using G = BrickGeom<DIM>;
     // Row pitch 24 in 3D: a warp's particles span about four consecutive cell
@@ -633,9 +666,14 @@ __global__ void __launch_bounds__(kGradNT) k_pressure_gradient(Lattice L, Phys P
         __syncthreads();
         const int total  = rinc[ROWS - 1];
         const bool walls = bnear[b] != 0;
-        // tile origin (node coordinates of tile index 0)
-        const float tox = float(x0 - G::HALO), toy = float(bc.y * G::BY - G::HALO);
-        const float toz = DIM == 3 ? float(bc.z * G::BZ - G::HALO) : 0.f;
+        // tile origin (node of tile index 0) of the FP64 lattice as float-float
+        // pairs: a particle's offset from it, (q - hi) - lo, is exact to a few ulp
+        // (the tile spans 16 nodes), where (q - origin) / dx - index would carry
+        // the FP32 rounding of q - origin (~1e-7 at |q| ~ 2)
+        const double tod_x = L.ox_d + (x0 - G::HALO) * L.dx_d, tod_y = L.oy_d + (bc.y * G::BY - G::HALO) * L.dx_d;
+        const double tod_z = DIM == 3 ? L.oz_d + (bc.z * G::BZ - G::HALO) * L.dx_d : 0.0;
+        const float tox = float(tod_x), toy = float(tod_y), toz = float(tod_z);
+        const float tlx = float(tod_x - double(tox)), tly = float(tod_y - double(toy)), tlz = float(tod_z - double(toz));
         for (int p = t; p < total; p += kGradNT) {
             int lo = 0, hi = ROWS - 1;
             while (lo < hi) {
@@ -646,8 +684,8 @@ __global__ void __launch_bounds__(kGradNT) k_pressure_gradient(Lattice L, Phys P
             const int j     = rbeg[lo] + p;
             const float4 q  = pos[j];
             const float4 vi = vel[j];
-            const float ux = (q.x - L.ox) * L.inv_dx - tox, uy = (q.y - L.oy) * L.inv_dx - toy;
-            const float uz = DIM == 3 ? (q.z - L.oz) * L.inv_dx - toz : 0.f;
+            const float ux = ((q.x - tox) - tlx) * L.inv_dx, uy = ((q.y - toy) - tly) * L.inv_dx;
+            const float uz = DIM == 3 ? ((q.z - toz) - tlz) * L.inv_dx : 0.f;
             float3 f = make_float3(0.f, 0.f, 0.f);
             const bool inside = ux >= 3.f && ux < float(G::TX) - 4.f && uy >= 3.f && uy < float(G::TY) - 4.f &&
                                 (DIM == 2 || (uz >= 3.f && uz < float(G::TZ) - 4.f));
@@ -681,7 +719,8 @@ __global__ void __launch_bounds__(kGradNT) k_pressure_gradient(Lattice L, Phys P
             } else {
                 f = gradient_virtual_global<DIM>(L, P, bflag, N, q);
             }
-            if (walls) {
+            // the wall sum only for particles whose cell is within reach of the boundary
+            if (walls && bcell[cell_linear(L, cell_of<DIM>(L, q.x, q.y, q.z))]) {
                 const float3 w = wall_term<DIM>(L, P, bcellStart, bpos, bvel, bnrm, q, vi);
                 f.x += w.x;
                 f.y += w.y;
@@ -704,9 +743,10 @@ template<int DIM>
 void launch_pressure_gradient(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
                               const int * plist, const int * pcount, const unsigned char * bnear, const float4 * pos,
                               float4 * vel, const int * cellStart, const float4 * bpos, const float4 * bvel,
-                              const float4 * bnrm, const int * bcellStart, int grid, int * queue, cudaStream_t st) {
+                              const float4 * bnrm, const int * bcellStart, const unsigned char * bcell, int grid,
+                              int * queue, cudaStream_t st) {
     launch_pdl(k_pressure_gradient<DIM>, grid, kGradNT, 0, st, L, P, B.flag, N, plist, pcount, bnear, pos, vel, cellStart, bpos,
-                                                   bvel, bnrm, bcellStart, queue);
+                                                   bvel, bnrm, bcellStart, bcell, queue);
 }
 template<int DIM> int pressure_gradient_blocks_per_sm() {
     int n = 0;
@@ -728,15 +768,15 @@ void launch_brick_list(const unsigned char * bflag, int nbricks, int * list, int
 template<int DIM>
 void launch_node_gather(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
                         const float4 * pos, const float4 * vel, const int * cellStart, const float4 * bpos,
-                        const float4 * bvel, const int * bcellStart, const unsigned char * bnear, int grid,
-                        int * queue, cudaStream_t st) {
+                        const float4 * bvel, const int * bcellStart, const unsigned char * bnear,
+                        const unsigned char * bcell, int grid, int * queue, cudaStream_t st) {
     // H >= 2h: particles within h only reach the inner branch of W_H
     if (double(P.H) >= 2.0 * double(P.h) * (1.0 - 1e-6))
         launch_pdl(k_node_gather<DIM, true>, grid, 128, 0, st, L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel,
-                                                       bcellStart, bnear, queue);
+                                                       bcellStart, bnear, bcell, queue);
     else
         launch_pdl(k_node_gather<DIM, false>, grid, 128, 0, st, L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel,
-                                                        bcellStart, bnear, queue);
+                                                        bcellStart, bnear, bcell, queue);
 }
 
 template<int DIM>
@@ -797,11 +837,12 @@ void launch_zero_active(const Lattice & L, const BrickArrays & B, float * a, int
 #define SWC_INST(D)                                                                                                    \
     template void launch_node_gather<D>(const Lattice &, const Phys &, const BrickArrays &, const NodeArrays &,        \
                                         const float4 *, const float4 *, const int *, const float4 *, const float4 *,   \
-                                        const int *, const unsigned char *, int, int *, cudaStream_t);                 \
+                                        const int *, const unsigned char *, const unsigned char *, int, int *,         \
+                                        cudaStream_t);                                                                 \
     template void launch_pressure_gradient<D>(const Lattice &, const Phys &, const BrickArrays &, const NodeArrays &,  \
                                               const int *, const int *, const unsigned char *, const float4 *,         \
                                               float4 *, const int *, const float4 *, const float4 *, const float4 *,   \
-                                              const int *, int, int *, cudaStream_t);                                  \
+                                              const int *, const unsigned char *, int, int *, cudaStream_t);           \
     template int pressure_gradient_blocks_per_sm<D>();                                                                 \
     template int node_gather_blocks_per_sm<D>();                                                                       \
     template void launch_segments<D>(const Lattice &, const BrickArrays &, const NodeArrays &, int *, int,             \

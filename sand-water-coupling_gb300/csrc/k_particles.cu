@@ -437,6 +437,36 @@ __global__ void __launch_bounds__(256) k_mark_bricks(Lattice L, const int * __re
     }
 }
 
+// Cells within reach of the boundary: near[c] = 1 when some boundary particle is
+// binned within R cells of cell c along every axis (a box dilation of the
+// boundary's occupancy, done axis by axis).  The x pass reads the occupancy of
+// the whole x-range from the row's prefix sums; the y / z passes OR R cells on
+// either side.  With R = ceil(h / dx) + 1 a particle (or node) whose cell is not
+// flagged has no boundary particle within h.
+template<int DIM>
+__global__ void __launch_bounds__(256) k_near_x(Lattice L, const int * __restrict__ cellStart, int R,
+                                                unsigned char * __restrict__ out) {
+    pdl_wait_and_release();
+    for (long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x; c < L.ncells;
+         c += (long long) gridDim.x * blockDim.x) {
+        const int x = int(c % L.nx);
+        const long long row = c - x;
+        out[c] = cellStart[row + min(x + R, L.nx - 1) + 1] > cellStart[row + max(x - R, 0)] ? 1 : 0;
+    }
+}
+__global__ void __launch_bounds__(256) k_near_dilate(long long ncells, long long stride, int extent, int R,
+                                                     const unsigned char * __restrict__ in,
+                                                     unsigned char * __restrict__ out) {
+    pdl_wait_and_release();
+    for (long long c = blockIdx.x * (long long) blockDim.x + threadIdx.x; c < ncells;
+         c += (long long) gridDim.x * blockDim.x) {
+        const int k = int((c / stride) % extent);
+        unsigned char v = 0;
+        for (int d = max(-R, -k); d <= min(R, extent - 1 - k); d++) v |= in[c + d * stride];
+        out[c] = v;
+    }
+}
+
 // Rigid motion of boundary particles flagged as moving (paddle): rotation about
 // the y axis through c with angular velocity omega; v_b = omega x (x - c).
 // The moving flag travels with the particle in bnrm.w (1 = moving).
@@ -776,6 +806,24 @@ void launch_mark_bricks(const int * cellStart, long long n, const Lattice & L, c
     const long long b = (L.nbricks + 7) / 8;  // eight warps per block, one warp per brick
     launch_pdl(k_mark_bricks<DIM>, int(std::min<long long>(b, 152LL * 64)), 256, 0, st, L, cellStart, reach, bflag, pflag);
 }
+template<int DIM>
+void launch_near_cells(const int * cellStart, long long n, const Lattice & L, const Phys & P, unsigned char * near,
+                       unsigned char * tmp, cudaStream_t st) {
+    if (n <= 0 || L.ncells <= 0) {
+        cudaMemsetAsync(near, 0, size_t(L.ncells), st);
+        return;
+    }
+    const int R = int(std::ceil(double(P.h) / double(L.dx))) + 1;
+    const int g = int(std::min<long long>((L.ncells + 255) / 256, 152LL * 16));
+    // 3D: x -> near, y: near -> tmp, z: tmp -> near; 2D: x -> tmp, y: tmp -> near
+    unsigned char * xo = DIM == 3 ? near : tmp;
+    launch_pdl(k_near_x<DIM>, g, 256, 0, st, L, cellStart, R, xo);
+    launch_pdl(k_near_dilate, g, 256, 0, st, L.ncells, (long long) L.nx, L.ny, R, (const unsigned char *) xo,
+               DIM == 3 ? tmp : near);
+    if (DIM == 3)
+        launch_pdl(k_near_dilate, g, 256, 0, st, L.ncells, (long long) L.nx * L.ny, L.nz, R, (const unsigned char *) tmp,
+                   near);
+}
 void launch_rotate_boundary(float4 * bpos, float4 * bvel, float4 * bnrm, long long nb, float cx, float cz,
                             float omega, float dt, cudaStream_t st) {
     if (nb > 0) k_rotate_boundary<<<grid_for(nb, 256), 256, 0, st>>>(bpos, bvel, bnrm, nb, cx, cz, omega, dt);
@@ -818,6 +866,8 @@ void launch_debug_neighbors(int which, long long nq, const double * q, const Lat
                                    const int *, float, int *, cudaStream_t);                                           \
     template void launch_boundary_density<D>(float4 *, float4 *, float *, long long, const Lattice &, const Phys &,    \
                                              const int *, cudaStream_t);                                               \
+    template void launch_near_cells<D>(const int *, long long, const Lattice &, const Phys &, unsigned char *,         \
+                                       unsigned char *, cudaStream_t);                                                 \
     template void launch_mark_bricks<D>(const int *, long long, const Lattice &, const Phys &, unsigned char *,        \
                                         unsigned char *,                                                               \
                                         cudaStream_t);                                                                 \

@@ -93,6 +93,8 @@ struct swc_ctx {
     int *           plist = nullptr;
     int *           pcount = nullptr;
     unsigned char * bnear = nullptr;  // bricks within reach of boundary particles
+    unsigned char * bcell = nullptr;  // node cells within reach of boundary particles
+    unsigned char * bcell_tmp = nullptr;
     // learned warm start / training-data logging
     float * mlp_params = nullptr;  // SWC_MLP_PARAMS
     float * mlp_norm   = nullptr;  // SWC_MLP_NORM
@@ -267,6 +269,10 @@ void setup_phys(swc_ctx * c) {
     coeffs(H, P.inv_H, P.c0H, P.c1H);
     P.h_d     = h;
     P.inv_h_d = 1 / h;
+    // |d|^2 within tie2 of h^2 is re-decided in FP64 where a jump at h matters
+    // (rho_I sums W_H cut at h): a few relative roundings of the FP32 square,
+    // whose offsets come from float-float node positions
+    P.tie2 = float(8e-6 * h * h);
     P.c0h_d   = std::numbers::inv_pi * (1 / (h * h)) * (dim == 2 ? 40.0 / 7 : 8 * (1 / h));
     P.mass    = float(s.mass);
     P.inv_mass = float(1.0 / s.mass);
@@ -302,6 +308,7 @@ template<int DIM> int run_bin_real(swc_ctx * c, float advect_dt = 0.f) {
 template<int DIM> int run_bin_boundary(swc_ctx * c) {
     launch_bin<DIM>(c->L, c->nb, c->bpos, c->bvel, c->bnrm, c->bid, c->sortB, c->bcellStart, 0.f, c->stream);
     launch_mark_bricks<DIM>(c->bcellStart, c->nb, c->L, c->P, c->bnear, nullptr, c->stream);
+    launch_near_cells<DIM>(c->bcellStart, c->nb, c->L, c->P, c->bcell, c->bcell_tmp, c->stream);
     return SWC_OK;
 }
 
@@ -316,7 +323,7 @@ template<int DIM> void run_generate(swc_ctx * c, bool with_ahat) {
     launch_brick_list(c->B.flag, c->L.nbricks, c->B.list, c->B.count, c->stream);
     launch_brick_list(c->pflag, c->L.nbricks, c->plist, c->pcount, c->stream);
     launch_node_gather<DIM>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel, c->bcellStart,
-                            c->bnear, c->ggrid, c->queues, c->stream);
+                            c->bnear, c->bcell, c->ggrid, c->queues, c->stream);
     launch_segments<DIM>(c->L, c->B, c->N, c->scan_tiles, c->grid, c->stream);
     if (with_ahat) launch_ahat<DIM>(c->L, c->P, c->B, c->N, c->S, c->sgrid, c->stream);
 }
@@ -541,7 +548,8 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     }
     mark(c, 6);
     launch_pressure_gradient<DIM>(c->L, c->P, c->B, c->N, c->plist, c->pcount, c->bnear, c->pos, c->vel,
-                                  c->cellStart, c->bpos, c->bvel, c->bnrm, c->bcellStart, c->pgrid, c->queues + 2, c->stream);
+                                  c->cellStart, c->bpos, c->bvel, c->bnrm, c->bcellStart, c->bcell, c->pgrid, c->queues + 2,
+                                  c->stream);
     mark(c, 7);
     // p in reference order (the next step's prefix warm start) and N_v for it;
     // other modes skip it (a switch to the prefix mode exports the last solution)
@@ -789,7 +797,8 @@ int swc_create(const swc_scene * s, const swc_solver_opts * o, swc_ctx ** out) {
         (rc = dalloc(c, &c->scan_tiles, scan_tile_count(std::max<long long>(c->B.nseg, L.ncells) + 1) + 2)) ||
         (rc = dalloc(c, &c->cg, 1)) || (rc = dalloc(c, &c->partials, npart)) || (rc = dalloc(c, &c->queues, 4)) ||
         (rc = dalloc(c, &c->diag_bits, 1)) || (rc = dalloc(c, &c->max_bits, 1)) || (rc = dalloc(c, &c->res2, 2)) ||
-        (rc = dalloc(c, &c->cellStart, L.ncells + 1)) || (rc = dalloc(c, &c->bcellStart, L.ncells + 1)))
+        (rc = dalloc(c, &c->cellStart, L.ncells + 1)) || (rc = dalloc(c, &c->bcellStart, L.ncells + 1)) ||
+        (rc = dalloc(c, &c->bcell, L.ncells)) || (rc = dalloc(c, &c->bcell_tmp, L.ncells)))
         return fail(rc);
     if (cudaMallocHost(reinterpret_cast<void **>(&c->hcg), sizeof(HostCg)) != cudaSuccess) return fail(SWC_OUT_OF_MEMORY);
     cudaMemsetAsync(c->cg, 0, sizeof(CgState), c->stream);
@@ -801,6 +810,8 @@ int swc_create(const swc_scene * s, const swc_solver_opts * o, swc_ctx ** out) {
     cudaMemsetAsync(c->N.x, 0, slots * sizeof(float), c->stream);
     cudaMemsetAsync(c->nv_prev, 0, sizeof(int), c->stream);
     cudaMemsetAsync(c->bcellStart, 0, sizeof(int) * (L.ncells + 1), c->stream);
+    cudaMemsetAsync(c->bnear, 0, L.nbricks, c->stream);
+    cudaMemsetAsync(c->bcell, 0, L.ncells, c->stream);
     for (auto & e : c->ev) cudaEventCreate(&e);
     cudaEventCreate(&c->evA);
     cudaEventCreate(&c->evB);
@@ -869,6 +880,8 @@ void swc_destroy(swc_ctx * c) {
     dfree(c->plist);
     dfree(c->pcount);
     dfree(c->bnear);
+    dfree(c->bcell);
+    dfree(c->bcell_tmp);
     dfree(c->pcomp);
     dfree(c->nv_prev);
     dfree(c->scan_tiles);
@@ -1364,12 +1377,12 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
             case 6: launch_cg_direction<3>(c->B, c->N, c->cg, c->grid, c->stream); break;
             case 2:
                 launch_node_gather<3>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel,
-                                      c->bcellStart, c->bnear, c->ggrid, c->queues, c->stream);
+                                      c->bcellStart, c->bnear, c->bcell, c->ggrid, c->queues, c->stream);
                 break;
             case 3:
                 launch_pressure_gradient<3>(c->L, c->P, c->B, c->N, c->plist, c->pcount, c->bnear, c->pos, c->vel,
-                                            c->cellStart, c->bpos, c->bvel, c->bnrm, c->bcellStart, c->pgrid, c->queues + 2,
-                                            c->stream);
+                                            c->cellStart, c->bpos, c->bvel, c->bnrm, c->bcellStart, c->bcell, c->pgrid,
+                                            c->queues + 2, c->stream);
                 break;
             case 4: launch_density<3>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->pleft, c->stream); break;
             case 5: launch_forces<3>(c->pos, c->vel, c->vel2, c->n, c->L, c->P, c->cellStart, 0.f, c->pleft, c->stream); break;
@@ -1378,7 +1391,7 @@ int swc_time_kernel(swc_ctx * c, int which, int reps, double * mean_ms) {
             switch (which) {
             case 2:
                 launch_node_gather<2>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel,
-                                      c->bcellStart, c->bnear, c->ggrid, c->queues, c->stream);
+                                      c->bcellStart, c->bnear, c->bcell, c->ggrid, c->queues, c->stream);
                 break;
             case 4: launch_density<2>(c->pos, c->vel, c->rho, c->n, c->L, c->P, c->cellStart, c->pleft, c->stream); break;
             default: break;

@@ -55,6 +55,7 @@ struct Phys {
     float h, h2, inv_h, c0h, c1h;   // real / boundary kernel, support h = 4 r
     float H, H2, inv_H, c0H, c1H;   // virtual kernel, support H = 4 * grid spacing
     double h_d, inv_h_d, c0h_d;     // FP64 copies for the activation re-test
+    float tie2;                     // band around h^2 of an FP64 re-test of membership within h
     float mass, bmass, inv_mass;
     float rho0, kappa, alpha0;
     int   cell_lo, cell_hi;         // node-centred cell window for a radius-h query

@@ -106,6 +106,11 @@ template<int DIM>
 // bricks holding their cells); n = 0 clears the flags
 void launch_mark_bricks(const int * cellStart, long long n, const Lattice & L, const Phys & P, unsigned char * bflag,
                         unsigned char * pflag, cudaStream_t st);
+// cells within reach (h) of the particles binned in cellStart, one byte per node
+// cell (a box dilation by ceil(h / dx) + 1 cells; tmp: scratch of the same size)
+template<int DIM>
+void launch_near_cells(const int * cellStart, long long n, const Lattice & L, const Phys & P, unsigned char * near,
+                       unsigned char * tmp, cudaStream_t st);
 template<int DIM>
 void launch_debug_neighbors(int which, long long nq, const double * q, const Lattice & L, const Phys & P,
                             const float4 * pos, const int * id, const int * cellStart, const unsigned char * bflag,
@@ -117,15 +122,16 @@ void launch_brick_list(const unsigned char * bflag, int nbricks, int * list, int
 template<int DIM>
 void launch_node_gather(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
                         const float4 * pos, const float4 * vel, const int * cellStart, const float4 * bpos,
-                        const float4 * bvel, const int * bcellStart, const unsigned char * bnear, int grid,
-                        int * queue, cudaStream_t st);
+                        const float4 * bvel, const int * bcellStart, const unsigned char * bnear,
+                        const unsigned char * bcell, int grid, int * queue, cudaStream_t st);
 // Pressure-gradient update over the bricks that hold particles (plist / pcount),
 // node field staged per brick in shared memory; bnear flags bricks near walls.
 template<int DIM>
 void launch_pressure_gradient(const Lattice & L, const Phys & P, const BrickArrays & B, const NodeArrays & N,
                               const int * plist, const int * pcount, const unsigned char * bnear, const float4 * pos,
                               float4 * vel, const int * cellStart, const float4 * bpos, const float4 * bvel,
-                              const float4 * bnrm, const int * bcellStart, int grid, int * queue, cudaStream_t st);
+                              const float4 * bnrm, const int * bcellStart, const unsigned char * bcell, int grid,
+                              int * queue, cudaStream_t st);
 // Resident blocks per SM of the persistent brick kernels (their grids are
 // SMs x this; gather and gradient take bricks from a zero-initialised queue of
 // two ints).
@@ -197,7 +203,7 @@ void launch_true_residual(const Lattice & L, const BrickArrays & B, const NodeAr
 
 // ---- k_mlp.cu (learned warm start) ----
 void launch_mlp_forward_array(long long n, const float * params, const float * norm, const float * feat, float * out,
-                              float * z1s, float * h1s, float * z2s, int * err, cudaStream_t st);
+                              int * err, cudaStream_t st);
 // node mode: every slot of the active bricks (inactive slots are skipped), the
 // active-node count at B.seg_off[B.nseg]
 void launch_mlp_forward_nodes(const float * params, const float * norm, const NodeArrays & N, const BrickArrays & B,
@@ -206,10 +212,17 @@ void launch_mlp_forward_nodes(const float * params, const float * norm, const No
 void launch_node_features(const NodeArrays & N, const int * slot_of, const int * nv, long long rows_max,
                           const CgState * cg, float inv_alpha0, float inv_rho0, float inv_nreal, float * feat_out,
                           cudaStream_t st);
-void launch_mlp_backward(long long n, const float * params, const float * norm, const float * feat,
-                         const float * pred, const float * target, const float * z1s, const float * h1s,
-                         const float * z2s, float * dz1, float * dz2, float * dy, float * sq_err, float * grad,
-                         cudaStream_t st);
+// Loss gradient of one batch on the tensor cores (k_mlp_train.cu): `ctas` CTAs
+// (mlp_train_ctas(n)) write their shares into share (mlp_train_share_floats(ctas)
+// floats), a second kernel adds them in order into grad[SWC_MLP_PARAMS] and the
+// mean squared error into *loss (NaN with *err set on a tensor-core timeout).
+// Returns nonzero when a launch failed.
+constexpr int kMlpTrainShare = 128 * 80 + 64 + 2;  // floats of one CTA's share (D, dw3, db3, loss)
+int    mlp_train_ctas(long long n);
+size_t mlp_train_share_floats(int ctas);
+int    launch_mlp_train_grad(long long n, const float * params, const float * norm, const float * feat,
+                             const float * target, float * share, int ctas, int * err, float * grad, float * loss,
+                             cudaStream_t st);
 void launch_adam(float * p, const float * g, float * m, float * v, int count, float lr, float b1, float b2, float eps,
                  float bc1, float bc2, cudaStream_t st);
 template<int DIM>

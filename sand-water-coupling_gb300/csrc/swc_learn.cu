@@ -1,7 +1,8 @@
 // swc_learn.cu -- device-side training of the learned CG warm start and the
 // stateless forward / gradient helpers of the C ABI (include/swc.h).  The
-// dataset stays in device memory; every batch runs the tensor-core forward
-// (saving pre-activations), the FP32 backward and an Adam step.
+// dataset stays in device memory; every batch runs the fused tensor-core
+// gradient pass (k_mlp_train.cu: forward, backward and weight gradients as
+// tcgen05 BF16 products with FP32 accumulation) and an Adam step.
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -25,7 +26,8 @@ struct swc_trainer {
     float *feat = nullptr, *tgt = nullptr;                       // dataset
     float *params = nullptr, *norm = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr;
     float *bfeat = nullptr, *btgt = nullptr, *pred = nullptr;    // batch
-    float *z1 = nullptr, *h1 = nullptr, *z2 = nullptr, *dz1 = nullptr, *dz2 = nullptr, *dy = nullptr, *sq = nullptr;
+    float *share = nullptr, *loss = nullptr;                     // per-CTA gradient shares, batch loss
+    int    ctas  = 1;
     int *  idx = nullptr, *err = nullptr;
     long long adam_t = 0;
 };
@@ -40,10 +42,15 @@ template<class T> void tfree(T *& p) {
     p = nullptr;
 }
 
-int forward_batch(swc_trainer * t, const float * feat, long long n, float * out, bool save) {
-    launch_mlp_forward_array(n, t->params, t->norm, feat, out, save ? t->z1 : nullptr, save ? t->h1 : nullptr,
-                             save ? t->z2 : nullptr, t->err, t->st);
+int forward_batch(swc_trainer * t, const float * feat, long long n, float * out) {
+    launch_mlp_forward_array(n, t->params, t->norm, feat, out, t->err, t->st);
     return cudaGetLastError() == cudaSuccess ? SWC_OK : SWC_CUDA_ERROR;
+}
+// loss gradient of one batch (features / targets on the device) into t->grad, t->loss
+int gradient_batch(swc_trainer * t, const float * feat, const float * tgt, long long n) {
+    return launch_mlp_train_grad(n, t->params, t->norm, feat, tgt, t->share, t->ctas, t->err, t->grad, t->loss, t->st)
+               ? SWC_CUDA_ERROR
+               : SWC_OK;
 }
 
 int check_err(swc_trainer * t) {
@@ -64,12 +71,13 @@ int swc_trainer_create(int64_t capacity, int32_t batch, swc_trainer ** out) {
     t->cap   = capacity;
     t->batch = batch;
     const size_t B = size_t(batch);
+    t->ctas = mlp_train_ctas(batch);
     bool ok = cudaStreamCreateWithFlags(&t->st, cudaStreamNonBlocking) == cudaSuccess;
     ok = ok && talloc(&t->feat, size_t(capacity) * kIn) && talloc(&t->tgt, size_t(capacity)) && talloc(&t->params, kP) &&
          talloc(&t->norm, kN) && talloc(&t->m, kP) && talloc(&t->v, kP) && talloc(&t->grad, kP) &&
-         talloc(&t->bfeat, B * kIn) && talloc(&t->btgt, B) && talloc(&t->pred, B) && talloc(&t->z1, B * kH) &&
-         talloc(&t->h1, B * kH) && talloc(&t->z2, B * kH) && talloc(&t->dz1, B * kH) && talloc(&t->dz2, B * kH) &&
-         talloc(&t->dy, B) && talloc(&t->sq, B) && talloc(&t->idx, size_t(capacity)) && talloc(&t->err, 1);
+         talloc(&t->bfeat, B * kIn) && talloc(&t->btgt, B) && talloc(&t->pred, B) &&
+         talloc(&t->share, mlp_train_share_floats(t->ctas)) && talloc(&t->loss, 1) &&
+         talloc(&t->idx, size_t(capacity)) && talloc(&t->err, 1);
     if (!ok) {
         swc_trainer_destroy(t);
         return SWC_OUT_OF_MEMORY;
@@ -86,7 +94,7 @@ void swc_trainer_destroy(swc_trainer * t) {
     if (!t) return;
     if (t->st) cudaStreamSynchronize(t->st);
     for (float ** p : {&t->feat, &t->tgt, &t->params, &t->norm, &t->m, &t->v, &t->grad, &t->bfeat, &t->btgt, &t->pred,
-                       &t->z1, &t->h1, &t->z2, &t->dz1, &t->dz2, &t->dy, &t->sq})
+                       &t->share, &t->loss})
         tfree(*p);
     tfree(t->idx);
     tfree(t->err);
@@ -141,10 +149,7 @@ int swc_trainer_fit(swc_trainer * t, int32_t epochs, float lr, uint64_t seed, fl
         for (long long b0 = 0; b0 < t->n; b0 += t->batch) {
             const long long nb = std::min<long long>(t->batch, t->n - b0);
             launch_gather_rows(t->feat, t->tgt, t->idx + b0, nb, t->bfeat, t->btgt, t->st);
-            int rc = forward_batch(t, t->bfeat, nb, t->pred, true);
-            if (rc) return rc;
-            launch_mlp_backward(nb, t->params, t->norm, t->bfeat, t->pred, t->btgt, t->z1, t->h1, t->z2, t->dz1,
-                                t->dz2, t->dy, t->sq, t->grad, t->st);
+            if (int rc = gradient_batch(t, t->bfeat, t->btgt, nb)) return rc;
             t->adam_t++;
             const float bc1 = 1.f - std::pow(b1, float(t->adam_t)), bc2 = 1.f - std::pow(b2, float(t->adam_t));
             launch_adam(t->params, t->grad, t->m, t->v, kP, lr, b1, b2, eps, bc1, bc2, t->st);
@@ -155,7 +160,7 @@ int swc_trainer_fit(swc_trainer * t, int32_t epochs, float lr, uint64_t seed, fl
             pred_h.resize(t->n);
             for (long long b0 = 0; b0 < t->n; b0 += t->batch) {
                 const long long nb = std::min<long long>(t->batch, t->n - b0);
-                int rc = forward_batch(t, t->feat + b0 * kIn, nb, t->pred, false);
+                int rc = forward_batch(t, t->feat + b0 * kIn, nb, t->pred);
                 if (rc) return rc;
                 cudaMemcpyAsync(pred_h.data() + b0, t->pred, sizeof(float) * nb, cudaMemcpyDeviceToHost, t->st);
             }
@@ -185,7 +190,7 @@ int swc_mlp_forward(const float * params, const float * norm, const float * f, i
     std::vector<float> tmp;
     for (long long b0 = 0; b0 < n && !rc; b0 += t->batch) {
         const long long nb = std::min<long long>(t->batch, n - b0);
-        rc = forward_batch(t, t->feat + b0 * kIn, nb, t->pred, false);
+        rc = forward_batch(t, t->feat + b0 * kIn, nb, t->pred);
         cudaMemcpyAsync(out + b0, t->pred, sizeof(float) * nb, cudaMemcpyDeviceToHost, t->st);
     }
     if (!rc) rc = check_err(t);
@@ -205,21 +210,11 @@ int swc_mlp_gradient(const float * params, const float * norm, const float * f, 
     }
     cudaMemcpy(t->bfeat, f, sizeof(float) * kIn * n, cudaMemcpyHostToDevice);
     cudaMemcpy(t->btgt, y, sizeof(float) * n, cudaMemcpyHostToDevice);
-    rc = forward_batch(t, t->bfeat, n, t->pred, true);
-    if (!rc) {
-        launch_mlp_backward(n, t->params, t->norm, t->bfeat, t->pred, t->btgt, t->z1, t->h1, t->z2, t->dz1, t->dz2,
-                            t->dy, t->sq, t->grad, t->st);
-        rc = check_err(t);
-    }
+    rc = gradient_batch(t, t->bfeat, t->btgt, n);
+    if (!rc) rc = check_err(t);
     if (!rc) {
         cudaMemcpy(grad, t->grad, sizeof(float) * kP, cudaMemcpyDeviceToHost);
-        if (loss) {
-            std::vector<float> sq(n);
-            cudaMemcpy(sq.data(), t->sq, sizeof(float) * n, cudaMemcpyDeviceToHost);
-            double s = 0;
-            for (float e : sq) s += e;
-            *loss = float(s / double(n));
-        }
+        if (loss) cudaMemcpy(loss, t->loss, sizeof(float), cudaMemcpyDeviceToHost);
     }
     swc_trainer_destroy(t);
     return rc;

@@ -6,15 +6,18 @@
 // (fixed arenas, no allocator calls between steps), code running under a memory
 // budget that a late allocation could exceed, or a plugin that must not change
 // the process's allocation pattern.  swc_mlp_gradient allocates its scratch on
-// every call; swc_mlp_gradient_noalloc keeps the same scratch (pre-activations,
-// per-row gradients, predictions, an error flag) in file-scope device arrays
-// sized for SWC_MLP_NOALLOC_MAX_ROWS rows, and only launches kernels.
+// every call; swc_mlp_gradient_noalloc keeps the same scratch (the per-CTA
+// gradient shares of the tensor-core pass and an error flag) in file-scope
+// device arrays sized for SWC_MLP_NOALLOC_MAX_ROWS rows, and only launches
+// kernels.
 //
 // The arrays exist once per device that loads this library and live until the
-// process exits (about 2.7 MB).  Every call reuses them and they keep the last
-// call's contents; nothing in them needs to start at zero except the error flag,
-// which each call clears.  Calls that overlap on the GPU (different streams, or
-// the same arrays used by two host threads at once) race on the scratch.
+// process exits (about 0.7 MB).  Every call reuses them and they keep the last
+// call's contents; the shares are overwritten in full by each call and only the
+// error flag needs to start at zero, which each call clears.  Calls that overlap
+// on the GPU (different streams, or the same arrays used by two host threads at
+// once) race on the scratch.  The device addresses of the arrays are looked up
+// once per device; they do not survive a cudaDeviceReset of that device.
 #include <algorithm>
 #include <mutex>
 
@@ -25,23 +28,16 @@ namespace swc {
 
 namespace {
 
-constexpr int kRows = SWC_MLP_NOALLOC_MAX_ROWS;
-constexpr int kHid  = 64;
+constexpr int kRows  = SWC_MLP_NOALLOC_MAX_ROWS;
+constexpr int kShare = ((kRows + 127) / 128) * kMlpTrainShare;  // one share per 128-row tile at most
 
 // Scratch of one gradient evaluation (device memory, never allocated at run time).
-static __device__ __align__(256) float g_z1[kRows * kHid];
-static __device__ __align__(256) float g_h1[kRows * kHid];
-static __device__ __align__(256) float g_z2[kRows * kHid];
-static __device__ __align__(256) float g_dz1[kRows * kHid];
-static __device__ __align__(256) float g_dz2[kRows * kHid];
-static __device__ __align__(256) float g_pred[kRows];
-static __device__ __align__(256) float g_dy[kRows];
-static __device__ __align__(256) float g_sq[kRows];
+static __device__ __align__(256) float g_share[kShare];
 static __device__ __align__(256) int g_err;
 
 struct ScratchPtrs {
-    float *z1, *h1, *z2, *dz1, *dz2, *pred, *dy, *sq;
-    int *  err;
+    float * share;
+    int *   err;
 };
 
 constexpr int kMaxDevices = 64;
@@ -57,14 +53,7 @@ int scratch_for_current_device(ScratchPtrs & out) {
     std::lock_guard<std::mutex> lock(g_mutex);
     if (!g_ready[dev]) {
         ScratchPtrs p{};
-        if (cudaGetSymbolAddress(reinterpret_cast<void **>(&p.z1), g_z1) != cudaSuccess ||
-            cudaGetSymbolAddress(reinterpret_cast<void **>(&p.h1), g_h1) != cudaSuccess ||
-            cudaGetSymbolAddress(reinterpret_cast<void **>(&p.z2), g_z2) != cudaSuccess ||
-            cudaGetSymbolAddress(reinterpret_cast<void **>(&p.dz1), g_dz1) != cudaSuccess ||
-            cudaGetSymbolAddress(reinterpret_cast<void **>(&p.dz2), g_dz2) != cudaSuccess ||
-            cudaGetSymbolAddress(reinterpret_cast<void **>(&p.pred), g_pred) != cudaSuccess ||
-            cudaGetSymbolAddress(reinterpret_cast<void **>(&p.dy), g_dy) != cudaSuccess ||
-            cudaGetSymbolAddress(reinterpret_cast<void **>(&p.sq), g_sq) != cudaSuccess ||
+        if (cudaGetSymbolAddress(reinterpret_cast<void **>(&p.share), g_share) != cudaSuccess ||
             cudaGetSymbolAddress(reinterpret_cast<void **>(&p.err), g_err) != cudaSuccess)
             return SWC_CUDA_ERROR;
         g_ptrs[dev]  = p;
@@ -72,21 +61,6 @@ int scratch_for_current_device(ScratchPtrs & out) {
     }
     out = g_ptrs[dev];
     return SWC_OK;
-}
-
-// loss = mean of the per-row squared errors (single block, fixed order); an
-// error of the tensor-core forward pass turns the loss into NaN.
-__global__ void k_noalloc_loss(long long n, float * __restrict__ loss) {
-    __shared__ double red[256];
-    double s = 0;
-    for (long long i = threadIdx.x; i < n; i += 256) s += g_sq[i];
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *loss = g_err ? __int_as_float(0x7fc00000) : float(red[0] / double(n));
 }
 
 }  // namespace
@@ -102,11 +76,11 @@ extern "C" int swc_mlp_gradient_noalloc(const float * d_params, const float * d_
     ScratchPtrs s{};
     int rc = scratch_for_current_device(s);
     if (rc) return rc;
+    const int ctas = mlp_train_ctas(n);
+    if (mlp_train_share_floats(ctas) > size_t(kShare)) return SWC_BAD_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(s.err, 0, sizeof(int), st) != cudaSuccess) return SWC_CUDA_ERROR;
-    launch_mlp_forward_array(n, d_params, d_norm, d_features, s.pred, s.z1, s.h1, s.z2, s.err, st);
-    launch_mlp_backward(n, d_params, d_norm, d_features, s.pred, d_targets, s.z1, s.h1, s.z2, s.dz1, s.dz2, s.dy, s.sq,
-                        d_grad, st);
-    k_noalloc_loss<<<1, 256, 0, st>>>(n, d_loss);
-    return cudaGetLastError() == cudaSuccess ? SWC_OK : SWC_CUDA_ERROR;
+    return launch_mlp_train_grad(n, d_params, d_norm, d_features, d_targets, s.share, ctas, s.err, d_grad, d_loss, st)
+               ? SWC_CUDA_ERROR
+               : SWC_OK;
 }

@@ -219,6 +219,33 @@ __device__ __forceinline__ void stencil_row(const float * tile, int ly, int lz, 
 // Halo tile of the CG SpMV: x halo 4 (16-byte aligned rows), y/z halo 3 (the
 // stencil reach), pitch chosen so the 8 rows read by a quarter-warp's LDS.128
 // hit distinct banks.
+__device__ __forceinline__ void cp_async16(float * smem_dst, const float * gsrc, bool valid) {
+    const unsigned sa = unsigned(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(sa), "l"(gsrc), "r"(valid ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// cp.async 16-byte copies (zero-filled when !valid) and their groups.
+// Neighbour-brick table of brick b: tab[(k+1)*9 + (j+1)*3 + (i+1)] = id of brick
+// (bx+i, by+j, bz+k) when it exists and is active, else -1.
+template<int DIM>
+__device__ __forceinline__ void neighbour_table(const Lattice & L, const unsigned char * __restrict__ bflag, int b,
+                                                int * tab) {
+    const int t = threadIdx.x;
+    if (t < 27) {
+        const int3 bc = brick_coords(L, b);
+        const int i = t % 3 - 1, j = (t / 3) % 3 - 1, k = t / 9 - 1;
+        const int x = bc.x + i, y = bc.y + j, z = bc.z + k;
+        int id = -1;
+        if (x >= 0 && x < L.bnx && y >= 0 && y < L.bny && z >= 0 && z < L.bnz && (DIM == 3 || k == 0)) {
+            const int nb = x + L.bnx * (y + L.bny * z);
+            if (bflag[nb]) id = nb;
+        }
+        tab[t] = id;
+    }
+}
+
 template<int DIM> struct SpmvTile {
     using G = BrickGeom<DIM>;
     static constexpr int HX = 4, HY = 3, HZ = DIM == 3 ? 3 : 0;

@@ -5,7 +5,7 @@ correction of the pressure extrapolated in time from the node's previous
 pressures, in units of sD / alpha_hat_I (see include/swc.h for the feature
 definitions).  Training data are logged by the plain solver started from that
 extrapolated pressure (CG to the configured tolerance); training runs on the GPU
-through swc_trainer_* (tensor-core forward, FP32 backward, Adam).  A trained
+through swc_trainer_* (one fused tensor-core pass for the gradient, Adam).  A trained
 model is a pair (params[N_PARAMS], norm[N_NORM]) stored in an .npz file.
 """
 from __future__ import annotations

@@ -1,10 +1,11 @@
 """GPU parity at the benchmark workloads' own sizes: the CUDA path through the C ABI
 against the FP64 oracle (VirtualParticle.cpp:18-201, DualParticleSphLiquid.cpp:112-126).
 
-Per-step replay, as in test_gpu_parity.py: before the compared step the oracle is
-handed the GPU's state (particles, V_i, boundary particles as they stand, rho_b /
-V_b, rho0, alpha0, kappa), so a comparison measures one step of the path and not
-the divergence of two chaotic FP32 / FP64 trajectories.
+Per-step replay: before the compared step the oracle is handed the GPU's state
+(particles, V_i, boundary particles as they stand, rho_b / V_b, rho0, alpha0,
+kappa), so a comparison measures one step of the path and not the divergence of
+two chaotic FP32 / FP64 trajectories; after its own move (checked against the
+GPU's to 1e-6) it projects the GPU's moved positions (see replay).
 
   2D dam break, 3,200 particles: all 200 steps replayed, both solvers starting CG
       from the same vector (the reference's stale prefix of the GPU's last
@@ -19,6 +20,8 @@ the divergence of two chaotic FP32 / FP64 trajectories.
 For the learned steps the oracle's CG starts from the GPU's solution: its FP64
 residual must already be near the tolerance (the oracle then adds a few
 iterations at most), and the velocity update compared is the one of that pressure.
+The plain steps start both solvers from the same stale-prefix vector and compare
+their iteration counts.
 
 Bars (FP32 state and sums against FP64): identical active virtual sets; rho_I,
 V_I, alpha_hat 2e-5 relative; D_I 1e-4 of max |D|; vbar_I and post-projection
@@ -87,17 +90,33 @@ def compare(liq, ref, st, tol, label):
             "gpu_iterations": st["cg_iterations"], "oracle_iterations": ref.stats()["iterations"]}
 
 
-def replay_from_gpu_solution(liq, ref, s, label, boundary=False):
-    """One advance on both sides, the oracle's CG started from the GPU's solution."""
+def replay(liq, ref, s, label, start, boundary=False):
+    """One advance on both sides from the GPU's pre-step state.  The oracle moves
+    the particles and applies gravity and viscosity itself (FP64), then takes the
+    GPU's moved positions (and boundary) before its projection, so that both
+    project the same positions: the FP32 rounding of the move is checked on its
+    own (1e-6) and cannot flip a neighbour at r = h, where rho_I's W_H cut at h
+    jumps.  start: "prefix" hands the oracle the GPU's previous solution as the
+    stale-prefix warm start (the same CG iteration from the same vector), "gpu"
+    the GPU's solution of this step."""
     sync(liq, ref, boundary)
+    p_prev = liq.virtual()["p"]
     st = liq.advance(s.dt)
-    assert st["status"] == 0, st
-    ref.set_pressure(liq.virtual()["p"])
-    ref.advance(s.dt)
+    assert st["status"] == 0, (label, st)
+    ref.move_and_forces(s.dt)
+    xg, _ = liq.getParticles()
+    xo, vo = ref.particles()
+    np.testing.assert_allclose(xg, xo, rtol=0, atol=1e-6)
+    ref.set_particles(xg, vo)
+    if boundary:
+        xb, nb, vb = liq.getBoundary()
+        ref.set_boundary(xb, nb, vb)
+    ref.set_pressure(p_prev if start == "prefix" else liq.virtual()["p"])
+    ref.project()
     out = compare(liq, ref, st, s.tolerance, label)
-    # the GPU's pressure is converged in FP64 too: the oracle has little left to do
-    assert out["oracle_iterations"] <= max(5, out["gpu_iterations"]), (label, out)
-    print(f"\n{label}: {out}")
+    if start == "gpu":
+        # the GPU's pressure is converged in FP64 too: the oracle has little left to do
+        assert out["oracle_iterations"] <= max(5, out["gpu_iterations"]), (label, out)
     return out
 
 
@@ -111,12 +130,7 @@ def test_dam_break_2d_all_200_steps(swc_mod, oracle_mod):
     worst = {"velocity": 0.0, "vbar": 0.0, "fp64_residual_of_gpu_p": 0.0}
     it_diff = []
     for step in range(s.steps):
-        sync(liq, ref)
-        ref.set_pressure(liq.virtual()["p"] if step else np.zeros(0))  # the same stale-prefix start
-        st = liq.advance(s.dt)
-        assert st["status"] == 0, (step, st)
-        ref.advance(s.dt)
-        out = compare(liq, ref, st, s.tolerance, f"step {step}")
+        out = replay(liq, ref, s, f"step {step}", "prefix")
         for k in worst:
             worst[k] = max(worst[k], out[k])
         it_diff.append(out["gpu_iterations"] - out["oracle_iterations"])
@@ -134,12 +148,7 @@ def test_dam_break_3d_524k(swc_mod, oracle_mod):
     for _ in range(10):
         assert liq.advance(s.dt)["status"] == 0
     ref = oracle_mod.Oracle(s, searcher="cells")
-    sync(liq, ref)
-    ref.set_pressure(liq.virtual()["p"])  # the same stale-prefix start on both sides
-    st = liq.advance(s.dt)
-    assert st["status"] == 0
-    ref.advance(s.dt)
-    out = compare(liq, ref, st, s.tolerance, "3D dam break 524,288")
+    out = replay(liq, ref, s, "3D dam break 524,288, step 11", "prefix")
     assert abs(out["gpu_iterations"] - out["oracle_iterations"]) <= 1, out
     print(f"\n3D dam break, step 11: {out}")
 
@@ -153,7 +162,7 @@ def test_projection_block_2m(swc_mod, oracle_mod):
     for _ in range(5):
         assert liq.advance(s.dt)["status"] == 0
     ref = oracle_mod.Oracle(s, searcher="cells")
-    replay_from_gpu_solution(liq, ref, s, "projection block 2,097,152, step 6")
+    print(f"\n{replay(liq, ref, s, 'projection block 2,097,152, step 6', 'gpu')}")
 
 
 def test_paddle_tank(swc_mod, oracle_mod):
@@ -172,4 +181,4 @@ def test_paddle_tank(swc_mod, oracle_mod):
     moving = np.zeros(s.n_boundary, np.uint8)
     moving[s.meta["n_walls"]:] = 1
     ref.set_boundary_motion(moving, s.meta["paddle_center"], s.meta["paddle_omega"])
-    replay_from_gpu_solution(liq, ref, s, label, boundary=True)
+    print(f"\n{label}: {replay(liq, ref, s, label, 'gpu', boundary=True)}")
