@@ -361,6 +361,57 @@ def run_sand_leg(args, torch, stream, hbm, peak_kind, with_cpu):
     return out
 
 
+def host_link(torch, stream, nbytes, reps=10):
+    """The host link's own copy rate (pinned host <-> device, one direction at a
+    time, CUDA events) for the e2e step's byte count, and the time its copies
+    take at that rate."""
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, (dst, src) in (("h2d", (d, h)), ("d2h", (h, d))):
+        with torch.cuda.stream(stream):
+            dst.copy_(src, non_blocking=True)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                dst.copy_(src, non_blocking=True)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        out[f"{name}_GBps"] = nbytes * reps / (e0.elapsed_time(e1) / 1e3) / 1e9
+    out["copy_ms_at_link_rate"] = 1e3 * nbytes * (1 / out["h2d_GBps"] + 1 / out["d2h_GBps"]) / 1e9
+    del h, d
+    return out
+
+
+def run_training_leg(args, torch, epochs=2):
+    """The learned warm start's training path on the tensor cores: the loss-gradient
+    pass alone (rows of seeded synthetic features, CUDA events) and Adam epochs
+    through the trainer (wall clock, the dataset resident on the device)."""
+    from swc import learn
+
+    rng = np.random.default_rng(0)
+
+    def data(n):
+        f = rng.normal(size=(n, learn.N_IN)).astype(np.float32)
+        return f, (np.tanh(f[:, 0]) + 0.5 * f[:, 4]).astype(np.float32)
+
+    f, t = data(args.train_rows)
+    norm = learn.normalisation(f, t)
+    p = learn.init_params(1)
+    for _ in range(3):
+        g, loss = learn.gradient(p, norm, f, t)  # host arrays in and out (allocating helper)
+    out = {"gradient_rows": args.train_rows, "loss": float(loss)}
+    if epochs:
+        F, T = data(1 << 21)
+        t0 = time.perf_counter()
+        learn.train(F, T, epochs=epochs, lr=1e-3, batch=16384, seed=0)
+        dt = time.perf_counter() - t0
+        out.update({"train_rows": F.shape[0], "epochs": epochs, "batch": 16384, "seconds": dt,
+                    "rows_per_s": epochs * F.shape[0] / dt,
+                    "note": "fused tcgen05 gradient pass (BF16 operands, FP32 accumulation) + Adam per batch"})
+    return out
+
+
 def workload_config(args):
     return {"workload": f"isolated projection block {args.n}^3 = {args.n**3} fluid particles, "
                         f"{(args.n + 4)**3 - args.n**3} boundary, spacing 0.01, dt 5e-4, tol 1e-5",
@@ -520,7 +571,8 @@ def run_gpu_arm(args):
     torch.cuda.synchronize()
     e2e_ms = reduce_max(dist, f0.elapsed_time(f1))
     e2e = {"value": ws * args.steps / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
-           "d2h_bytes_per_step": 2 * nbytes}
+           "d2h_bytes_per_step": 2 * nbytes, "host_link": host_link(torch, stream, 2 * nbytes)}
+    e2e["host_link"]["copy_share_of_e2e_step"] = e2e["host_link"]["copy_ms_at_link_rate"] / (e2e_ms / args.steps)
     le.close()
     L.swc_host_free(hx_p)
     L.swc_host_free(hv_p)
@@ -552,6 +604,7 @@ def run_gpu_arm(args):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_reference(args, steps=args.cpu_steps, warmup=1, policy=True)
+    training = run_training_leg(args, torch) if args.training else None
     sand = None
     if args.sand:
         sand = run_sand_leg(args, torch, stream, hbm, peak_kind, with_cpu=rank == 0 and ws == 1 and not args.no_cpu)
@@ -567,7 +620,7 @@ def run_gpu_arm(args):
                 "wall_s_timed": wall, "cg_iterations_mean": float(np.mean(iters)), "n_virtual": nv,
                 "phases_ms": phases, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk.summary(), "gpu_launches": int(round(launches_per_step * args.steps)),
-                "forms": forms, "sand": sand}
+                "forms": forms, "sand": sand, "training": training}
         print(json.dumps(line), flush=True)
     liq.close()
     if dist is not None:
@@ -600,11 +653,21 @@ def main():
                     help="only the DEM sand leg (for profiler captures); prints the sand object")
     ap.add_argument("--profile-run", dest="profile_run", action="store_true",
                     help="only the timed steps (for profiler captures); prints a reduced line")
+    ap.add_argument("--training", type=int, default=1, help="also time the learned warm start's training path")
+    ap.add_argument("--train-rows", dest="train_rows", type=int, default=65536,
+                    help="rows of the timed loss-gradient pass")
+    ap.add_argument("--train-only", dest="train_only", action="store_true",
+                    help="only the loss-gradient pass on --train-rows rows (for profiler captures)")
     args = ap.parse_args()
     if args.warm_start == "auto":
         args.warm_start = "learned" if os.path.exists(MODEL) else "node"
     if args.impl == "reference":
         run_reference_arm(args)
+    elif args.train_only:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps(run_training_leg(args, torch, epochs=0)), flush=True)
     elif args.sand_only:
         import torch
 

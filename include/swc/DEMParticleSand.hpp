@@ -7,7 +7,7 @@
 // getTimeStep(frameRate, stepRate), dimension(), writeFrame(frameDir, staticDraw),
 // saveFrame(frameDir), loadFrame(frameDir); plus addShape (DEMParticleSand.cpp:167-175)
 // and the DEMParticle setters setYoung / setPoisson / setfricangle
-// (Cores/Structures/DEMParticle.cpp:158-174), which apply from the next initialize().
+// (Cores/Structures/DEMParticle.cpp:44-60), which apply from the next initialize().
 // Positions and velocities are FP64 arrays of Dim components per particle.
 // Errors throw swc::SandError carrying the swc_status code.
 #pragma once

@@ -3,7 +3,7 @@
  * DEMParticleSand<Dim>::advance of skytang0205/sand-water-coupling
  * (Cores/Physics/DEMParticleSand.h:13-58, DEMParticleSand.cpp:90-152) with the
  * contact model of DEMParticle (Cores/Structures/DEMParticle.h:57-112,
- * DEMParticle.cpp:128-248).
+ * DEMParticle.cpp:15-134).
  *
  * Conventions (as include/swc.h)
  *   - One context owns every device buffer of one sand simulation on one GPU
@@ -35,7 +35,7 @@ extern "C" {
 typedef struct swc_sand swc_sand;
 
 /* Replaces the constructor DEMParticleSand(particleRadius) and the DEMParticle
- * setters (DEMParticle.cpp:129-174). */
+ * setters (DEMParticle.cpp:15-60). */
 typedef struct swc_sand_params {
     int32_t dim;            /* 2 or 3 */
     int32_t enable_gravity; /* DEMParticleSand::_enableGravity (true in the reference) */

@@ -2,7 +2,7 @@
 //
 // CPU FP64 restatement of the DEM sand step of skytang0205/sand-water-coupling
 // (DEMParticleSand<Dim>::advance, Cores/Physics/DEMParticleSand.cpp:90-152, with
-// the contact model of DEMParticle, Cores/Structures/DEMParticle.cpp:128-248).
+// the contact model of DEMParticle, Cores/Structures/DEMParticle.cpp:15-134).
 // Only the tests, the smoke check and the CPU-baseline leg of the benchmark load
 // it; the product never links or calls it.
 //
@@ -14,15 +14,15 @@
 //
 // Reference behaviour kept on purpose:
 //   * neighbours of a sand particle are the particles with |x_j - x_i|^2 < (2r)^2
-//     (kernel_rate 2, DEMParticle.cpp:131; strict test of the hash searcher),
+//     (kernel_rate 2, DEMParticle.cpp:17; strict test of the hash searcher),
 //     boundary neighbours those within 4r (BoundaryParticles' default kernel_rate 4,
 //     Cores/Structures/SmoothedParticles.h:124-126);
 //   * the pair term carries no mass: v_i += dt * sum_j F_ij, and the boundary
 //     friction term is added without dt (DEMParticleSand.cpp:130-150);
 //   * the penetration depth uses the distance before its clamp to 1e-4 r, the
-//     normal uses the clamped one (DEMParticle.cpp:186-194);
+//     normal uses the clamped one (DEMParticle.cpp:77-80);
 //   * phi of the capillary term takes a single-precision sqrtf
-//     (DEMParticle.cpp:231).  The capillary branch needs H = |d| - 2r > 1e-6,
+//     (DEMParticle.cpp:103).  The capillary branch needs H = |d| - 2r > 1e-6,
 //     which no visited pair has (|d| < 2r), so it never contributes; it is
 //     restated for completeness and checked on its own.
 // One deliberate choice: the reference updates velocities[i] inside a parallel
@@ -38,12 +38,12 @@ struct DemParams {
     int32_t enable_gravity;
     double  radius;       // particle radius r (DEMParticleSand(particleRadius))
     double  mass;         // particle and boundary mass (DEMParticleSand.cpp:79)
-    double  young;        // DEMParticle::setYoung (default 1e9, DEMParticle.cpp:132)
+    double  young;        // DEMParticle::setYoung (default 1e9, DEMParticle.cpp:18)
     double  poisson;      // DEMParticle::setPoisson (default 0.3)
     double  fric_angle;   // DEMParticle::setfricangle, radians (default 0.5)
 };
 
-// DEMParticle's constants (DEMParticle.cpp:129-147) and its Bezier coefficient
+// DEMParticle's constants (DEMParticle.cpp:15-33) and its Bezier coefficient
 // QuadraticBezierCoeff::calculate (Cores/Structures/DEMParticle.h:14-55).
 struct DemModel {
     double r = 0, K_norm = 0, K_tang = 0, tan_fric = 0;
@@ -72,7 +72,7 @@ struct DemModel {
     }
 };
 
-// DEMParticle::ComputeDemForces (DEMParticle.cpp:183-210): d = x_j - x_i, w = v_j - v_i.
+// DEMParticle::ComputeDemForces (DEMParticle.cpp:69-96): d = x_j - x_i, w = v_j - v_i.
 template<int D> Vec<D> demContact(const DemModel & M, const Vec<D> & d, const Vec<D> & w) {
     Vec<D> f{};
     double dist      = norm<D>(d);
@@ -95,7 +95,7 @@ template<int D> Vec<D> demContact(const DemModel & M, const Vec<D> & d, const Ve
     return f;
 }
 
-// DEMParticle::ComputeDemCapillaryForces (DEMParticle.cpp:212-238).
+// DEMParticle::ComputeDemCapillaryForces (DEMParticle.cpp:98-124).
 template<int D> Vec<D> demCapillary(const DemModel & M, const Vec<D> & d) {
     Vec<D> f{};
     const double dist = norm<D>(d);

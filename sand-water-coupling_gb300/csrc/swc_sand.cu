@@ -5,7 +5,7 @@
 //      counting sort into cells of 2r (moveParticles + resetNearbySearcher,
 //      DEMParticleSand.cpp:98-109);
 //   2. one thread per sorted particle: contact forces of the particles within 2r
-//      (DEMParticle::getForceSum, Cores/Structures/DEMParticle.cpp:240-248), the
+//      (DEMParticle::getForceSum, Cores/Structures/DEMParticle.cpp:126-134), the
 //      friction of the boundary particles within 4r (DEMParticleSand.cpp:130-151)
 //      and gravity (DEMParticleSand.cpp:111-115), written to a second velocity
 //      buffer so every particle reads the velocities from the start of the pass.
@@ -25,7 +25,7 @@ using namespace swc;
 
 namespace swc {
 
-// Constants of the contact model (DEMParticle.cpp:129-147) and the boundary kernel.
+// Constants of the contact model (DEMParticle.cpp:15-33) and the boundary kernel.
 struct SandPhys {
     float R, R2;              // contact reach 2r and (2r)^2, FP32 (cell windows)
     float Rh, Rl, R2h, R2l;   // 2r and (2r)^2 as float-float (exact tests)
@@ -264,7 +264,7 @@ __global__ void k_sand_lattice(unsigned * __restrict__ box, float3 home_lo, floa
 }
 
 // The contact pass.  d = x_j - x_i, w = v_j - v_i as in DEMParticle::getForce
-// (DEMParticle.cpp:176-181).
+// (DEMParticle.cpp:62-67).
 template<int DIM>
 __global__ void __launch_bounds__(kSandNT, 5) k_sand_forces(const Lattice * __restrict__ Ld, Lattice Lb, SandPhys P,
                                                         const int * __restrict__ cellStart,
@@ -305,10 +305,10 @@ __global__ void __launch_bounds__(kSandNT, 5) k_sand_forces(const Lattice * __re
             // |d| = s0 + sl: one Newton correction of the rounded square root
             const float s0 = __fsqrt_rn(Dh);
             const float sl = s0 > 0.f ? __fmul_rn(__fadd_rn(__fmaf_rn(-s0, s0, Dh), Dl), __fdividef(0.5f, s0)) : 0.f;
-            // penetration 2r - |d| (DEMParticle.cpp:186-187); Rh - s0 is exact for |d| >= r
+            // penetration 2r - |d| (DEMParticle.cpp:72-73); Rh - s0 is exact for |d| >= r
             const float pen = __fadd_rn(__fsub_rn(P.Rh, s0), __fsub_rn(P.Rl, sl));
             if (pen > 0.f) {
-                // DEMParticle::ComputeDemForces (DEMParticle.cpp:188-208)
+                // DEMParticle::ComputeDemForces (DEMParticle.cpp:74-94)
                 const float dist = __fadd_rn(s0, sl);
                 const bool clamp = dist <= P.rclamp;
                 const float inv  = __frcp_rn(clamp ? P.rclamp : dist);
@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(kSandNT, 5) k_sand_forces(const Lattice * __re
                 fy -= Ny + Sy;
                 fz -= Nz + Sz;
             }
-            // DEMParticle::ComputeDemCapillaryForces (DEMParticle.cpp:212-238).  Every pair
+            // DEMParticle::ComputeDemCapillaryForces (DEMParticle.cpp:98-124).  Every pair
             // that gets here has |d| < 2r, so H = |d| - 2r < 0 fails H > 1e-6: the
             // liquid bridge never acts between neighbours found within 2r.
             const float H = -pen;
@@ -526,7 +526,7 @@ void setup_phys(swc_sand * s) {
     P.Kn           = float(Kn);
     P.Kt           = float(Kt);
     P.tanf         = float(std::tan(s->p.fric_angle));
-    // capillary constants (DEMParticle.cpp:134-145); coefficient G.calculate(0.1) = 1
+    // capillary constants (DEMParticle.cpp:20-31); coefficient G.calculate(0.1) = 1
     const double theta = 30. / 180. * std::numbers::pi;
     const double vlb   = 4. / 3. * std::numbers::pi * std::pow(r, 3.) * 0.01 * 0.01;
     P.drup     = float((1.f + 0.5f * theta) * (std::pow(vlb, 1. / 3.) + 0.1 * std::pow(vlb, 2. / 3.)));

@@ -3,8 +3,8 @@ only.  It shares no code with the C++ oracle (dense pair matrices instead of the
 hash searcher) so the two check each other.
 
 Reference behaviour restated (skytang0205/sand-water-coupling):
-  contact model      Cores/Structures/DEMParticle.cpp:128-210, 240-248
-  capillary bridge   DEMParticle.cpp:212-238 (never active between pairs within 2r)
+  contact model      Cores/Structures/DEMParticle.cpp:15-96, 126-134
+  capillary bridge   DEMParticle.cpp:98-124 (never active between pairs within 2r)
   boundary friction  Cores/Physics/DEMParticleSand.cpp:130-151
   move / gravity     DEMParticleSand.cpp:90-115
   boundary volumes   Cores/Structures/SmoothedParticles.cpp:25-41 (kernel radius 4r)

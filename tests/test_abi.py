@@ -78,7 +78,7 @@ def test_no_cpu_fallback(swc_mod):
 
 def test_sand_params_layout_and_defaults(swc_mod):
     """swc_sand_params as laid out in include/swc_sand.h; defaults are the reference's
-    (DEMParticle.cpp:132-136, DEMParticleSandBuilder case 0 radius at scale 30)."""
+    (DEMParticle.cpp:18-22, DEMParticleSandBuilder case 0 radius at scale 30)."""
     from swc import _lib
 
     assert C.sizeof(_lib.SandParams) == 2 * 4 + 5 * 8
