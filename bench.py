@@ -14,10 +14,11 @@ its result inside the timed region.  The headline form is the learned warm
 start (the trained model in swc/models/: a per-node correction of the
 pressure extrapolated in time, kept when it starts CG from a smaller residual
 than the extrapolation itself, the network skipped for 8 steps after 2
-consecutive rejections); ``forms`` reports plain CG from the node-mapped
-previous pressure, from the reference's stale prefix and from zero, the
-extrapolated start alone, the learned start evaluated every step and the
-learned start without the residual test, all on the same scene and steps.
+consecutive rejections, each further window without a kept prediction twice
+as long); ``forms`` reports plain CG from the node-mapped previous pressure,
+from the reference's stale prefix and from zero, the extrapolated start alone,
+the learned start evaluated every step and the learned start without the
+residual test, all on the same scene and steps.
 ``sand`` measures the DEM sand step (DEMParticleSand::advance) on a 2,009,840
 particle block the same way (device steps/s, e2e, roofline, CPU port).
 
@@ -53,7 +54,8 @@ UNIT = "steps/s"
 # disjoint from the benchmark block's)
 MODEL = os.path.join(ROOT, "sand-water-coupling_gb300", "swc", "models", "warm_start.npz")
 # the headline learned form skips the network for 8 steps after 2 consecutive
-# rejections by the residual test (learned_always evaluates it every step)
+# rejections by the residual test, doubling while it keeps being rejected
+# (learned_always evaluates it every step)
 LEARNED_GATE = 2
 
 
@@ -69,10 +71,10 @@ def peaks():
 SM_MAX_MHZ = 2070.0
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 128^3 block,
 # per active node of the captured launch: k_cg_spmv 32,769,792 B at 2,246,535 nodes,
-# k_node_gather 88,687,616 + 14,859,776 B and k_pressure_gradient 111,554,816 + 10,510,336 B
+# k_node_gather 90,965,504 + 13,017,856 B and k_pressure_gradient 113,461,248 + 12,455,680 B
 # at 2,246,538 nodes (profiles/)
-DRAM_BYTES_PER_NODE = {"cg_spmv": 32769792 / 2246535, "virtual_gather": (88687616 + 14859776) / 2246538,
-                       "pressure_gradient": (111554816 + 10510336) / 2246538}
+DRAM_BYTES_PER_NODE = {"cg_spmv": 32769792 / 2246535, "virtual_gather": (90965504 + 13017856) / 2246538,
+                       "pressure_gradient": (113461248 + 12455680) / 2246538}
 
 
 class ClockSampler:

@@ -112,6 +112,7 @@ struct swc_ctx {
     // learned-start gate: consecutive rejections by the residual test, steps left to skip
     int     gate_rejects = 0;
     int     gate_skip    = 0;
+    int     gate_windows = 0;  // skip windows since the prediction was last kept
     float *     pcomp = nullptr;    // last solution in reference order (prefix warm start)
     int *       nv_prev = nullptr;
     bool        pcomp_stale = false;  // the last projection did not export pcomp (other warm-start modes)
@@ -517,8 +518,11 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
         used = c->hcg->st.start == 0 ? SWC_WARM_LEARNED : base_used;
         if (c->opts.learned_gate > 0) {
             c->gate_rejects = used == SWC_WARM_LEARNED ? 0 : c->gate_rejects + 1;
+            if (used == SWC_WARM_LEARNED) c->gate_windows = 0;
             if (c->gate_rejects >= c->opts.learned_gate) {
-                c->gate_skip    = 4 * c->opts.learned_gate;
+                // the window doubles with every window since the prediction was last kept
+                c->gate_skip    = (4 * c->opts.learned_gate) << std::min(c->gate_windows, 4);
+                c->gate_windows++;
                 c->gate_rejects = 0;
             }
         }
@@ -672,7 +676,7 @@ template<int DIM> int do_initialize(swc_ctx * c) {
     // no previous pressure: empty prefix, no extrapolation history
     c->extrap_steps = 0;
     c->pcomp_stale  = false;
-    c->gate_rejects = c->gate_skip = 0;
+    c->gate_rejects = c->gate_skip = c->gate_windows = 0;
     CK(cudaMemsetAsync(c->nv_prev, 0, sizeof(int), c->stream));
     CK(cudaMemsetAsync(c->N.x, 0, sizeof(float) * size_t(c->L.nbricks) * (DIM == 3 ? 512 : 256), c->stream));
     CK(cudaMemsetAsync(c->N.flag, 0, size_t(c->L.nbricks) * (DIM == 3 ? 512 : 256), c->stream));
@@ -929,7 +933,7 @@ int swc_set_solver_opts(swc_ctx * c, const swc_solver_opts * o) {
     const bool need_vbar = o->keep_virtual_velocity && !c->N.vbar;
     const bool need_feat = o->keep_features && !c->N.nreal;
     c->opts         = *o;
-    c->gate_rejects = c->gate_skip = 0;
+    c->gate_rejects = c->gate_skip = c->gate_windows = 0;
     const size_t slots = size_t(c->L.nbricks) * (c->dim == 3 ? 512 : 256);
     int rc;
     if (need_vbar || need_feat) {

@@ -213,8 +213,9 @@ def test_learned_start_with_feature_logging(swc_mod):
 
 def test_learned_gate(swc_mod):
     """learned_gate: after that many consecutive rejections by the residual test the
-    network is skipped (base start) for 4 x gate steps; the solution stays the
-    extrapolated start's to the CG tolerance and skipped steps report the base."""
+    network is skipped (base start) for 4 x gate steps, doubling with every window
+    since the prediction was last kept; the solution stays the extrapolated start's
+    to the CG tolerance and skipped steps report the base."""
     import os
 
     from swc import learn
@@ -236,16 +237,20 @@ def test_learned_gate(swc_mod):
         liq.close()
     used = out["learned"][1]
     assert np.linalg.norm(out["learned"][0] - out["extrapolate"][0]) / np.linalg.norm(out["extrapolate"][0]) < 1e-4
-    # replay the gate on the reported starts: no learned start inside a skip window
-    skip = rejects = windows = 0
+    # replay the gate on the reported starts: no learned start inside a skip window, and
+    # every window since the prediction was last kept twice the one before
+    skip = rejects = windows = failed = 0
     for u in used:
         if skip > 0:
             assert u != 3, used
             skip -= 1
             continue
         rejects = 0 if u == 3 else rejects + 1
+        if u == 3:
+            failed = 0
         if rejects >= 1:
-            skip, rejects, windows = 4, 0, windows + 1
+            skip, rejects, windows = 4 << min(failed, 4), 0, windows + 1
+            failed += 1
     assert windows >= 1 and 3 in used, used
     print(f"\nwarm start used with learned_gate=1: {used}")
 
