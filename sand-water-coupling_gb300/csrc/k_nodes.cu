@@ -674,11 +674,7 @@ __global__ void __launch_bounds__(kGradNT) k_pressure_gradient(Lattice L, Phys P
         const double tod_z = DIM == 3 ? L.oz_d + (bc.z * G::BZ - G::HALO) * L.dx_d : 0.0;
         const float tox = float(tod_x), toy = float(tod_y), toz = float(tod_z);
         const float tlx = float(tod_x - double(tox)), tly = float(tod_y - double(toy)), tlz = float(tod_z - double(toz));
-        // two full rounds of one particle per thread; in 3D the particles beyond them
-        // go one per warp below, so a brick a few particles above 2 x 256 does not run
-        // a third round on a few threads while the rest of the block waits
-        const int main_n = DIM == 3 ? min(total, 2 * kGradNT) : total;
-        for (int p = t; p < main_n; p += kGradNT) {
+        for (int p = t; p < total; p += kGradNT) {
             int lo = 0, hi = ROWS - 1;
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
@@ -735,64 +731,6 @@ __global__ void __launch_bounds__(kGradNT) k_pressure_gradient(Lattice L, Phys P
             o.y += f.y;
             if (DIM == 3) o.z += f.z;
             vel[j] = o;
-        }
-        if (DIM == 3) {
-            // the rest: one warp per particle, the 64 rows of its window over the lanes
-            const int lane = t & 31;
-            for (int p = main_n + (t >> 5); p < total; p += kGradNT / 32) {
-                int lo = 0, hi = ROWS - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (rinc[mid] > p) hi = mid;
-                    else lo = mid + 1;
-                }
-                const int j     = rbeg[lo] + p;
-                const float4 q  = pos[j];
-                const float4 vi = vel[j];
-                const float ux = ((q.x - tox) - tlx) * L.inv_dx, uy = ((q.y - toy) - tly) * L.inv_dx;
-                const float uz = ((q.z - toz) - tlz) * L.inv_dx;
-                float3 f = make_float3(0.f, 0.f, 0.f);
-                const bool inside = ux >= 3.f && ux < float(G::TX) - 4.f && uy >= 3.f && uy < float(G::TY) - 4.f &&
-                                    uz >= 3.f && uz < float(G::TZ) - 4.f;
-                if (inside) {
-                    const int cx = int(ux), cy = int(uy), cz = int(uz);
-                    const float fx = ux - float(cx - 3);
-                    const float2 dxp[4] = {make_float2(fx - 2.f, fx - 3.f), make_float2(fx - 4.f, fx - 5.f),
-                                           make_float2(fx - 1.f, fx - 6.f), make_float2(fx, fx - 7.f)};
-                    float2 sx = make_float2(0.f, 0.f);
-                    float fy = 0.f, fz = 0.f;
-                    for (int r = lane; r < 64; r += 32) {
-                        const int kz = cz - 3 + (r >> 3), ky = cy - 3 + (r & 7);
-                        const float dz = uz - float(kz), dy = uy - float(ky);
-                        const float dyz2 = fmaf(dy, dy, dz * dz);
-                        if (dyz2 >= 16.f) continue;
-                        const float * trow = tile + PX * (ky + G::TY * kz) + (cx - 3);
-                        const float2 sg = gradient_row(trow, dxp, dyz2, sx);
-                        const float sr  = sg.x + sg.y;
-                        fy = fmaf(dy, sr, fy);
-                        fz = fmaf(dz, sr, fz);
-                    }
-                    float fxs = sx.x + sx.y;
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        fxs += __shfl_xor_sync(0xffffffffu, fxs, o);
-                        fy += __shfl_xor_sync(0xffffffffu, fy, o);
-                        fz += __shfl_xor_sync(0xffffffffu, fz, o);
-                    }
-                    f = make_float3(P.c1H * fxs, P.c1H * fy, P.c1H * fz);
-                } else if (lane == 0) {
-                    f = gradient_virtual_global<DIM>(L, P, bflag, N, q);
-                }
-                if (lane == 0) {
-                    if (walls && bcell[cell_linear(L, cell_of<DIM>(L, q.x, q.y, q.z))]) {
-                        const float3 w = wall_term<DIM>(L, P, bcellStart, bpos, bvel, bnrm, q, vi);
-                        f.x += w.x;
-                        f.y += w.y;
-                        f.z += w.z;
-                    }
-                    vel[j] = make_float4(vi.x + f.x, vi.y + f.y, vi.z + f.z, vi.w);
-                }
-            }
         }
     }
     queue_finish(queue);
