@@ -335,11 +335,10 @@ __device__ __forceinline__ float slab_dist(float q, int c, int n, float o, float
 
 // Neighbour iteration over cells for a query point and radius R (particle
 // queries): rows pruned by their slab distance, x-range per row from the
-// remaining radius; f(b, e) for the sorted index range [b, e) of the visited
-// cells of each row, rows in (z, y) order.
+// remaining radius; f(j) for every particle j of the visited cells.
 template<int DIM, class F>
-__device__ __forceinline__ void for_each_range_in_radius(const Lattice & L, const int * __restrict__ cellStart,
-                                                         float qx, float qy, float qz, float R, float R2, F && f) {
+__device__ __forceinline__ void for_each_in_radius(const Lattice & L, const int * __restrict__ cellStart,
+                                                   float qx, float qy, float qz, float R, float R2, F && f) {
     const int cy0 = clampi(__float2int_rd((qy - R - L.oy) * L.inv_dx), 0, L.ny - 1);
     const int cy1 = clampi(__float2int_rd((qy + R - L.oy) * L.inv_dx), 0, L.ny - 1);
     int cz0 = 0, cz1 = 0;
@@ -359,18 +358,10 @@ __device__ __forceinline__ void for_each_range_in_radius(const Lattice & L, cons
             const int cx0  = clampi(__float2int_rd((qx - rx - L.ox) * L.inv_dx), 0, L.nx - 1);
             const int cx1  = clampi(__float2int_rd((qx + rx - L.ox) * L.inv_dx), 0, L.nx - 1);
             const long long row = (long long) L.nx * (cy + (long long) L.ny * cz);
-            f(cellStart[row + cx0], cellStart[row + cx1 + 1]);
+            const int b = cellStart[row + cx0], e = cellStart[row + cx1 + 1];
+            for (int j = b; j < e; j++) f(j);
         }
     }
-}
-
-// The same visit with f(j) for every particle j of the visited cells.
-template<int DIM, class F>
-__device__ __forceinline__ void for_each_in_radius(const Lattice & L, const int * __restrict__ cellStart,
-                                                   float qx, float qy, float qz, float R, float R2, F && f) {
-    for_each_range_in_radius<DIM>(L, cellStart, qx, qy, qz, R, R2, [&](int b, int e) {
-        for (int j = b; j < e; j++) f(j);
-    });
 }
 
 // The same visit for two query points a and b at once (neighbours in the

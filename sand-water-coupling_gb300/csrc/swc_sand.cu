@@ -15,7 +15,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <mutex>
 #include <numbers>
 #include <string>
 
@@ -41,9 +40,8 @@ struct SandPhys {
 
 namespace {
 
-constexpr int kSandNT    = 256;
-constexpr int kSandList  = 16;    // candidates per thread gathered before their pair terms run
-constexpr int kSandStage = 2304;  // staged positions per chunk of kSandNT particles (36 KB)
+constexpr int kSandNT   = 256;
+constexpr int kSandList = 16;  // candidates per thread gathered before their pair terms run
 
 inline int sand_grid(long long n, int threads, int cap = 152 * 16) {
     const long long g = (n + threads - 1) / threads;
@@ -267,18 +265,8 @@ __global__ void k_sand_lattice(unsigned * __restrict__ box, float3 home_lo, floa
 
 // The contact pass.  d = x_j - x_i, w = v_j - v_i as in DEMParticle::getForce
 // (DEMParticle.cpp:62-67).
-//
-// A block takes chunks of kSandNT consecutive sorted particles.  Their
-// neighbours within 2r lie in the cell rows of the chunk and the rows next to
-// them (y +- 1, and z +- 1 in 3D), which in the sorted order are up to three
-// contiguous index ranges (one per z plane): the block copies their positions
-// (hi parts) into shared memory, coalesced, and the candidate pre-test reads
-// them from there.  A row range that is not wholly staged (a chunk whose rows
-// exceed kSandStage particles, or a cell reached beyond the neighbouring rows)
-// is read from global memory, so the staging never changes which particles
-// are visited.
 template<int DIM>
-__global__ void __launch_bounds__(kSandNT, 4) k_sand_forces(const Lattice * __restrict__ Ld, Lattice Lb, SandPhys P,
+__global__ void __launch_bounds__(kSandNT, 5) k_sand_forces(const Lattice * __restrict__ Ld, Lattice Lb, SandPhys P,
                                                         const int * __restrict__ cellStart,
                                                         const float4 * __restrict__ pos, const float4 * __restrict__ plo,
                                                         const float4 * __restrict__ vel, float4 * __restrict__ vel_out,
@@ -288,51 +276,9 @@ __global__ void __launch_bounds__(kSandNT, 4) k_sand_forces(const Lattice * __re
                                                         const float4 * __restrict__ bnrm,
                                                         const unsigned char * __restrict__ bnear) {
     pdl_wait_and_release();
-    extern __shared__ float4 spos[];            // staged positions (hi), kSandStage
     __shared__ int clist[kSandList * kSandNT];  // per-thread candidate lists, slot-major
-    __shared__ int sseg[9];                     // per z plane: first index, end, shared-memory offset - first
     const Lattice L = *Ld;
-    for (long long c0 = (long long) blockIdx.x * kSandNT; c0 < n; c0 += (long long) gridDim.x * kSandNT) {
-        const long long c1 = min(c0 + kSandNT, n) - 1;
-        __syncthreads();  // the previous chunk is done with spos and sseg
-        if (threadIdx.x == 0) {
-            const float4 qa = pos[c0], qb = pos[c1];
-            const int3 ca = cell_of<DIM>(L, qa.x, qa.y, qa.z), cb = cell_of<DIM>(L, qb.x, qb.y, qb.z);
-            const int ra = min(ca.y + L.ny * ca.z, cb.y + L.ny * cb.z), rb = max(ca.y + L.ny * ca.z, cb.y + L.ny * cb.z);
-            const int nrows = L.ny * L.nz;
-            int used = 0, prev = 0;
-            for (int d = 0; d < 3; d++) {
-                int lo = 0, end = 0;
-                if (DIM == 3 || d == 1) {
-                    const int r0 = max(ra - 1 + (d - 1) * L.ny, 0), r1 = min(rb + 1 + (d - 1) * L.ny, nrows - 1);
-                    if (r0 <= r1) {
-                        const int b = max(cellStart[(long long) r0 * L.nx], prev);
-                        const int e = cellStart[(long long) (r1 + 1) * L.nx];
-                        prev        = max(prev, e);
-                        if (b < e) {
-                            lo  = b;
-                            end = b + min(e - b, kSandStage - used);
-                        }
-                    }
-                }
-                sseg[3 * d]     = lo;
-                sseg[3 * d + 1] = end;
-                sseg[3 * d + 2] = used - lo;
-                used += end - lo;
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            const int lo = sseg[3 * d], end = sseg[3 * d + 1], off = sseg[3 * d + 2];
-            for (int j = lo + threadIdx.x; j < end; j += kSandNT) spos[j + off] = pos[j];
-        }
-        __syncthreads();
-        const long long i = c0 + threadIdx.x;
-        if (i > c1) continue;
-        int s_lo[3], s_end[3], s_off[3];
-#pragma unroll
-        for (int d = 0; d < 3; d++) s_lo[d] = sseg[3 * d], s_end[d] = sseg[3 * d + 1], s_off[d] = sseg[3 * d + 2];
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
         const float4 qi = pos[i], li = plo[i], vi = vel[i];
         // The FP32 window and pre-test ignore the low parts (|lo| <= 2^-24 |x|) and
         // round the difference once: widen the reach by 2^-21 (|x|_max + 2r).
@@ -417,23 +363,15 @@ __global__ void __launch_bounds__(kSandNT, 4) k_sand_forces(const Lattice * __re
             }
         };
         int cnt = 0;
-        for_each_range_in_radius<DIM>(L, cellStart, qi.x, qi.y, qi.z, Rq, Rq2, [&](int jb, int je) {
-            // the row's range from shared memory when a staged plane holds all of it
-            int off = 0;
-            bool staged = false;
-#pragma unroll
-            for (int d = 0; d < 3; d++)
-                if (jb >= s_lo[d] && je <= s_end[d]) off = s_off[d], staged = true;
-            for (int j = jb; j < je; j++) {
-                if (j == int(i)) continue;  // d = 0, w = 0: the reference's self term is zero
-                const float4 qj = staged ? spos[j + off] : pos[j];
-                const float ex = qj.x - qi.x, ey = qj.y - qi.y, ez = DIM == 3 ? qj.z - qi.z : 0.f;
-                if (ex * ex + ey * ey + ez * ez >= Rq2) continue;
-                clist[cnt * kSandNT + threadIdx.x] = j;
-                if (++cnt == kSandList) {
-                    for (int k = 0; k < cnt; k++) contact(clist[k * kSandNT + threadIdx.x]);
-                    cnt = 0;
-                }
+        for_each_in_radius<DIM>(L, cellStart, qi.x, qi.y, qi.z, Rq, Rq2, [&](int j) {
+            if (j == int(i)) return;  // d = 0, w = 0: the reference's self term is zero
+            const float4 qj = pos[j];
+            const float ex = qj.x - qi.x, ey = qj.y - qi.y, ez = DIM == 3 ? qj.z - qi.z : 0.f;
+            if (ex * ex + ey * ey + ez * ez >= Rq2) return;
+            clist[cnt * kSandNT + threadIdx.x] = j;
+            if (++cnt == kSandList) {
+                for (int k = 0; k < cnt; k++) contact(clist[k * kSandNT + threadIdx.x]);
+                cnt = 0;
             }
         });
         for (int k = 0; k < cnt; k++) contact(clist[k * kSandNT + threadIdx.x]);
@@ -736,33 +674,12 @@ template<int DIM> int do_initialize(swc_sand * s) {
     return SWC_OK;
 }
 
-// The contact pass's shared memory exceeds the 48 KB default: allowed once per
-// device and dimension (cudaFuncSetAttribute is per device).
-template<int DIM> bool sand_forces_smem_ready() {
-    constexpr int kMaxDev = 64;
-    static bool ready[kMaxDev];
-    static std::mutex m;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return false;
-    std::lock_guard<std::mutex> lock(m);
-    if (!ready[dev])
-        ready[dev] = cudaFuncSetAttribute(k_sand_forces<DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          int(kSandStage * sizeof(float4))) == cudaSuccess;
-    return ready[dev];
-}
-
-template<int DIM> int launch_forces(swc_sand * s, float4 * out) {
-    if (s->n == 0) return SWC_OK;
-    if (!sand_forces_smem_ready<DIM>()) {
-        s->err = "cudaFuncSetAttribute (contact pass shared memory) failed";
-        return SWC_CUDA_ERROR;
-    }
-    launch_pdl(k_sand_forces<DIM>, sand_grid(s->n, kSandNT, 152 * 64), kSandNT, kSandStage * sizeof(float4), s->stream,
-               (const Lattice *) s->dL,
+template<int DIM> void launch_forces(swc_sand * s, float4 * out) {
+    if (s->n == 0) return;
+    launch_pdl(k_sand_forces<DIM>, sand_grid(s->n, kSandNT, 152 * 64), kSandNT, 0, s->stream, (const Lattice *) s->dL,
                s->Lb, s->P, (const int *) s->cellStart, (const float4 *) s->pos, (const float4 *) s->plo,
                (const float4 *) s->vel, out, s->n, (const int *) s->bcellStart, (const float4 *) s->bpos,
                (const float4 *) s->blo, (const float4 *) s->bnrm, (const unsigned char *) s->bnear);
-    return SWC_OK;
 }
 
 template<int DIM> int do_advance(swc_sand * s, double dt) {
@@ -770,8 +687,7 @@ template<int DIM> int do_advance(swc_sand * s, double dt) {
     s->P.dt  = dth;
     s->P.gdt = s->p.enable_gravity ? float(9.8 * dt) : 0.f;  // kGravity, Cores/Utilities/Constants.h:7
     bin_sand<DIM>(s, dth, dtl);
-    const int rc = launch_forces<DIM>(s, s->vel2);
-    if (rc) return rc;
+    launch_forces<DIM>(s, s->vel2);
     std::swap(s->vel, s->vel2);
     SK(cudaGetLastError());
     return SWC_OK;
@@ -1009,8 +925,8 @@ int swc_sand_time_kernel(swc_sand * s, int which, int reps, double * mean_ms) {
     SK(cudaEventRecord(s->e0, s->stream));
     for (int r = 0; r < reps; r++) {
         if (which == 0) {
-            const int rc = s->dim == 2 ? launch_forces<2>(s, s->vel2) : launch_forces<3>(s, s->vel2);
-            if (rc) return rc;
+            if (s->dim == 2) launch_forces<2>(s, s->vel2);
+            else launch_forces<3>(s, s->vel2);
         } else {
             if (s->dim == 2) bin_sand<2>(s, 0.f, 0.f);
             else bin_sand<3>(s, 0.f, 0.f);
