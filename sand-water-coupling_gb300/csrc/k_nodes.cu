@@ -67,7 +67,8 @@ struct NodeSums2 {
 // only takes particles with r^2 < h^2 (a is zeroed otherwise).  rho_I uses W_H
 // truncated at h: for H >= 2h (FAST_H) only its inner branch
 // wH = 1 + 6 x^2 (x - 1), x = r / H, is reached; otherwise wH = 2 aH^3 - 8 bH^3.
-template<bool REAL, bool FAST_H>
+// FEAT adds the real-neighbour count (a feature of the learned warm start).
+template<bool REAL, bool FAST_H, bool FEAT>
 __device__ __forceinline__ void pair_add(NodeSums2 & s, const Phys & P, float2 dxx, float dy, float dz, float2 r2,
                                          bool m0, bool m1, float4 p, float4 u) {
     const float2 ri = make_float2(rsqrt_n(fmaxf(r2.x, 1e-30f)), rsqrt_n(fmaxf(r2.y, 1e-30f)));
@@ -93,7 +94,7 @@ __device__ __forceinline__ void pair_add(NodeSums2 & s, const Phys & P, float2 d
         s.wsum = add2(s.wsum, w);
         s.rhoI = add2(s.rhoI, wH);
         s.VI   = fma2(f2(p.w * p.w), w, s.VI);
-        s.cnt  = add2(s.cnt, make_float2(m0 ? 1.f : 0.f, m1 ? 1.f : 0.f));
+        if (FEAT) s.cnt = add2(s.cnt, make_float2(m0 ? 1.f : 0.f, m1 ? 1.f : 0.f));
     }
     const float2 mw = mul2(f2(u.w), w);
     s.ux  = fma2(f2(u.x), mw, s.ux);
@@ -124,7 +125,7 @@ __device__ __forceinline__ void pair_add(NodeSums2 & s, const Phys & P, float2 d
 // Five 128-thread blocks per SM (96 registers, no spills): 10% faster than the
 // unconstrained 109-register build at four blocks.
 // ---------------------------------------------------------------------------
-template<int DIM, bool FAST_H>
+template<int DIM, bool FAST_H, bool FEAT>
 __global__ void __launch_bounds__(128, 5) k_node_gather(Lattice L, Phys P, const int * __restrict__ blist,
                                                     const int * __restrict__ bcount, NodeArrays N,
                                                     const float4 * __restrict__ pos, const float4 * __restrict__ vel,
@@ -221,8 +222,8 @@ __global__ void __launch_bounds__(128, 5) k_node_gather(Lattice L, Phys P, const
                                 m1 = (DIM == 3 ? fma(ez, ez, s1) : s1) < hh;
                             }
                             if (!(m0 || m1)) continue;
-                            if (pass == 0) pair_add<true, FAST_H>(a, P, dxx, dy, dz, r2, m0, m1, p, u);
-                            else pair_add<false, FAST_H>(a, P, dxx, dy, dz, r2, m0, m1, p, u);
+                            if (pass == 0) pair_add<true, FAST_H, FEAT>(a, P, dxx, dy, dz, r2, m0, m1, p, u);
+                            else pair_add<false, FAST_H, FEAT>(a, P, dxx, dy, dz, r2, m0, m1, p, u);
                         }
                         if (!more) break;
                         cy = ny, cz = nz, jb = nb_, je = ne_;
@@ -274,7 +275,7 @@ __global__ void __launch_bounds__(128, 5) k_node_gather(Lattice L, Phys P, const
                 N.V[s]    = active ? w2 * pick(a.VI) : 0.f;
                 N.D[s]    = active ? Dv : 0.f;
                 N.rho[s]  = active ? rho : 0.f;
-                if (N.nreal) N.nreal[s] = (unsigned short) min(int(pick(a.cnt)), 65535);
+                if (FEAT) N.nreal[s] = (unsigned short) min(int(pick(a.cnt)), 65535);
                 if (N.vbar) N.vbar[s] = make_float4(vbx, vby, vbz, 0.f);
             }
         }
@@ -754,11 +755,12 @@ template<int DIM> int pressure_gradient_blocks_per_sm() {
     return n > 0 ? n : 1;
 }
 template<int DIM> int node_gather_blocks_per_sm() {
-    int n = 0;
-    int m = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_node_gather<DIM, true>, 128, 0) != cudaSuccess) n = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_node_gather<DIM, false>, 128, 0) != cudaSuccess) m = 1;
-    n = std::min(n, m);
+    auto blocks = [](auto kernel) {
+        int k = 0;
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, kernel, 128, 0) == cudaSuccess ? k : 1;
+    };
+    const int n = std::min(std::min(blocks(k_node_gather<DIM, true, true>), blocks(k_node_gather<DIM, true, false>)),
+                           std::min(blocks(k_node_gather<DIM, false, true>), blocks(k_node_gather<DIM, false, false>)));
     return n > 0 ? n : 1;
 }
 void launch_brick_list(const unsigned char * bflag, int nbricks, int * list, int * count, cudaStream_t st) {
@@ -770,13 +772,15 @@ void launch_node_gather(const Lattice & L, const Phys & P, const BrickArrays & B
                         const float4 * pos, const float4 * vel, const int * cellStart, const float4 * bpos,
                         const float4 * bvel, const int * bcellStart, const unsigned char * bnear,
                         const unsigned char * bcell, int grid, int * queue, cudaStream_t st) {
-    // H >= 2h: particles within h only reach the inner branch of W_H
-    if (double(P.H) >= 2.0 * double(P.h) * (1.0 - 1e-6))
-        launch_pdl(k_node_gather<DIM, true>, grid, 128, 0, st, L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel,
-                                                       bcellStart, bnear, bcell, queue);
-    else
-        launch_pdl(k_node_gather<DIM, false>, grid, 128, 0, st, L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel,
-                                                        bcellStart, bnear, bcell, queue);
+    // H >= 2h: particles within h only reach the inner branch of W_H; the
+    // real-neighbour counts only where N.nreal is given
+    const bool fast = double(P.H) >= 2.0 * double(P.h) * (1.0 - 1e-6), feat = N.nreal != nullptr;
+    auto go = [&](auto kernel) {
+        launch_pdl(kernel, grid, 128, 0, st, L, P, B.list, B.count, N, pos, vel, cellStart, bpos, bvel, bcellStart, bnear,
+                   bcell, queue);
+    };
+    if (fast) feat ? go(k_node_gather<DIM, true, true>) : go(k_node_gather<DIM, true, false>);
+    else feat ? go(k_node_gather<DIM, false, true>) : go(k_node_gather<DIM, false, false>);
 }
 
 template<int DIM>

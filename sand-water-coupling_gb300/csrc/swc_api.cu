@@ -319,11 +319,15 @@ inline void mark(swc_ctx * c, int k) {
 
 // Virtual generation: active bricks, fused gather, reference-order compaction,
 // alpha_hat (VirtualParticle::generateParticles + calculateCoef diagonal).
-template<int DIM> void run_generate(swc_ctx * c, bool with_ahat) {
+// `features`: the step needs the learned warm start's per-node features (the
+// real-neighbour counts of the gather); without them the gather skips the count.
+template<int DIM> void run_generate(swc_ctx * c, bool with_ahat, bool features = true) {
     launch_mark_bricks<DIM>(c->cellStart, c->n, c->L, c->P, c->B.flag, c->pflag, c->stream);
     launch_brick_list(c->B.flag, c->L.nbricks, c->B.list, c->B.count, c->stream);
     launch_brick_list(c->pflag, c->L.nbricks, c->plist, c->pcount, c->stream);
-    launch_node_gather<DIM>(c->L, c->P, c->B, c->N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel, c->bcellStart,
+    NodeArrays N = c->N;
+    if (!features) N.nreal = nullptr;
+    launch_node_gather<DIM>(c->L, c->P, c->B, N, c->pos, c->vel, c->cellStart, c->bpos, c->bvel, c->bcellStart,
                             c->bnear, c->bcell, c->ggrid, c->queues, c->stream);
     launch_segments<DIM>(c->L, c->B, c->N, c->scan_tiles, c->grid, c->stream);
     if (with_ahat) launch_ahat<DIM>(c->L, c->P, c->B, c->N, c->S, c->sgrid, c->stream);
@@ -437,9 +441,6 @@ bool history_on(const swc_ctx * c) {
 
 // The shared tail of advance / project: virtual generation, projection, G_i.
 template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
-    mark(c, 3);
-    run_generate<DIM>(c, true);
-    mark(c, 4);
     const int mode     = c->opts.warm_start;
     // the gate skips the network (base start) while it keeps losing the residual test
     const bool gated   = mode == SWC_WARM_LEARNED && c->mlp_ready && c->opts.learned_gate > 0 &&
@@ -447,6 +448,10 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
     if (gated) c->gate_skip--;
     const bool learned = mode == SWC_WARM_LEARNED && c->mlp_ready && !gated;
     const bool logging = c->opts.keep_features != 0 && c->feat_buf;
+    mark(c, 3);
+    // a step that runs neither the network nor the feature logging needs no features
+    run_generate<DIM>(c, true, learned || logging);
+    mark(c, 4);
     const int * nv     = c->B.seg_off + c->B.nseg;
     const size_t slots = size_t(c->L.nbricks) * BrickGeom<DIM>::BN;
     int used           = mode;
@@ -506,8 +511,10 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
             launch_warm_start<DIM>(c->L, c->B, c->N, mode, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
         }
     } else if (hist_on) {
-        launch_warm_start<DIM>(c->L, c->B, c->N, kWarmExtrap, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream,
-                               history);
+        // the second differences are a feature: not written on a step without the network
+        NodeArrays N = c->N;
+        N.d2p        = nullptr;
+        launch_warm_start<DIM>(c->L, c->B, N, kWarmExtrap, c->pcomp, c->nv_prev, nullptr, c->grid, c->stream, history);
     } else {
         launch_warm_start<DIM>(c->L, c->B, c->N, mode == SWC_WARM_LEARNED || mode == SWC_WARM_EXTRAPOLATE ? kWarmNode : mode,
                                c->pcomp, c->nv_prev, nullptr, c->grid, c->stream);
