@@ -83,9 +83,9 @@ typedef struct swc_solver_opts {
     int32_t learned_gate;          /* learned start with the residual test: after this many
                                       consecutive rejections of the prediction, skip the network
                                       (base start) for 4 * learned_gate advance steps, then test
-                                      it again; every further window without a kept prediction
-                                      doubles (up to 64 * learned_gate steps); 0: evaluate the
-                                      network every step */
+                                      it again: one rejection of that test starts the next window,
+                                      twice as long (up to 64 * learned_gate steps) until a
+                                      prediction is kept; 0: evaluate the network every step */
 } swc_solver_opts;
 
 typedef struct swc_stats {

@@ -526,7 +526,8 @@ template<int DIM> int run_projection(swc_ctx * c, swc_stats * st) {
         if (c->opts.learned_gate > 0) {
             c->gate_rejects = used == SWC_WARM_LEARNED ? 0 : c->gate_rejects + 1;
             if (used == SWC_WARM_LEARNED) c->gate_windows = 0;
-            if (c->gate_rejects >= c->opts.learned_gate) {
+            // after a window, the re-test's rejection alone starts the next one
+            if (c->gate_rejects >= c->opts.learned_gate || (c->gate_windows > 0 && c->gate_rejects > 0)) {
                 // the window doubles with every window since the prediction was last kept
                 c->gate_skip    = (4 * c->opts.learned_gate) << std::min(c->gate_windows, 4);
                 c->gate_windows++;

@@ -211,11 +211,13 @@ def test_learned_start_with_feature_logging(swc_mod):
     assert np.linalg.norm(vel["learned"] - vel["node"]) / np.linalg.norm(vel["node"]) < 1e-4
 
 
-def test_learned_gate(swc_mod):
+@pytest.mark.parametrize("gate", [1, 2])
+def test_learned_gate(swc_mod, gate):
     """learned_gate: after that many consecutive rejections by the residual test the
-    network is skipped (base start) for 4 x gate steps, doubling with every window
-    since the prediction was last kept; the solution stays the extrapolated start's
-    to the CG tolerance and skipped steps report the base."""
+    network is skipped (base start) for 4 x gate steps; after a window one rejection
+    of the re-test starts the next, twice as long, until a prediction is kept; the
+    solution stays the extrapolated start's to the CG tolerance and skipped steps
+    report the base."""
     import os
 
     from swc import learn
@@ -223,13 +225,13 @@ def test_learned_gate(swc_mod):
     path = os.path.join(os.path.dirname(learn.__file__), "models", "warm_start.npz")
     sc = scenes.projection_block_3d(n=20, seed=8).rounded_to_float32()
     out = {}
-    for mode, gate in (("extrapolate", 0), ("learned", 1)):
-        liq = swc_mod.DualParticleSphLiquid(sc, warm_start=mode, learned_gate=gate)
+    for mode, g in (("extrapolate", 0), ("learned", gate)):
+        liq = swc_mod.DualParticleSphLiquid(sc, warm_start=mode, learned_gate=g)
         if mode == "learned":
             liq.setMlp(*learn.load_model(path))
         liq.initialize()
         used = []
-        for _ in range(16):
+        for _ in range(24):
             st = liq.advance(sc.dt)
             assert st["status"] == 0
             used.append(st["warm_start_used"])
@@ -237,8 +239,9 @@ def test_learned_gate(swc_mod):
         liq.close()
     used = out["learned"][1]
     assert np.linalg.norm(out["learned"][0] - out["extrapolate"][0]) / np.linalg.norm(out["extrapolate"][0]) < 1e-4
-    # replay the gate on the reported starts: no learned start inside a skip window, and
-    # every window since the prediction was last kept twice the one before
+    # replay the gate on the reported starts: no learned start inside a skip window,
+    # every window since the prediction was last kept twice the one before, and a
+    # single rejection after a window starting the next
     skip = rejects = windows = failed = 0
     for u in used:
         if skip > 0:
@@ -248,11 +251,11 @@ def test_learned_gate(swc_mod):
         rejects = 0 if u == 3 else rejects + 1
         if u == 3:
             failed = 0
-        if rejects >= 1:
-            skip, rejects, windows = 4 << min(failed, 4), 0, windows + 1
+        if rejects >= gate or (failed > 0 and rejects > 0):
+            skip, rejects, windows = (4 * gate) << min(failed, 4), 0, windows + 1
             failed += 1
     assert windows >= 1 and 3 in used, used
-    print(f"\nwarm start used with learned_gate=1: {used}")
+    print(f"\nwarm start used with learned_gate={gate}: {used}")
 
 
 @pytest.mark.parametrize("case", ["block_64", "dam_break"])
