@@ -629,6 +629,51 @@ def run_gpu_arm(args):
         dist.destroy_process_group()
 
 
+def run_scene_leg(args):
+    """Throughput of the other configurations (wall time of the device steps on the
+    library's stream, CUDA events) for the node-mapped, extrapolated and learned
+    warm starts, after one untimed step, with one profiled step's phase split."""
+    import torch
+
+    import swc
+    from swc import learn, scenes
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    scene = scenes.dam_break_3d(seed=args.seed) if args.scene == "dam_break_3d" else scenes.paddle_tank_3d(seed=args.seed)
+    stream = torch.cuda.Stream()
+    forms = {}
+    for warm in ("node", "extrapolate", "learned"):
+        liq = swc.DualParticleSphLiquid(scene, warm_start=warm, tolerance=scene.tolerance,
+                                        learned_gate=LEARNED_GATE if warm == "learned" else 0)
+        if warm == "learned":
+            liq.setMlp(*learn.load_model(MODEL))
+        liq.setStream(stream.cuda_stream)
+        liq.initialize()
+        liq.advance(scene.dt)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        its = []
+        e0.record(stream)
+        for _ in range(args.steps):
+            st = liq.advance(scene.dt)
+            if st["status"] not in (0, 1):
+                raise RuntimeError(f"step failed: {st}")
+            its.append(st["cg_iterations"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        liq.setProfiling(True)
+        liq.advance(scene.dt)
+        phases = liq.phaseTimes()
+        liq.setProfiling(False)
+        forms[warm] = {"steps_per_s": args.steps / (e0.elapsed_time(e1) / 1e3),
+                       "cg_iterations_mean": float(np.mean(its)), "n_virtual": st["n_virtual"],
+                       "phases_ms": phases}
+        liq.close()
+    return {"scene": scene.name, "particles": scene.n_particles, "boundary": scene.n_boundary,
+            "steps": args.steps, "dt": scene.dt, "tolerance": scene.tolerance, "forms": forms}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -658,6 +703,9 @@ def main():
     ap.add_argument("--training", type=int, default=1, help="also time the learned warm start's training path")
     ap.add_argument("--train-rows", dest="train_rows", type=int, default=65536,
                     help="rows of the timed loss-gradient pass")
+    ap.add_argument("--scene", default="block", choices=["block", "dam_break_3d", "paddle_tank"],
+                    help="block: the benchmark; the others print the throughput of that configuration "
+                         "(3D dam break, 524,288 particles; paddle tank, 8,388,608 particles with a rotating paddle)")
     ap.add_argument("--train-only", dest="train_only", action="store_true",
                     help="only the loss-gradient pass on --train-rows rows (for profiler captures)")
     args = ap.parse_args()
@@ -665,6 +713,8 @@ def main():
         args.warm_start = "learned" if os.path.exists(MODEL) else "node"
     if args.impl == "reference":
         run_reference_arm(args)
+    elif args.scene != "block":
+        print(json.dumps(run_scene_leg(args)), flush=True)
     elif args.train_only:
         import torch
 

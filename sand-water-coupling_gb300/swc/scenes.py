@@ -241,25 +241,53 @@ def dam_break_3d_variant(seed: int, height: float, target_particles: int = 400_0
                         domain=(dom_x, dom_yz, dom_yz))
 
 
-def paddle_tank_3d(seed: int = 0, spacing: float = 0.01, cells=(256, 128, 256),
+def paddle_tank_3d(seed: int = 0, spacing: float = 0.01, n_fluid: int = 8_388_608, cells=None,
                    domain=(4.0, 2.0, 2.0), paddle_particles: int = 1_000_000,
-                   paddle_half=(0.25, 0.05, 0.5), omega: float = 2.0, steps: int = 100) -> Scene:
-    """Largest scene: tank [0,4]x[0,2]x[0,2], 256 x 128 x 256 = 8,388,608 fluid
-    particles at spacing 0.01 (seeded jitter), walls of two layers, and about 1M
-    solid particles sampled uniformly inside a 0.5 x 0.1 x 1.0 paddle centred in the
-    tank, rotating at 2 rad/s about the vertical (y) axis.  Paddle particles carry
-    the rigid velocity omega x (x - c); their normals point away from the paddle's
-    mid-plane."""
+                   paddle_half=(0.05, 0.5, 0.25), omega: float = 2.0, steps: int = 100) -> Scene:
+    """Largest scene: tank [0,4]x[0,2]x[0,2] (y up) filled from the floor with
+    n_fluid = 8,388,608 fluid particles on the lattice of spacing 0.01 (400 x 200
+    points per layer, about 105 layers, the top one partial) with seeded +-1e-4
+    jitter, walls of two layers, and about 1M solid particles sampled uniformly
+    inside a paddle blade centred in the tank, 0.1 thick (x) x 1.0 tall (y) x 0.5
+    wide (z), rotating at 2 rad/s about the vertical (y) axis through its centre.
+    Paddle particles carry the rigid velocity omega x (x - c); their normals point
+    away from the blade's mid-plane (along x before rotation).  Lattice points inside
+    the blade are left out and further points fill the count.
+
+    `cells` instead places a block of that many lattice points in the tank's
+    corner (small test tanks).  The fluid must lie inside the tank: particles
+    beyond its walls would sit outside the node lattice."""
     rng = np.random.default_rng(seed)
-    pos = lattice_block(cells, spacing)
-    pos = pos + rng.uniform(-1e-4, 1e-4, size=pos.shape)
-    vel = np.zeros_like(pos)
     dom = tuple(int(round(d / spacing)) for d in domain)
+    c = np.array(domain, dtype=np.float64) / 2
+    ph = np.asarray(paddle_half, dtype=np.float64)
+
+    def outside_blade(p):
+        return ~np.all(np.abs(p - c) < ph + spacing / 2, axis=1)
+
+    if cells is not None:
+        if any(int(n) > d for n, d in zip(cells, dom)):
+            raise ValueError(f"fluid block {tuple(cells)} does not fit the tank's {dom} lattice cells")
+        pos = lattice_block(cells, spacing)
+        pos = pos + rng.uniform(-1e-4, 1e-4, size=pos.shape)
+        pos = pos[outside_blade(pos)]
+    else:
+        layer = lattice_block((dom[0], 1, dom[2]), spacing)  # one y layer, x fastest
+        parts, count, k = [], 0, 0
+        while count < n_fluid:
+            if k >= dom[1]:
+                raise ValueError(f"{n_fluid} fluid particles do not fit the tank")
+            pts = layer + np.array([0.0, k * spacing, 0.0])
+            pts = pts[outside_blade(pts)]
+            parts.append(pts)
+            count += pts.shape[0]
+            k += 1
+        pos = np.concatenate(parts)[:n_fluid]
+        pos = pos + rng.uniform(-1e-4, 1e-4, size=pos.shape)
+    vel = np.zeros_like(pos)
     wpos, wnrm = box_wall_layers(dom, spacing, 2)
-    c = np.array(domain) / 2
-    ph = np.asarray(paddle_half)
     ppos = c + rng.uniform(-1.0, 1.0, size=(paddle_particles, 3)) * ph
-    # outward normal of the thin paddle slab along its thin axis (x before rotation)
+    # outward normal of the blade along x (its thin axis at the default size)
     pn = np.zeros_like(ppos)
     pn[:, 0] = np.sign(ppos[:, 0] - c[0])
     pn[pn[:, 0] == 0, 0] = 1.0
@@ -267,9 +295,6 @@ def paddle_tank_3d(seed: int = 0, spacing: float = 0.01, cells=(256, 128, 256),
     rel = ppos - c
     pvel[:, 0] = omega * rel[:, 2]
     pvel[:, 2] = -omega * rel[:, 0]
-    # drop fluid particles inside the paddle
-    keep = ~np.all(np.abs(pos - c) < ph + spacing / 2, axis=1)
-    pos, vel = pos[keep], vel[keep]
     bpos = np.concatenate([wpos, ppos])
     bnrm = np.concatenate([wnrm, pn])
     bvel = np.concatenate([np.zeros_like(wpos), pvel])

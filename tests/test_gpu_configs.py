@@ -13,9 +13,10 @@ GPU's to 1e-6) it projects the GPU's moved positions (see replay).
   3D dam break, 524,288 particles: one step after 10 advances, same start.
   isolated projection block, 128^3 = 2,097,152 particles: one step after 5
       advances with the learned warm start the benchmark runs.
-  paddle tank, 8.4M particles with a 1M-particle rotating paddle: one step after
-      3 advances with the learned warm start (a smaller tank when the host has no
-      room for the oracle's 6.9M-row operator; the size is printed).
+  paddle tank, 8,388,608 particles filling the tank from the floor with a
+      1M-particle rotating paddle blade: one step after 3 advances with the learned
+      warm start (a smaller tank when the host has no room for the oracle's
+      ~8.9M-row operator; the size is printed).
 
 For the learned steps the oracle's CG starts from the GPU's solution: its FP64
 residual must already be near the tolerance (the oracle then adds a few
@@ -166,10 +167,10 @@ def test_projection_block_2m(swc_mod, oracle_mod):
 
 
 def test_paddle_tank(swc_mod, oracle_mod):
-    # the oracle's operator holds ~3.1 kB per active node (6.9M nodes at full size)
+    # the oracle's operator holds ~3.1 kB per active node (about 8.9M nodes at full size)
     full = mem_available_gb() >= 64
-    kw = {} if full else dict(cells=(128, 64, 128), domain=(2.0, 1.0, 1.0), paddle_particles=125_000,
-                              paddle_half=(0.125, 0.025, 0.25))
+    kw = {} if full else dict(n_fluid=1_048_576, domain=(2.0, 1.0, 1.0), paddle_particles=125_000,
+                              paddle_half=(0.025, 0.25, 0.125))
     s = scenes.paddle_tank_3d(seed=0, **kw).rounded_to_float32()
     label = f"paddle tank {s.n_particles} particles, {s.n_boundary} boundary ({'full size' if full else 'reduced'})"
     liq = swc_mod.DualParticleSphLiquid(s, warm_start="learned", learned_gate=2, keep_virtual_velocity=True)
