@@ -603,6 +603,25 @@ def run_gpu_arm(args):
                            "cg_iterations_mean": float(np.mean(its))}
             l2.close()
 
+    # Whole-step HBM roofline per warm-start form, on the algorithmic bytes of one
+    # step (each array once per pass; FP32 state): binning 92 N, rho_i 20 N,
+    # viscosity + gravity 48 N, node activation 12 per lattice node, the fused
+    # gather 36 (N + N_b) + 16 N_v, alpha_hat 8 N_v, CG 52 N_v per iteration
+    # (SpMV + dot 16, x/r update 24, direction 12), the pressure gradient
+    # 48 N + 8 N_v + 36 N_b.  The network's 28 N_v on the steps it runs is left out.
+    def step_bytes(cg_its):
+        return (92 + 20 + 48 + 48) * n + 12 * scene.n_nodes + 36 * (n + nb) + (16 + 8 + 8) * nv + 36 * nb + \
+            52 * nv * cg_its
+    step_roof = {"bytes_model": "92N + 20N + 48N + 12 N_nodes + 36(N+N_b) + 16N_v + 8N_v + 52 N_v x iterations "
+                                "+ 48N + 8N_v + 36N_b (FP32 state, each array once per pass)",
+                 "n_nodes": scene.n_nodes}
+    for form, sps, its in [(args.warm_start, value / ws, float(np.mean(iters)))] + \
+            [(k, v["steps_per_s"], v["cg_iterations_mean"]) for k, v in forms.items()]:
+        b = step_bytes(its)
+        step_roof[form] = {"bytes_per_step": b, "GBps": b * sps / 1e9, "frac": b * sps / 1e9 / hbm,
+                           "cg_iterations_mean": its}
+    roofline["step"] = step_roof
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_reference(args, steps=args.cpu_steps, warmup=1, policy=True)
