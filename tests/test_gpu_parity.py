@@ -125,6 +125,63 @@ def test_moving_paddle_parity(swc_mod, oracle_mod):
         assert rel(v, vr) < TOL_V, (step, rel(v, vr))
 
 
+def scene_with_outliers():
+    """block_3d_n16 with 30 particles moved outside the node lattice: 24 far beyond
+    each face (no neighbours) and 6 within 0.3 spacings of a face, in reach of the
+    border nodes (both sides clamp them into the border cells of their grids)."""
+    sc = scenes.projection_block_3d(n=16, seed=6)
+    o = np.asarray(sc.grid_origin[:3])
+    hi = o + (np.asarray(sc.grid_size[:3]) - 1) * sc.grid_spacing
+    mid = (o + hi) / 2
+    x = sc.positions.copy()
+    rng = np.random.default_rng(6)
+    k = 0
+    for axis in range(3):
+        for side, edge in ((-1, o[axis]), (1, hi[axis])):
+            for _ in range(4):
+                p = mid + rng.uniform(-0.05, 0.05, 3)
+                p[axis] = edge + side * rng.uniform(0.05, 0.2)
+                x[k] = p
+                k += 1
+            p = mid + rng.uniform(-0.05, 0.05, 3)
+            p[axis] = edge + side * 0.3 * sc.grid_spacing
+            x[k] = p
+            k += 1
+    sc.positions = x
+    return sc
+
+
+def test_particles_outside_the_lattice(swc_mod, oracle_mod):
+    """Particles beyond the node lattice (escaped past the walls) sit in the border
+    cells on the GPU: the same neighbour sets, virtual sets and velocities as the
+    oracle over three steps."""
+    s, liq, ref = make_pair(swc_mod, oracle_mod, scene_with_outliers())
+    for step in range(3):
+        sync_oracle(liq, ref)
+        ref.set_pressure(liq.virtual()["p"] if step else np.zeros(0))
+        st = liq.advance(s.dt)
+        ref.advance(s.dt)
+        assert st["status"] == 0
+        gv, ov = liq.virtual(), ref.virtual()
+        assert np.array_equal(gv["node"], ov["node"]), "active virtual sets differ"
+        np.testing.assert_allclose(gv["rho"], ov["rho"], rtol=2e-5, atol=1e-6 * np.abs(ov["rho"]).max())
+        x, v = liq.getParticles()
+        xr, vr = ref.particles()
+        np.testing.assert_allclose(x, xr, rtol=0, atol=1e-6)
+        assert rel(v, vr) < TOL_V, (step, rel(v, vr))
+        outer = np.arange(30)  # the outliers keep their rows (ids) in getParticles
+        assert rel(v[outer], vr[outer]) < TOL_V, (step, rel(v[outer], vr[outer]))
+    for which in ("real", "boundary", "virtual"):
+        cg, og, ig = liq.neighbors(which, x[:30])
+        co, oo, io = ref.neighbors(which, x[:30])
+        assert np.array_equal(cg, co), which
+        if which == "virtual":
+            io = ref.virtual()["node"][io]
+            for t in range(30):
+                io[oo[t]:oo[t + 1]].sort()
+        assert np.array_equal(ig, io), which
+
+
 @pytest.mark.parametrize("name", ["dam_break_2d", "block_3d_n16"])
 def test_neighbour_sets_exact(swc_mod, oracle_mod, name):
     s, liq, ref = make_pair(swc_mod, oracle_mod, SCENES[name]())
