@@ -631,10 +631,11 @@ def run_gpu_arm(args):
         sand = run_sand_leg(args, torch, stream, hbm, peak_kind, with_cpu=rank == 0 and ws == 1 and not args.no_cpu)
 
     # kernels launched per step (counted in the ncu launch list of this workload):
-    # binning 10 (count, three scan passes, scatter, segment sort, permute), density 2,
-    # viscosity 2, brick marking and lists 3, gather 1, segment count + scan 4, alpha_hat 1,
-    # warm start 1, CG start 3, 3 per CG iteration, gradient 1; a step that evaluates the
-    # network adds 4 more (not counted here, so this is a lower bound)
+    # binning 7 (count, three scan passes, scatter, segment sort, permute), density 2,
+    # viscosity 2, virtual generation 8 (brick marking, two brick lists, gather, segment
+    # count and its three scan passes), alpha_hat 1, warm start 1, CG start 3, 3 per CG
+    # iteration, gradient 1; a step that evaluates the network adds 4 more (not counted
+    # here, so this is a lower bound)
     launches_per_step = 25 + 3 * float(np.mean(iters))
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
