@@ -139,7 +139,7 @@ def dist_setup():
         import torch
         import torch.distributed as dist
 
-        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        backend = os.environ.get("SWC_DIST_BACKEND") or ("nccl" if torch.cuda.is_available() else "gloo")
         if backend == "nccl":
             torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group(backend=backend)
@@ -161,6 +161,12 @@ def reduce_max(dist, value):
 def barrier(dist):
     if dist is not None:
         dist.barrier()
+
+
+def replica_value(ws, steps, ms_max):
+    """Whole-job steps/s of `ws` independent replicas that each ran `steps` steps, the
+    slowest taking `ms_max` milliseconds (replicas only: the path does not shard)."""
+    return ws * steps / (ms_max / 1e3)
 
 
 def cpu_reference(args, steps=2, warmup=1, policy=False, time_cap=None):
@@ -469,7 +475,7 @@ def run_gpu_arm(args):
     barrier(dist)
     ms = e0.elapsed_time(e1)
     ms_max = reduce_max(dist, ms)
-    value = ws * args.steps / (ms_max / 1e3)
+    value = replica_value(ws, args.steps, ms_max)
     nv = st["n_virtual"]
     if args.profile_run:
         # minimal run for profiler captures: the timed steps only
