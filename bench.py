@@ -668,7 +668,9 @@ def run_scene_leg(args):
     from swc import learn, scenes
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    scene = scenes.dam_break_3d(seed=args.seed) if args.scene == "dam_break_3d" else scenes.paddle_tank_3d(seed=args.seed)
+    build = {"dam_break_2d": scenes.dam_break_2d, "dam_break_3d": scenes.dam_break_3d,
+             "paddle_tank": scenes.paddle_tank_3d}[args.scene]
+    scene = build(seed=args.seed)
     stream = torch.cuda.Stream()
     forms = {}
     for warm in ("node", "extrapolate", "learned"):
@@ -732,9 +734,10 @@ def main():
     ap.add_argument("--training", type=int, default=1, help="also time the learned warm start's training path")
     ap.add_argument("--train-rows", dest="train_rows", type=int, default=65536,
                     help="rows of the timed loss-gradient pass")
-    ap.add_argument("--scene", default="block", choices=["block", "dam_break_3d", "paddle_tank"],
+    ap.add_argument("--scene", default="block", choices=["block", "dam_break_2d", "dam_break_3d", "paddle_tank"],
                     help="block: the benchmark; the others print the throughput of that configuration "
-                         "(3D dam break, 524,288 particles; paddle tank, 8,388,608 particles with a rotating paddle)")
+                         "(2D dam break, 3,200 particles; 3D dam break, 524,288 particles; paddle tank, "
+                         "8,388,608 particles with a rotating paddle)")
     ap.add_argument("--train-only", dest="train_only", action="store_true",
                     help="only the loss-gradient pass on --train-rows rows (for profiler captures)")
     args = ap.parse_args()
