@@ -230,8 +230,9 @@ void swc_trainer_destroy(swc_trainer * tr);
 int  swc_trainer_add(swc_trainer * tr, const float * features, const float * targets, int64_t n);
 int  swc_trainer_set_params(swc_trainer * tr, const float * params, const float * norm);
 int  swc_trainer_get_params(swc_trainer * tr, float * params, float * norm);
-/* `epochs` passes over the shuffled dataset (seeded); epoch_loss[e] = mean squared
- * error of the normalised output after epoch e. */
+/* `epochs` passes over the dataset, each in a pseudo-random row order computed on the
+ * device (a Feistel permutation keyed by `seed` and the epoch); epoch_loss[e] = mean
+ * squared error of the normalised output after epoch e, over the whole dataset. */
 int  swc_trainer_fit(swc_trainer * tr, int32_t epochs, float lr, uint64_t seed, float * epoch_loss);
 /* Stateless helpers on host arrays (run on the GPU): predictions, and the loss
  * gradient for one batch (the mean squared error of the normalised output in *loss). */

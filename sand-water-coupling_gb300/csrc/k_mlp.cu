@@ -354,15 +354,68 @@ __global__ void k_node_features(NodeArrays N, const int * __restrict__ slot_of, 
 }
 
 // Batch gather for training: dst[i] = src[idx[i]] (kMlpIn features), dst_t[i] = src_t[idx[i]].
-__global__ void k_gather_rows(const float * __restrict__ src, const float * __restrict__ src_t,
-                              const int * __restrict__ idx, long long n, float * __restrict__ dst,
-                              float * __restrict__ dst_t) {
-    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
-        const long long j = idx[i];
+// Pseudo-random permutation of [0, n) for the training epochs: a four-round
+// Feistel network on 2 x half bits (Luby-Rackoff; round function a 32-bit integer
+// mixer, the "lowbias32" constants of C. Wellons' hash-prospector), walking the
+// cycle until the value falls inside [0, n) (at most 4 n / n on average).
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+__device__ __forceinline__ uint32_t feistel(uint32_t x, int half, uint4 key) {
+    const uint32_t mask = (1u << half) - 1u;
+    uint32_t l = x >> half, r = x & mask;
+    const uint32_t k[4] = {key.x, key.y, key.z, key.w};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const uint32_t t = l ^ (mix32(r ^ k[i]) & mask);
+        l = r;
+        r = t;
+    }
+    return (l << half) | r;
+}
+__device__ __forceinline__ long long shuffled(long long i, long long n, int half, uint4 key) {
+    uint32_t x = uint32_t(i);
+    do {
+        x = feistel(x, half, key);
+    } while (x >= uint32_t(n));
+    return x;
+}
+
+// Rows b0 .. b0 + nb - 1 of the epoch's permutation of the n dataset rows into
+// the batch buffers.
+__global__ void k_gather_shuffled(const float * __restrict__ src, const float * __restrict__ src_t, long long n,
+                                  long long b0, long long nb, int half, uint4 key, float * __restrict__ dst,
+                                  float * __restrict__ dst_t) {
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < nb; i += (long long) gridDim.x * blockDim.x) {
+        const long long j = shuffled(b0 + i, n, half, key);
 #pragma unroll
         for (int k = 0; k < kMlpIn; k++) dst[i * kMlpIn + k] = src[j * kMlpIn + k];
         dst_t[i] = src_t[j];
     }
+}
+
+// Per-block sums of ((pred - target) / t_std)^2 in FP64 (the epoch loss; the host
+// adds the block sums in order).
+__global__ void __launch_bounds__(256) k_sq_err(const float * __restrict__ pred, const float * __restrict__ tgt,
+                                                long long n, float inv_tstd, double * __restrict__ part) {
+    __shared__ double sm[256];
+    double s = 0;
+    for (long long i = blockIdx.x * 256LL + threadIdx.x; i < n; i += gridDim.x * 256LL) {
+        const double d = (double(pred[i]) - double(tgt[i])) * double(inv_tstd);
+        s += d * d;
+    }
+    sm[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
 }
 
 // ---------------------------------------------------------------------------
@@ -376,10 +429,15 @@ void launch_node_features(const NodeArrays & N, const int * slot_of, const int *
     k_node_features<<<int(std::min<long long>((rows_max + 255) / 256, 152 * 8)), 256, 0, st>>>(N, slot_of, nv, cg, F,
                                                                                              feat_out);
 }
-void launch_gather_rows(const float * src, const float * src_t, const int * idx, long long n, float * dst,
-                        float * dst_t, cudaStream_t st) {
-    if (n <= 0) return;
-    k_gather_rows<<<int(std::min<long long>((n + 255) / 256, 152 * 8)), 256, 0, st>>>(src, src_t, idx, n, dst, dst_t);
+void launch_gather_shuffled(const float * src, const float * src_t, long long n, long long b0, long long nb, int half,
+                            const unsigned * key, float * dst, float * dst_t, cudaStream_t st) {
+    if (nb <= 0) return;
+    k_gather_shuffled<<<int(std::min<long long>((nb + 255) / 256, 152 * 8)), 256, 0, st>>>(
+        src, src_t, n, b0, nb, half, make_uint4(key[0], key[1], key[2], key[3]), dst, dst_t);
+}
+void launch_sq_err(const float * pred, const float * tgt, long long n, float inv_tstd, double * part, int blocks,
+                   cudaStream_t st) {
+    k_sq_err<<<blocks, 256, 0, st>>>(pred, tgt, n, inv_tstd, part);
 }
 // Resident CTAs per SM of a forward instantiation, capped by TMEM (a CTA that
 // found its columns taken would wait in tcgen05.alloc).  When shared memory and

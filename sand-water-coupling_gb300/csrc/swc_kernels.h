@@ -231,8 +231,13 @@ void launch_slot_of(const Lattice & L, const BrickArrays & B, const NodeArrays &
 void launch_mlp_targets(long long rows_max, const int * nv, const int * slot_of, const float * x, const float * prev,
                         const float * xm1, const float * d2p, const float * ahat, const CgState * cg, float * target,
                         cudaStream_t st);
-void launch_gather_rows(const float * src, const float * src_t, const int * idx, long long n, float * dst,
-                        float * dst_t, cudaStream_t st);
+// Rows b0 .. b0 + nb - 1 of a pseudo-random permutation of the n rows (a Feistel
+// network on 2 x half bits, 2^(2 half) >= n, keyed by key[4]) into dst / dst_t.
+void launch_gather_shuffled(const float * src, const float * src_t, long long n, long long b0, long long nb, int half,
+                            const unsigned * key, float * dst, float * dst_t, cudaStream_t st);
+// Per-block FP64 sums of ((pred - tgt) * inv_tstd)^2 over n rows into part[blocks].
+void launch_sq_err(const float * pred, const float * tgt, long long n, float inv_tstd, double * part, int blocks,
+                   cudaStream_t st);
 
 // ---- host-side allocation fault injection (tests of the failure paths) ----
 // True when the device allocation about to be made is the one armed by

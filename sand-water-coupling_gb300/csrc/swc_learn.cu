@@ -5,8 +5,7 @@
 // tcgen05 BF16 products with FP32 accumulation) and an Adam step.
 #include <algorithm>
 #include <cstring>
-#include <numeric>
-#include <random>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -16,7 +15,8 @@
 using namespace swc;
 
 namespace {
-constexpr int kP = SWC_MLP_PARAMS, kN = SWC_MLP_NORM, kH = 64, kIn = SWC_MLP_IN;
+constexpr int kP = SWC_MLP_PARAMS, kN = SWC_MLP_NORM, kIn = SWC_MLP_IN;
+constexpr int kLossBlocks = 512;  // block sums of the epoch loss
 }
 
 struct swc_trainer {
@@ -26,9 +26,11 @@ struct swc_trainer {
     float *feat = nullptr, *tgt = nullptr;                       // dataset
     float *params = nullptr, *norm = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr;
     float *bfeat = nullptr, *btgt = nullptr, *pred = nullptr;    // batch
+    float * fpred = nullptr;                                     // predictions of the whole dataset (epoch loss)
+    double * part = nullptr;                                     // block sums of the epoch loss
     float *share = nullptr, *loss = nullptr;                     // per-CTA gradient shares, batch loss
     int    ctas  = 1;
-    int *  idx = nullptr, *err = nullptr;
+    int *  err = nullptr;
     long long adam_t = 0;
 };
 
@@ -77,7 +79,7 @@ int swc_trainer_create(int64_t capacity, int32_t batch, swc_trainer ** out) {
          talloc(&t->norm, kN) && talloc(&t->m, kP) && talloc(&t->v, kP) && talloc(&t->grad, kP) &&
          talloc(&t->bfeat, B * kIn) && talloc(&t->btgt, B) && talloc(&t->pred, B) &&
          talloc(&t->share, mlp_train_share_floats(t->ctas)) && talloc(&t->loss, 1) &&
-         talloc(&t->idx, size_t(capacity)) && talloc(&t->err, 1);
+         talloc(&t->part, kLossBlocks) && talloc(&t->err, 1);
     if (!ok) {
         swc_trainer_destroy(t);
         return SWC_OUT_OF_MEMORY;
@@ -94,9 +96,9 @@ void swc_trainer_destroy(swc_trainer * t) {
     if (!t) return;
     if (t->st) cudaStreamSynchronize(t->st);
     for (float ** p : {&t->feat, &t->tgt, &t->params, &t->norm, &t->m, &t->v, &t->grad, &t->bfeat, &t->btgt, &t->pred,
-                       &t->share, &t->loss})
+                       &t->fpred, &t->share, &t->loss})
         tfree(*p);
-    tfree(t->idx);
+    tfree(t->part);
     tfree(t->err);
     if (t->st) cudaStreamDestroy(t->st);
     delete t;
@@ -135,42 +137,48 @@ int swc_trainer_get_params(swc_trainer * t, float * params, float * norm) {
 
 int swc_trainer_fit(swc_trainer * t, int32_t epochs, float lr, uint64_t seed, float * epoch_loss) {
     if (!t || epochs < 0 || t->n <= 0) return SWC_BAD_ARG;
-    std::mt19937_64 rng(seed);
-    std::vector<int> perm(t->n);
-    std::vector<float> pred_h, tgt_h(t->n), norm_h(kN);
-    cudaMemcpy(tgt_h.data(), t->tgt, sizeof(float) * t->n, cudaMemcpyDeviceToHost);
-    cudaMemcpy(norm_h.data(), t->norm, sizeof(float) * kN, cudaMemcpyDeviceToHost);
+    if (t->n >= (1LL << 31)) return SWC_BAD_ARG;
+    // each epoch visits the rows in a pseudo-random order computed on the device (a
+    // keyed Feistel permutation, keys from the seed and the epoch by splitmix64)
+    int half = 0;
+    while ((1LL << (2 * half)) < t->n) half++;
+    uint64_t state = seed;
+    auto splitmix = [&state]() {
+        uint64_t z = (state += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    float norm_h[kN];
+    if (epoch_loss) {
+        if (cudaMemcpy(norm_h, t->norm, sizeof(float) * kN, cudaMemcpyDeviceToHost) != cudaSuccess) return SWC_CUDA_ERROR;
+        if (!t->fpred && !talloc(&t->fpred, size_t(t->cap))) return SWC_OUT_OF_MEMORY;
+    }
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
     for (int e = 0; e < epochs; e++) {
-        std::iota(perm.begin(), perm.end(), 0);
-        std::shuffle(perm.begin(), perm.end(), rng);
-        if (cudaMemcpyAsync(t->idx, perm.data(), sizeof(int) * t->n, cudaMemcpyHostToDevice, t->st) != cudaSuccess)
-            return SWC_CUDA_ERROR;
+        const uint64_t k0 = splitmix(), k1 = splitmix();
+        const unsigned key[4] = {unsigned(k0), unsigned(k0 >> 32), unsigned(k1), unsigned(k1 >> 32)};
         for (long long b0 = 0; b0 < t->n; b0 += t->batch) {
             const long long nb = std::min<long long>(t->batch, t->n - b0);
-            launch_gather_rows(t->feat, t->tgt, t->idx + b0, nb, t->bfeat, t->btgt, t->st);
+            launch_gather_shuffled(t->feat, t->tgt, t->n, b0, nb, half, key, t->bfeat, t->btgt, t->st);
             if (int rc = gradient_batch(t, t->bfeat, t->btgt, nb)) return rc;
             t->adam_t++;
             const float bc1 = 1.f - std::pow(b1, float(t->adam_t)), bc2 = 1.f - std::pow(b2, float(t->adam_t));
             launch_adam(t->params, t->grad, t->m, t->v, kP, lr, b1, b2, eps, bc1, bc2, t->st);
         }
-        if (int rc = check_err(t)) return rc;
         if (epoch_loss) {
-            // loss of the epoch's parameters over the whole dataset
-            pred_h.resize(t->n);
-            for (long long b0 = 0; b0 < t->n; b0 += t->batch) {
-                const long long nb = std::min<long long>(t->batch, t->n - b0);
-                int rc = forward_batch(t, t->feat + b0 * kIn, nb, t->pred);
-                if (rc) return rc;
-                cudaMemcpyAsync(pred_h.data() + b0, t->pred, sizeof(float) * nb, cudaMemcpyDeviceToHost, t->st);
-            }
+            // loss of the epoch's parameters over the whole dataset, on the device
+            if (int rc = forward_batch(t, t->feat, t->n, t->fpred)) return rc;
+            launch_sq_err(t->fpred, t->tgt, t->n, 1.f / norm_h[2 * kIn + 1], t->part, kLossBlocks, t->st);
+            double part[kLossBlocks];
+            if (cudaMemcpyAsync(part, t->part, sizeof(part), cudaMemcpyDeviceToHost, t->st) != cudaSuccess)
+                return SWC_CUDA_ERROR;
             if (int rc = check_err(t)) return rc;
             double s = 0;
-            for (long long i = 0; i < t->n; i++) {
-                const double d = (double(pred_h[i]) - tgt_h[i]) / norm_h[2 * kIn + 1];
-                s += d * d;
-            }
+            for (int b = 0; b < kLossBlocks; b++) s += part[b];
             epoch_loss[e] = float(s / double(t->n));
+        } else if (int rc = check_err(t)) {
+            return rc;
         }
     }
     return cudaGetLastError() == cudaSuccess ? SWC_OK : SWC_CUDA_ERROR;
